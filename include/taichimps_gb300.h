@@ -1,0 +1,231 @@
+/*
+ * taichimps_gb300 — C ABI of the GB300 (sm_103a) granular-DEM contact path.
+ *
+ * Every entry point takes plain device pointers owned by the caller (the
+ * library never allocates or frees caller memory), a stream, and returns an
+ * int: TMPS_OK, or TMPS_ERR_BAD_ARG / TMPS_ERR_CUDA for a launch that could
+ * not be made.  Launches are asynchronous on the given stream.  Errors found
+ * on the device (a neighbor row that overflowed, a non-finite position, a box
+ * driven non-positive) are OR-ed into the caller's `int32_t* status` word,
+ * which the host reads when it synchronises anyway (rebuilds, output, the end
+ * of a run) — the same places the reference raises.
+ *
+ * Layout (internal atom order; the neighbor build re-sorts atoms by cell):
+ *   xr  double[n][4]  x, y, z, radius
+ *   vm  double[n][4]  vx, vy, vz, mass
+ *   om  double[n][4]  wx, wy, wz, moment of inertia 0.4*m*r*r
+ *   f, torque  double[3][n]   (component-major)
+ *   virial     double[6][n]   [xx, yy, zz, xy, xz, yz], optional
+ *   nbr    int32[slots][n]    full neighbor list, slot-major
+ *   shear  double[3][slots][n] per-slot shear, in the row atom's i->j sense
+ *   touch  uint64[n]          bit k set while slot k is in contact
+ *
+ * Each declaration names the reference interface it replaces
+ * (taichimps, path within the project, file:line).
+ */
+#ifndef TAICHIMPS_GB300_H
+#define TAICHIMPS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    TMPS_OK = 0,
+    TMPS_ERR_BAD_ARG = 1,
+    TMPS_ERR_CUDA = 2,
+};
+
+/* Bits of the device status word. */
+enum {
+    TMPS_STATUS_NLIST_OVERFLOW = 1,   /* a row needed more than `slots` entries */
+    TMPS_STATUS_NONFINITE = 2,        /* a position became NaN/Inf */
+    TMPS_STATUS_BOX_NONPOSITIVE = 4,  /* the servo drove a box length <= 0 */
+    TMPS_STATUS_CELL_OVERFLOW = 8,    /* grid larger than the cell buffers */
+};
+
+/* Device-resident box: written by the host (tmps_box_set) or by the servo
+ * kernel, read by every kernel.  Replaces the zero-dimensional box fields of
+ * Domain (src/taichimps/domain.py:55-68, _sync_kernel :188-233). */
+typedef struct tmps_box {
+    double lo[3];
+    double hi[3];
+    double prd[3];
+    double inv_prd[3];  /* 1/prd, kept beside prd so no kernel divides per thread */
+    double h_rate[6];   /* box length rates [x, y, z, yz, xz, xy] */
+    int32_t per[3];
+    int32_t vremap;     /* remap v: partner velocity shift across images */
+    /* neighbor grid, fixed at the last build */
+    int32_t g[3];
+    int32_t ncell;
+    double csize[3];    /* lamda bin size 1/g */
+    double hcell[3];    /* Cartesian bin size prd/g (follows the box) */
+    /* box as it was before the last servo update (remap x reads it) */
+    double old_lo[3];
+    double old_prd[3];
+    int32_t remap_pending;
+    int32_t pad_;
+} tmps_box;
+
+/* Per-atom storage (pointers into caller memory). */
+typedef struct tmps_atoms {
+    int32_t n;
+    int32_t pad_;
+    double* xr;
+    double* vm;
+    double* om;
+    double* f;
+    double* torque;
+    double* virial;     /* may be NULL */
+    int32_t* tag;
+    int32_t* uid;       /* insertion index of each internal slot */
+    double* x0;         /* double[3][n]: positions at the last build */
+    /* mixed-precision mirrors (may be NULL in the FP64 form) */
+    float* pos32;       /* float[n][4]: offset from cell origin, radius */
+    int32_t* cell32;    /* cell coordinate, cx | cy << 10 | cz << 20 */
+    float* vel32;       /* float[n][4]: v, mass */
+    float* om32;        /* float[n][4]: omega, inertia */
+    float* f32;         /* float[3][n] contact force, mixed form */
+    float* torque32;    /* float[3][n] */
+} tmps_atoms;
+
+/* Full neighbor list with its contact history. */
+typedef struct tmps_nlist {
+    int32_t n;
+    int32_t slots;
+    int32_t* nbr;
+    int32_t* nnb;
+    uint64_t* touch;
+    double* shear;
+} tmps_nlist;
+
+/* Contact law.  style: 0 gran/hooke, 1 gran/hooke/history, 2 gran/hertz,
+ * 3 gran/hertz/history, 4 granular.  Model ids for granular follow
+ * src/taichimps/GRANULAR/granular.py:50-64. */
+typedef struct tmps_pair_params {
+    int32_t style;
+    int32_t normal_id;
+    int32_t damping_id;
+    int32_t tangential_id;
+    int32_t limit_damping;
+    int32_t pad_;
+    double kn, kt, gamman, gammat, xmu;
+    double damp, xt, mu;
+} tmps_pair_params;
+
+/* Pressure servo / strain control for x, y, z (orthogonal box).
+ * Styles: 0 none, 1 erate, 2 trate, 3 vel, 4 wiggle, 5 final, 6 delta,
+ * 7 scale, 8 pressure, 9 pressure/mean (deform_pressure.py:76-82). */
+typedef struct tmps_servo {
+    int32_t style[3];
+    int32_t couple;     /* 0 none, 1 xyz, 2 xy, 3 yz, 4 xz */
+    int32_t normalize;
+    int32_t remap;      /* 0 none, 1 x, 2 v */
+    double max_rate;
+    double rate[3], vel[3], scale[3], flo[3], fhi[3], dlo[3], dhi[3];
+    double amp[3], tper[3], ptarget[3], pgain[3];
+    double lo_start[3], hi_start[3];
+    double cum[3];      /* cumulative shift of pressure-controlled axes */
+    double pressure[6]; /* last pressure tensor servoed on (output) */
+} tmps_servo;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* Version and build identity; no reference counterpart. */
+const char* tmps_version(void);
+
+/* Copies a host box into device memory (Domain._sync, domain.py:235-254). */
+int tmps_box_set(tmps_box* d_box, const tmps_box* h_box, void* stream);
+
+/* ---- integrator / fixes ----------------------------------------------- */
+
+/* FixNVESphere.initial_integrate (src/taichimps/EXTRA_FIX/nve_sphere.py:100-133,155-162). */
+int tmps_verlet_initial(const tmps_atoms* a, double dt, void* stream);
+
+/* FixNVESphere.final_integrate (src/taichimps/EXTRA_FIX/nve_sphere.py:135-153,164-171). */
+int tmps_verlet_final(const tmps_atoms* a, double dt, void* stream);
+
+/* AtomSystem.clear_forces (src/taichimps/atom.py:201-220). */
+int tmps_clear_forces(const tmps_atoms* a, void* stream);
+
+/* FixDampingCundall.post_force (src/taichimps/EXTRA_FIX/damping_cundall.py:206-234). */
+int tmps_damping_cundall(const tmps_atoms* a, double gamma_lin, double gamma_ang, void* stream);
+
+/* NeighborList.check_displacement (src/taichimps/neighbor.py:214-245).
+ * Sets *d_flag (device int32) to `stamp` when some atom moved more than
+ * half the skin since the last build. */
+int tmps_skin_check(const tmps_atoms* a, double trigger_sq, int32_t stamp, int32_t* d_flag,
+                    void* stream);
+
+/* Domain.pbc (src/taichimps/domain.py:560-584): wrap, plus the remap-v kick. */
+int tmps_pbc(const tmps_atoms* a, const tmps_box* d_box, void* stream);
+
+/* ---- neighbor list and contact history -------------------------------- */
+
+/* Scratch size (bytes) tmps_nlist_build needs for n atoms and ncell cells. */
+int64_t tmps_nlist_workspace_bytes(int32_t n, int32_t ncell);
+
+/* NeighborList.build (src/taichimps/neighbor.py:247-369,414-435): bins atoms
+ * by cell in lamda coordinates (grid g/csize already in d_box, `ncell` =
+ * gx*gy*gz), sorts them by cell (cells in Morton order, insertion order
+ * within a cell), permutes every per-atom array from `src` into `dst`, and
+ * builds the full list into `nl` (cut (ri + rj + skin)^2, exact FP64).
+ * `order` (int32[n]) receives, for each new slot, the old internal index;
+ * `cell_rank` (int32[ncell]) is the Morton rank of each linear cell id;
+ * `cell_of` (int32[n]) receives each atom's linear cell id in the new order.
+ * Row overflow sets TMPS_STATUS_NLIST_OVERFLOW in *d_status. */
+int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_box* d_box,
+                     int32_t ncell, double skin, const int32_t* cell_rank, int32_t* order,
+                     int32_t* cell_of, const tmps_nlist* nl, void* workspace,
+                     int64_t workspace_bytes, int32_t* d_status, void* stream);
+
+/* ContactHistory.save_state + restore_state (src/taichimps/contact_history.py:91-153):
+ * carries every touching contact of the old list onto the new list, keyed by
+ * the partner's identity, zeroing the rest.  `order` maps new -> old index. */
+int tmps_history_remap(const tmps_nlist* old_nl, const tmps_nlist* new_nl, const int32_t* order,
+                       void* stream);
+
+/* ---- contact force ------------------------------------------------------ */
+
+/* GranularPair.compute for every style (src/taichimps/GRANULAR/base.py:25-38,
+ * hooke.py:52-173, hooke_history.py:108-255, hertz.py:46-148,
+ * hertz_history.py:57-193, granular.py:282-452): full list, one thread per
+ * atom, no atomics; each contact is evaluated in one fixed orientation
+ * (lower internal index first) by both of its atoms, so the two copies of
+ * its shear stay exact negatives.  accumulate != 0 adds into
+ * f/torque/virial (the reference's atomic_add semantics); 0 overwrites
+ * them (clear_forces fused in). */
+int tmps_contact(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box,
+                 const tmps_pair_params* p, double dt, int32_t shearupdate, int32_t accumulate,
+                 void* stream);
+
+/* ---- virial, pressure servo, remap ------------------------------------- */
+
+/* Computes.compute_virial_kernel (src/taichimps/computes/thermo.py:62-109):
+ * sum of the per-atom virial (+ sum m v_a v_b when keflag) into d_out[6]
+ * (device), deterministic order. */
+int tmps_virial_reduce(const tmps_atoms* a, int32_t keflag, double* d_out, void* workspace,
+                       int64_t workspace_bytes, void* stream);
+
+/* Scratch size (bytes) tmps_virial_reduce needs for n atoms. */
+int64_t tmps_virial_workspace_bytes(int32_t n);
+
+/* FixDeformPressure._servo_kernel (src/taichimps/EXTRA_FIX/deform_pressure.py:598-702)
+ * with the host path's styles for x/y/z: pressure from d_virial / volume,
+ * couple, normalize, max/rate, new box into d_box (old box kept in
+ * d_box->old_lo/old_prd and remap_pending set for remap x). */
+int tmps_servo_step(tmps_box* d_box, tmps_servo* d_servo, const double* d_virial, double elapsed,
+                    double frac, double dt, int32_t* d_status, void* stream);
+
+/* FixDeformPressure.remap_positions (src/taichimps/EXTRA_FIX/deform_pressure.py:493-530):
+ * x from the old box's lamda coordinates into the new box; clears
+ * remap_pending. */
+int tmps_remap_x(const tmps_atoms* a, tmps_box* d_box, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAICHIMPS_GB300_H */

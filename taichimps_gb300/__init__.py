@@ -1,0 +1,18 @@
+"""
+taichimps_gb300: the per-step granular-DEM contact path of taichimps, native
+to GB300 (sm_103a CUDA behind a C ABI), behind the reference's own plug-in
+API (pair / fix / neighbor / history / compute classes driven by Simulation).
+"""
+
+from .atom import AtomSystem
+from .computes import Computes
+from .contact_history import ContactHistory
+from .domain import Domain
+from .EXTRA_FIX import Fix, FixDampingCundall, FixDeformPressure, FixNVESphere
+from .GRANULAR import GranHertz, GranHertzHistory, GranHooke, GranHookeHistory, GranularPair, PairGranular
+from .neighbor import NeighborList
+from .simulation import Simulation
+
+__all__ = ["AtomSystem", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
+           "FixDeformPressure", "FixNVESphere", "GranHertz", "GranHertzHistory", "GranHooke",
+           "GranHookeHistory", "GranularPair", "PairGranular", "NeighborList", "Simulation"]

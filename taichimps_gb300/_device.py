@@ -1,0 +1,46 @@
+"""Device plumbing: the CUDA device, the current stream, raw byte buffers."""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("taichimps_gb300 runs on a CUDA device (GB300, sm_103a); none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def lib():
+    device()
+    return _lib.load()
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def struct_buffer(st: ctypes.Structure) -> torch.Tensor:
+    """A device byte buffer the size of a ctypes struct (zeroed)."""
+    return torch.zeros(ctypes.sizeof(st), dtype=torch.uint8, device=device())
+
+
+def push_struct(buf: torch.Tensor, st: ctypes.Structure) -> None:
+    """Host struct -> device buffer, ordered on the current stream."""
+    raw = np.frombuffer(bytes(st), dtype=np.uint8).copy()
+    buf.copy_(torch.from_numpy(raw), non_blocking=False)
+
+
+def pull_struct(buf: torch.Tensor, cls: type[ctypes.Structure]) -> ctypes.Structure:
+    """Device buffer -> host struct (synchronises the stream)."""
+    raw = buf.cpu().numpy().tobytes()
+    return cls.from_buffer_copy(raw)

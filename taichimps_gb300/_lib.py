@@ -1,0 +1,142 @@
+"""
+ctypes binding of ``libtaichimps_gb300.so`` (the C ABI in include/taichimps_gb300.h).
+
+The library is the only compute path: if it is missing, or no CUDA device is
+present, every entry point raises.  There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+from . import build as _build
+
+c_i32 = ctypes.c_int32
+c_f64 = ctypes.c_double
+c_vp = ctypes.c_void_p
+
+
+class Box(ctypes.Structure):
+    """tmps_box"""
+
+    _fields_ = [
+        ("lo", c_f64 * 3), ("hi", c_f64 * 3), ("prd", c_f64 * 3), ("inv_prd", c_f64 * 3),
+        ("h_rate", c_f64 * 6),
+        ("per", c_i32 * 3), ("vremap", c_i32),
+        ("g", c_i32 * 3), ("ncell", c_i32),
+        ("csize", c_f64 * 3), ("hcell", c_f64 * 3),
+        ("old_lo", c_f64 * 3), ("old_prd", c_f64 * 3),
+        ("remap_pending", c_i32), ("pad_", c_i32),
+    ]
+
+
+class Atoms(ctypes.Structure):
+    """tmps_atoms"""
+
+    _fields_ = [
+        ("n", c_i32), ("pad_", c_i32),
+        ("xr", c_vp), ("vm", c_vp), ("om", c_vp), ("f", c_vp), ("torque", c_vp), ("virial", c_vp),
+        ("tag", c_vp), ("uid", c_vp), ("x0", c_vp),
+        ("pos32", c_vp), ("cell32", c_vp), ("vel32", c_vp), ("om32", c_vp), ("f32", c_vp),
+        ("torque32", c_vp),
+    ]
+
+
+class NList(ctypes.Structure):
+    """tmps_nlist"""
+
+    _fields_ = [("n", c_i32), ("slots", c_i32), ("nbr", c_vp), ("nnb", c_vp), ("touch", c_vp),
+                ("shear", c_vp)]
+
+
+class PairParams(ctypes.Structure):
+    """tmps_pair_params"""
+
+    _fields_ = [
+        ("style", c_i32), ("normal_id", c_i32), ("damping_id", c_i32), ("tangential_id", c_i32),
+        ("limit_damping", c_i32), ("pad_", c_i32),
+        ("kn", c_f64), ("kt", c_f64), ("gamman", c_f64), ("gammat", c_f64), ("xmu", c_f64),
+        ("damp", c_f64), ("xt", c_f64), ("mu", c_f64),
+    ]
+
+
+class Servo(ctypes.Structure):
+    """tmps_servo"""
+
+    _fields_ = [
+        ("style", c_i32 * 3), ("couple", c_i32), ("normalize", c_i32), ("remap", c_i32),
+        ("max_rate", c_f64),
+        ("rate", c_f64 * 3), ("vel", c_f64 * 3), ("scale", c_f64 * 3), ("flo", c_f64 * 3),
+        ("fhi", c_f64 * 3), ("dlo", c_f64 * 3), ("dhi", c_f64 * 3),
+        ("amp", c_f64 * 3), ("tper", c_f64 * 3), ("ptarget", c_f64 * 3), ("pgain", c_f64 * 3),
+        ("lo_start", c_f64 * 3), ("hi_start", c_f64 * 3), ("cum", c_f64 * 3),
+        ("pressure", c_f64 * 6),
+    ]
+
+
+TMPS_OK, TMPS_ERR_BAD_ARG, TMPS_ERR_CUDA = 0, 1, 2
+STATUS_NLIST_OVERFLOW, STATUS_NONFINITE, STATUS_BOX_NONPOSITIVE, STATUS_CELL_OVERFLOW = 1, 2, 4, 8
+
+# Every entry point the header declares, with its ctypes signature.
+_SIGS = {
+    "tmps_version": (ctypes.c_char_p, []),
+    "tmps_box_set": (c_i32, [c_vp, ctypes.POINTER(Box), c_vp]),
+    "tmps_verlet_initial": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),
+    "tmps_verlet_final": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),
+    "tmps_clear_forces": (c_i32, [ctypes.POINTER(Atoms), c_vp]),
+    "tmps_damping_cundall": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_f64, c_vp]),
+    "tmps_skin_check": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_i32, c_vp, c_vp]),
+    "tmps_pbc": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
+    "tmps_nlist_workspace_bytes": (ctypes.c_int64, [c_i32, c_i32]),
+    "tmps_nlist_build": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(Atoms), c_vp, c_i32, c_f64,
+                                 c_vp, c_vp, c_vp, ctypes.POINTER(NList), c_vp, ctypes.c_int64,
+                                 c_vp, c_vp]),
+    "tmps_history_remap": (c_i32, [ctypes.POINTER(NList), ctypes.POINTER(NList), c_vp, c_vp]),
+    "tmps_contact": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp,
+                             ctypes.POINTER(PairParams), c_f64, c_i32, c_i32, c_vp]),
+    "tmps_virial_reduce": (c_i32, [ctypes.POINTER(Atoms), c_i32, c_vp, c_vp, ctypes.c_int64, c_vp]),
+    "tmps_virial_workspace_bytes": (ctypes.c_int64, [c_i32]),
+    "tmps_servo_step": (c_i32, [c_vp, c_vp, c_vp, c_f64, c_f64, c_f64, c_vp, c_vp]),
+    "tmps_remap_x": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
+}
+
+_lib: ctypes.CDLL | None = None
+
+
+def lib_path() -> Path:
+    return _build.lib_path()
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load the CUDA library (building it first if it is absent and nvcc is present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = lib_path()
+    if build_if_missing:
+        p = _build.build()
+    if not p.exists():
+        raise RuntimeError(f"taichimps_gb300 CUDA library not found at {p}; run "
+                           "`python -m taichimps_gb300.build` (needs nvcc)")
+    L = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class TmpsError(RuntimeError):
+    pass
+
+
+def check(rc: int, what: str) -> None:
+    if rc != TMPS_OK:
+        kind = {TMPS_ERR_BAD_ARG: "bad argument", TMPS_ERR_CUDA: "CUDA launch failure"}.get(rc, str(rc))
+        raise TmpsError(f"{what} failed: {kind}")
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)

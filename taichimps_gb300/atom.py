@@ -1,0 +1,253 @@
+"""
+Per-atom state of atom_style sphere, held in device tensors.
+
+Mirrors taichimps ``AtomSystem`` (src/taichimps/atom.py:13-220).  Storage is
+internal-order and packed for the kernels (see include/taichimps_gb300.h):
+``xr`` = (x, y, z, radius), ``vm`` = (v, mass), ``om`` = (omega, inertia),
+``f``/``torque`` component-major.  The neighbor build re-sorts atoms by cell,
+so internal order changes; ``uid`` records each slot's insertion index and the
+field views below (``atom.x.to_numpy()`` ...) always present insertion order,
+padded to ``max_atoms`` rows like the reference's Taichi fields.
+"""
+
+from __future__ import annotations
+
+from typing import Any
+
+import numpy as np
+import torch
+
+from . import _device, _lib
+
+
+class _Buffers:
+    """One complete set of per-atom device arrays (two exist: build permutes A -> B)."""
+
+    def __init__(self, n: int, dev: torch.device) -> None:
+        f64 = dict(dtype=torch.float64, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.xr = torch.zeros((n, 4), **f64)
+        self.vm = torch.zeros((n, 4), **f64)
+        self.om = torch.zeros((n, 4), **f64)
+        self.f = torch.zeros((3, n), **f64)
+        self.torque = torch.zeros((3, n), **f64)
+        self.virial = torch.zeros((6, n), **f64)
+        self.tag = torch.zeros(n, **i32)
+        self.uid = torch.zeros(n, **i32)
+        self.x0 = torch.zeros((3, n), **f64)
+
+
+class FieldView:
+    """
+    Reference-style access to one per-atom quantity in insertion order:
+    ``to_numpy()``, ``from_numpy()``, ``fill()``, ``[i]`` and ``[i] = v``.
+    """
+
+    def __init__(self, atom: "AtomSystem", name: str, width: int, dtype) -> None:
+        self._atom, self._name, self._w, self._dtype = atom, name, width, dtype
+
+    def _internal(self) -> torch.Tensor:
+        return self._atom._internal_view(self._name)
+
+    def to_numpy(self) -> np.ndarray:
+        a = self._atom
+        shape = (a.max_atoms,) if self._w == 1 else (a.max_atoms, self._w)
+        out = np.zeros(shape, dtype=self._dtype)
+        if a.nlocal:
+            vals = self._internal().detach().cpu().numpy()
+            uid = a.uid_host()
+            out[uid] = vals
+        return out
+
+    def from_numpy(self, arr) -> None:
+        a = self._atom
+        arr = np.asarray(arr)
+        n = a.nlocal
+        vals = arr[:n]
+        uid = a.uid_host()
+        t = torch.from_numpy(np.ascontiguousarray(vals[uid]).astype(self._dtype)).to(a.device)
+        a._assign_internal(self._name, t)
+
+    def fill(self, value: float) -> None:
+        a = self._atom
+        if a.nlocal:
+            v = self._internal()
+            a._assign_internal(self._name, torch.full_like(v, value))
+
+    def __getitem__(self, i: int):
+        return self.to_numpy()[i]
+
+    def __setitem__(self, i: int, value) -> None:
+        full = self.to_numpy()
+        full[i] = np.asarray(value, dtype=self._dtype)
+        self.from_numpy(full)
+
+    def __array__(self, dtype=None):
+        a = self.to_numpy()
+        return a if dtype is None else a.astype(dtype)
+
+
+class AtomSystem:
+    def __init__(self, max_atoms: int, float_type: Any = None) -> None:
+        self.max_atoms = int(max_atoms)
+        self.nlocal = 0
+        self.float_type = float_type
+        self.device = _device.device()
+        self._buf = _Buffers(0, self.device)
+        self._alt = _Buffers(0, self.device)
+        self.atom_type_host = np.zeros(0, dtype=np.int32)
+        self.mask_host = np.zeros(0, dtype=np.int32)
+        self._uid_cache: np.ndarray | None = None
+        self.x = FieldView(self, "x", 3, np.float64)
+        self.v = FieldView(self, "v", 3, np.float64)
+        self.f = FieldView(self, "f", 3, np.float64)
+        self.omega = FieldView(self, "omega", 3, np.float64)
+        self.torque = FieldView(self, "torque", 3, np.float64)
+        self.radius = FieldView(self, "radius", 1, np.float64)
+        self.rmass = FieldView(self, "rmass", 1, np.float64)
+        self.tag = FieldView(self, "tag", 1, np.int32)
+        self.virial = FieldView(self, "virial", 6, np.float64)
+        self.max_radius = 0.0
+        self._listeners: list = []
+
+    # ------------------------------------------------------------ views
+
+    def _internal_view(self, name: str) -> torch.Tensor:
+        b = self._buf
+        return {
+            "x": lambda: b.xr[:, :3], "v": lambda: b.vm[:, :3], "omega": lambda: b.om[:, :3],
+            "radius": lambda: b.xr[:, 3], "rmass": lambda: b.vm[:, 3],
+            "f": lambda: b.f.t(), "torque": lambda: b.torque.t(), "virial": lambda: b.virial.t(),
+            "tag": lambda: b.tag,
+        }[name]()
+
+    def _assign_internal(self, name: str, t: torch.Tensor) -> None:
+        self._internal_view(name).copy_(t)
+        if name in ("radius", "rmass"):
+            # keep the packed inertia in step (atom.py:110-111, nve_sphere.py:120)
+            b = self._buf
+            m, r = b.vm[:, 3], b.xr[:, 3]
+            b.om[:, 3] = ((0.4 * m) * r) * r
+            self.max_radius = float(b.xr[:, 3].max().item()) if self.nlocal else 0.0
+
+    def uid_host(self) -> np.ndarray:
+        if self._uid_cache is None:
+            self._uid_cache = self._buf.uid.cpu().numpy().astype(np.int64)
+        return self._uid_cache
+
+    @property
+    def buffers(self) -> _Buffers:
+        return self._buf
+
+    @property
+    def alt_buffers(self) -> _Buffers:
+        return self._alt
+
+    def swap_buffers(self) -> None:
+        """Called by the neighbor build after permuting into the alternate set."""
+        self._buf, self._alt = self._alt, self._buf
+        self._uid_cache = None
+        for cb in self._listeners:
+            cb()
+
+    def cstruct(self, b: _Buffers | None = None) -> _lib.Atoms:
+        b = self._buf if b is None else b
+        s = _lib.Atoms()
+        s.n = self.nlocal
+        s.xr, s.vm, s.om = b.xr.data_ptr(), b.vm.data_ptr(), b.om.data_ptr()
+        s.f, s.torque, s.virial = b.f.data_ptr(), b.torque.data_ptr(), b.virial.data_ptr()
+        s.tag, s.uid, s.x0 = b.tag.data_ptr(), b.uid.data_ptr(), b.x0.data_ptr()
+        return s
+
+    # ---------------------------------------------------------- particles
+
+    def add_particles(self, x, radius, density, v=None, omega=None, tag=None, atom_type=1) -> None:
+        """Append particles; rmass = 4/3 pi r^3 density (atom.py:55-145)."""
+        x_np = np.asarray(x, dtype=np.float64)
+        if x_np.ndim == 1:
+            x_np = x_np.reshape(1, 3)
+        n_new = len(x_np)
+        if self.nlocal + n_new > self.max_atoms:
+            raise ValueError(f"Exceeded max_atoms capacity: {self.nlocal + n_new} > {self.max_atoms}")
+        v_np = np.zeros_like(x_np) if v is None else np.asarray(v, dtype=np.float64).reshape(n_new, 3)
+        o_np = np.zeros_like(x_np) if omega is None else np.asarray(omega, dtype=np.float64).reshape(n_new, 3)
+        rad = np.asarray(radius, dtype=np.float64)
+        if rad.ndim == 0:
+            rad = np.full(n_new, float(rad))
+        dens = np.full(n_new, float(density)) if np.isscalar(density) else np.asarray(density, dtype=np.float64)
+        types = (np.full(n_new, int(atom_type), dtype=np.int32) if np.isscalar(atom_type)
+                 else np.asarray(atom_type, dtype=np.int32))
+        vol = (4.0 / 3.0) * np.pi * (rad ** 3)
+        mass = vol * dens
+        inertia = ((0.4 * mass) * rad) * rad
+        start = self.nlocal
+        tags = (np.arange(start + 1, start + n_new + 1, dtype=np.int32) if tag is None
+                else np.asarray(tag, dtype=np.int32))
+
+        old = self._gather_all() if self.nlocal else None
+        n = start + n_new
+        nb = _Buffers(n, self.device)
+        host = {
+            "xr": np.zeros((n, 4)), "vm": np.zeros((n, 4)), "om": np.zeros((n, 4)),
+            "f": np.zeros((3, n)), "torque": np.zeros((3, n)), "virial": np.zeros((6, n)),
+            "tag": np.zeros(n, dtype=np.int32), "uid": np.arange(n, dtype=np.int32),
+            "x0": np.zeros((3, n)),
+        }
+        if old is not None:
+            for k in ("xr", "vm", "om", "tag"):
+                host[k][:start] = old[k]
+            for k in ("f", "torque", "virial", "x0"):
+                host[k][:, :start] = old[k]
+        host["xr"][start:, :3] = x_np
+        host["xr"][start:, 3] = rad
+        host["vm"][start:, :3] = v_np
+        host["vm"][start:, 3] = mass
+        host["om"][start:, :3] = o_np
+        host["om"][start:, 3] = inertia
+        host["tag"][start:] = tags
+        for k, arr in host.items():
+            getattr(nb, k).copy_(torch.from_numpy(np.ascontiguousarray(arr)))
+        self._buf = nb
+        self._alt = _Buffers(n, self.device)
+        self.atom_type_host = np.concatenate([self.atom_type_host, types])
+        self.mask_host = np.concatenate([self.mask_host, np.ones(n_new, dtype=np.int32)])
+        self.nlocal = n
+        self._uid_cache = None
+        self.max_radius = float(host["xr"][:, 3].max()) if n else 0.0
+        for cb in self._listeners:
+            cb()
+
+    def _gather_all(self) -> dict[str, np.ndarray]:
+        """All per-atom arrays in insertion order (host copies)."""
+        b = self._buf
+        uid = self.uid_host()
+        out = {}
+        for k in ("xr", "vm", "om", "tag"):
+            a = getattr(b, k).cpu().numpy()
+            o = np.empty_like(a)
+            o[uid] = a
+            out[k] = o
+        for k in ("f", "torque", "virial", "x0"):
+            a = getattr(b, k).cpu().numpy()
+            o = np.empty_like(a)
+            o[:, uid] = a
+            out[k] = o
+        return out
+
+    def on_reorder(self, cb) -> None:
+        """Register a callback run whenever internal order or size changes."""
+        self._listeners.append(cb)
+
+    @property
+    def atom_type(self) -> np.ndarray:
+        return self.atom_type_host
+
+    @property
+    def mask(self) -> np.ndarray:
+        return self.mask_host
+
+    def clear_forces(self) -> None:
+        """Zero f, torque and the per-atom virial (atom.py:201-220)."""
+        if self.nlocal == 0:
+            return
+        _lib.check(_device.lib().tmps_clear_forces(self.cstruct(), _device.stream()), "tmps_clear_forces")

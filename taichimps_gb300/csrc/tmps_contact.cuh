@@ -1,0 +1,259 @@
+// The contact laws, written once over the arithmetic type T.
+//
+// T = double gives the plain FP64 form; T = float gives the mixed form, where
+// the per-contact shear history stays double (the many tiny vtr*dt
+// increments are added in FP64) and everything else runs in FP32.
+//
+// Every law is evaluated for one canonical orientation a -> b of the pair
+// (d = x_a - x_b after the minimum image).  The expressions follow the
+// reference kernels term for term:
+//   gran/hooke            GRANULAR/hooke.py:83-143
+//   gran/hooke/history    GRANULAR/hooke_history.py:144-217
+//   gran/hertz            GRANULAR/hertz.py:77-118
+//   gran/hertz/history    GRANULAR/hertz_history.py:92-157
+//   granular              GRANULAR/granular.py:316-414 (+ rotate_rescale :271-280)
+#pragma once
+
+#include "tmps_common.cuh"
+
+namespace tmps {
+
+enum { STYLE_HOOKE = 0, STYLE_HOOKE_HISTORY = 1, STYLE_HERTZ = 2, STYLE_HERTZ_HISTORY = 3, STYLE_GRANULAR = 4 };
+
+template <int STYLE>
+struct StyleTraits {
+    static constexpr bool legacy = STYLE != STYLE_GRANULAR;
+    static constexpr bool hertz = STYLE == STYLE_HERTZ || STYLE == STYLE_HERTZ_HISTORY;
+    static constexpr bool legacy_history = STYLE == STYLE_HOOKE_HISTORY || STYLE == STYLE_HERTZ_HISTORY;
+};
+
+template <typename T>
+TMPS_DEV T dot3(const T* a, const T* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+template <typename T>
+TMPS_DEV T norm3(const T* a) { return sqrt(dot3(a, a)); }
+template <typename T>
+TMPS_DEV void cross3(const T* a, const T* b, T* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+template <typename T>
+struct PairIn {
+    T d[3];      // x_a - x_b, minimum image
+    T rsq;
+    T ra, rb, ma, mb;
+    T va[3], vb[3];  // vb already shifted by the remap-v image velocity
+    T wa[3], wb[3];
+};
+
+template <typename T>
+struct PairOut {
+    T f[3];      // force on a (b gets -f)
+    T tor[3];    // torque term; a gets arm_a * tor, b gets arm_b * tor
+    T arm_a, arm_b;
+};
+
+// Returns true when the pair is in contact.  `sh` (canonical sense) is read
+// and written only by history styles; `has_hist` says whether the slot held a
+// live contact before this call (the reference's partner == jtag test).
+template <typename T, int STYLE>
+TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, const PairIn<T>& in,
+                          double* sh, PairOut<T>& out) {
+    using S = StyleTraits<STYLE>;
+    const T radsum = in.ra + in.rb;
+    if constexpr (S::legacy) {
+        const T r = sqrt(in.rsq);
+        const T delta = radsum - r;
+        T polyhertz = T(1);
+        if constexpr (S::hertz) {
+            const T reff = (in.ra * in.rb) / (in.ra + in.rb);
+            polyhertz = sqrt(reff * delta);
+        }
+        const T meff = (in.ma * in.mb) / (in.ma + in.mb);
+        const T rsqinv = T(1) / in.rsq;
+        const T rinv = T(1) / r;
+        T vrel_t[3], vt[3], wr[3], cr[3], vtr[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) vrel_t[k] = in.va[k] - in.vb[k];
+        const T vnnr = dot3(vrel_t, in.d);
+        const T s = vnnr * rsqinv;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) vt[k] = vrel_t[k] - in.d[k] * s;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) wr[k] = (in.ra * in.wa[k] + in.rb * in.wb[k]) * rinv;
+        cross3(in.d, wr, cr);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) vtr[k] = vt[k] + cr[k];
+        const T damp = ((meff * T(P.gamman)) * vnnr) * rsqinv;
+        T ccel = (T(P.kn) * delta) * rinv - damp;
+        if constexpr (S::hertz) ccel = ccel * polyhertz;
+        if (P.limit_damping == 1 && ccel < T(0)) ccel = T(0);
+        T fs[3];
+        if constexpr (!S::legacy_history) {
+            const T vrel = norm3(vtr);
+            const T fn = T(P.xmu) * fabs(ccel * r);
+            const T fsd = (meff * T(P.gammat)) * vrel;
+            T ft = T(0);
+            if (vrel > T(1e-16)) ft = (fn < fsd ? fn : fsd) / vrel;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) fs[k] = (-ft) * vtr[k];
+        } else {
+            const T geff = meff * T(P.gammat);
+            T shf[3];
+            if (shearupdate) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) sh[k] = sh[k] + (double)(vtr[k] * dt);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) shf[k] = (T)sh[k];
+            const T shrmag = norm3(shf);
+            if (shearupdate) {
+                const T rsht = dot3(shf, in.d) * rsqinv;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    sh[k] = sh[k] - (double)(rsht * in.d[k]);
+                    shf[k] = (T)sh[k];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T t = T(P.kt) * shf[k] + geff * vtr[k];
+                if constexpr (S::hertz) fs[k] = (-polyhertz) * t;
+                else fs[k] = -t;
+            }
+            const T fsmag = norm3(fs);
+            const T fn = T(P.xmu) * fabs(ccel * r);
+            if (fsmag > fn) {
+                if (shrmag != T(0)) {
+                    const T ratio = fn / fsmag;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const T dc = (geff * vtr[k]) / T(P.kt);
+                        sh[k] = (double)ratio * (sh[k] + (double)dc) - (double)dc;
+                        fs[k] = ratio * fs[k];
+                    }
+                } else {
+                    fs[0] = fs[1] = fs[2] = T(0);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out.f[k] = in.d[k] * ccel + fs[k];
+        T c[3];
+        cross3(in.d, fs, c);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out.tor[k] = rinv * c[k];
+        out.arm_a = -in.ra;
+        out.arm_b = -in.rb;
+    } else {
+        const T r = sqrt(in.rsq);
+        const T rinv = T(1) / r;
+        T nv[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nv[k] = in.d[k] * rinv;
+        const T delta = radsum - r;
+        const T reff = (in.ra * in.rb) / radsum;
+        const T meff = (in.ma * in.mb) / (in.ma + in.mb);
+        const T a = sqrt(delta * reff);
+        T vr[3], vt[3], wr[3], cr[3], vtr[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) vr[k] = in.va[k] - in.vb[k];
+        const T vnnr = dot3(vr, nv);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) vt[k] = vr[k] - vnnr * nv[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) wr[k] = in.ra * in.wa[k] + in.rb * in.wb[k];
+        cross3(wr, nv, cr);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) vtr[k] = vt[k] - cr[k];
+        const T vrel = norm3(vtr);
+        const T fne = P.normal_id != 0 ? (T(P.kn) * a) * delta : T(P.kn) * delta;
+        T dpf = T(0);
+        switch (P.damping_id) {
+            case 1: dpf = T(P.damp); break;
+            case 2: dpf = T(P.damp) * meff; break;
+            case 3: dpf = (T(P.damp) * meff) * a; break;
+            case 4:
+            case 5: {
+                T arg = T(0);
+                if (delta > T(0)) {
+                    const T q = (meff * fne) / delta;
+                    arg = q > T(0) ? q : T(0);
+                }
+                dpf = T(P.damp) * sqrt(arg);
+                break;
+            }
+            default: break;
+        }
+        T fntot = fne - dpf * vnnr;
+        if (P.limit_damping == 1 && fntot < T(0)) fntot = T(0);
+        const T fscrit = T(P.mu) * fabs(fntot);
+        T fs[3] = {T(0), T(0), T(0)};
+        if (P.tangential_id == 1) {
+            const T damp_t = T(P.xt) * dpf;
+            T ft = T(0);
+            if (vrel != T(0)) {
+                const T q = damp_t * vrel;
+                ft = (fscrit < q ? fscrit : q) / vrel;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) fs[k] = (-ft) * vtr[k];
+        } else if (P.tangential_id == 2 || P.tangential_id == 3) {
+            T keff = T(P.kt);
+            if (P.tangential_id == 3) keff = T(P.kt) * a;
+            const T damp_t = T(P.xt) * dpf;
+            T hf[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) hf[k] = (T)sh[k];
+            if (shearupdate) {
+                const T rsht = dot3(hf, nv);
+                if (fabs(rsht) * keff > T(1e-10) * fscrit) {
+                    // rotate_rescale: project onto the tangent plane, keep |h|
+                    const T shrmag = norm3(hf);
+                    T o[3];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) o[k] = hf[k] - rsht * nv[k];
+                    const T prjmag = norm3(o);
+                    T scale = T(0);
+                    if (prjmag > T(0)) scale = shrmag / prjmag;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) sh[k] = (double)(o[k] * scale);
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    sh[k] = sh[k] + (double)(vtr[k] * dt);
+                    hf[k] = (T)sh[k];
+                }
+            }
+            T fdamp[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) fdamp[k] = (-damp_t) * vtr[k];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) fs[k] = (-keff) * hf[k] + fdamp[k];
+            const T magfs = norm3(fs);
+            if (magfs > fscrit) {
+                if (norm3(hf) != T(0)) {
+                    const T sc = fscrit / magfs;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        fs[k] = fs[k] * sc;
+                        sh[k] = (double)((-(fs[k] - fdamp[k])) / keff);
+                    }
+                } else {
+                    fs[0] = fs[1] = fs[2] = T(0);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out.f[k] = fntot * nv[k] + fs[k];
+        T c[3];
+        cross3(nv, fs, c);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out.tor[k] = -c[k];
+        out.arm_a = in.ra - T(0.5) * delta;
+        out.arm_b = in.rb - T(0.5) * delta;
+    }
+}
+
+}  // namespace tmps

@@ -1,0 +1,289 @@
+// Neighbor build and contact-history carry-over (FP64, exact).
+//
+// Atoms are binned in lamda coordinates exactly as NeighborList.get_cell_coord
+// does (neighbor.py:191-206), then physically re-sorted: cells laid out along a
+// Morton curve, atoms inside a cell by insertion index.  The full list (both
+// i->j and j->i) is then built from the 27-cell stencil with the reference's
+// periodic-wrap and single-bin skip rules (neighbor.py:329-351) and the exact
+// FP64 cut test (ri + rj + skin)^2 (neighbor.py:355-359), so the pair set is
+// bit-identical to the reference's half list on the same positions.
+#include "tmps_common.cuh"
+
+using namespace tmps;
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kScanBlock = 1024;
+
+// Cell of one position: floor(((x - lo) / prd) / csize), clamped.  The
+// reference's lamda for an orthogonal box adds products with zero tilt terms,
+// which leave the quotient unchanged.
+__device__ __forceinline__ int3 cell_coord(const tmps_box* __restrict__ b, double x, double y,
+                                           double z) {
+    double xx[3] = {x, y, z};
+    int c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double lam = __ddiv_rn(__dsub_rn(xx[k], b->lo[k]), b->prd[k]);
+        double q = floor(__ddiv_rn(lam, b->csize[k]));
+        // clamp in floating point first so a stray NaN/Inf cannot overflow
+        // the int conversion; NaN falls to cell 0
+        int ck = q >= (double)(b->g[k] - 1) ? b->g[k] - 1 : (q > 0.0 ? (int)q : 0);
+        c[k] = ck;
+    }
+    return make_int3(c[0], c[1], c[2]);
+}
+
+__global__ void __launch_bounds__(kBlock) k_bin(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                const int32_t* __restrict__ rank, int32_t* old_cell,
+                                                int32_t* count, int32_t* status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double4 x = ld4(a.xr, i);
+    if (!isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z)) atomicOr(status, TMPS_STATUS_NONFINITE);
+    int3 c = cell_coord(b, x.x, x.y, x.z);
+    int lin = c.x + c.y * b->g[0] + c.z * b->g[0] * b->g[1];
+    old_cell[i] = lin;
+    atomicAdd(&count[rank[lin]], 1);
+}
+
+// Exclusive scan of `count` (length m, by Morton rank) into start[0..m].
+// One block: each thread owns a contiguous chunk.  Runs once per rebuild.
+__global__ void __launch_bounds__(kScanBlock) k_scan(const int32_t* count, int32_t* start, int m) {
+    __shared__ int32_t part[kScanBlock];
+    const int t = threadIdx.x;
+    const int chunk = (m + kScanBlock - 1) / kScanBlock;
+    const int beg = t * chunk, end = min(m, beg + chunk);
+    int32_t s = 0;
+    for (int c = beg; c < end; ++c) s += count[c];
+    part[t] = s;
+    __syncthreads();
+    // Hillis-Steele inclusive scan of the per-thread sums
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+        int32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int32_t run = part[t] - s;
+    for (int c = beg; c < end; ++c) {
+        start[c] = run;
+        run += count[c];
+    }
+    if (t == kScanBlock - 1) start[m] = part[t];
+}
+
+__global__ void __launch_bounds__(kBlock) k_scatter(int n, const int32_t* __restrict__ rank,
+                                                    const int32_t* __restrict__ old_cell,
+                                                    const int32_t* __restrict__ start, int32_t* fill,
+                                                    int32_t* order) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int r = rank[old_cell[i]];
+    int slot = atomicAdd(&fill[r], 1);
+    order[start[r] + slot] = i;
+}
+
+// Within each cell, order atoms by insertion index: the layout then depends
+// only on positions, not on which atomics won the scatter.
+__global__ void __launch_bounds__(kBlock) k_cell_sort(int m, const int32_t* __restrict__ start,
+                                                      const int32_t* __restrict__ uid, int32_t* order) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    int beg = start[r], end = start[r + 1];
+    for (int p = beg + 1; p < end; ++p) {
+        int v = order[p];
+        int key = uid[v];
+        int q = p - 1;
+        while (q >= beg && uid[order[q]] > key) {
+            order[q + 1] = order[q];
+            --q;
+        }
+        order[q + 1] = v;
+    }
+}
+
+// Gather every per-atom array into the new order; store x0 for the skin check.
+__global__ void __launch_bounds__(kBlock) k_permute(tmps_atoms src, tmps_atoms dst,
+                                                    const int32_t* __restrict__ order,
+                                                    const int32_t* __restrict__ old_cell,
+                                                    int32_t* cell_of) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = src.n;
+    if (p >= n) return;
+    int i = order[p];
+    double4 x = ld4(src.xr, i);
+    st4(dst.xr, p, x);
+    st4(dst.vm, p, ld4(src.vm, i));
+    st4(dst.om, p, ld4(src.om, i));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        dst.f[k * n + p] = src.f[k * n + i];
+        dst.torque[k * n + p] = src.torque[k * n + i];
+    }
+    if (src.virial && dst.virial) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dst.virial[k * n + p] = src.virial[k * n + i];
+    }
+    dst.tag[p] = src.tag[i];
+    dst.uid[p] = src.uid[i];
+    dst.x0[p] = x.x;
+    dst.x0[n + p] = x.y;
+    dst.x0[2 * n + p] = x.z;
+    cell_of[p] = old_cell[i];
+}
+
+// The full list.  Stencil order and wrap/skip rules of neighbor.py:329-351;
+// the cut test is done with explicit round-to-nearest operations so no
+// multiply-add contraction can move a pair across the cut.
+__global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                  double skin, const int32_t* __restrict__ cell_of,
+                                                  const int32_t* __restrict__ rank,
+                                                  const int32_t* __restrict__ start, tmps_nlist nl,
+                                                  int32_t* status) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    if (p >= n) return;
+    const int gx = b->g[0], gy = b->g[1], gz = b->g[2], gxy = gx * gy;
+    const int px = b->per[0], py = b->per[1], pz = b->per[2];
+    const int lin = cell_of[p];
+    const int cz = lin / gxy, cy = (lin - cz * gxy) / gx, cx = lin - cz * gxy - cy * gx;
+    const double4 xi = ld4(a.xr, p);
+    const double prd[3] = {b->prd[0], b->prd[1], b->prd[2]};
+    int count = 0;
+    bool overflow = false;
+    for (int ox = -1; ox <= 1; ++ox)
+        for (int oy = -1; oy <= 1; ++oy)
+            for (int oz = -1; oz <= 1; ++oz) {
+                bool skip = (px == 1 && gx == 1 && ox != 0) || (py == 1 && gy == 1 && oy != 0) ||
+                            (pz == 1 && gz == 1 && oz != 0);
+                int nx = cx + ox, ny = cy + oy, nz = cz + oz;
+                if (px == 1) nx = (nx % gx + gx) % gx;
+                if (py == 1) ny = (ny % gy + gy) % gy;
+                if (pz == 1) nz = (nz % gz + gz) % gz;
+                if (skip || nx < 0 || nx >= gx || ny < 0 || ny >= gy || nz < 0 || nz >= gz) continue;
+                const int r = rank[nx + ny * gx + nz * gxy];
+                const int code = (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1);
+                const int beg = start[r], end = start[r + 1];
+                for (int q = beg; q < end; ++q) {
+                    if (q == p) continue;
+                    const double4 xj = ld4(a.xr, q);
+                    double d[3] = {__dsub_rn(xi.x, xj.x), __dsub_rn(xi.y, xj.y), __dsub_rn(xi.z, xj.z)};
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        if (b->per[k] == 1)
+                            d[k] = __dsub_rn(d[k], __dmul_rn(prd[k], round(__ddiv_rn(d[k], prd[k]))));
+                    double rsq = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])),
+                                           __dmul_rn(d[2], d[2]));
+                    double rad = __dadd_rn(__dadd_rn(xi.w, xj.w), skin);
+                    if (rsq < __dmul_rn(rad, rad)) {
+                        if (count < nl.slots) {
+                            nl.nbr[(size_t)count * n + p] = q | (code << kNbrIndexBits);
+                            ++count;
+                        } else {
+                            overflow = true;
+                        }
+                    }
+                }
+            }
+    nl.nnb[p] = count;
+    if (overflow) atomicOr(status, TMPS_STATUS_NLIST_OVERFLOW);
+}
+
+// ContactHistory save/restore (contact_history.py:91-139) in one pass: for
+// each slot of the new list, find the same partner among the old row's
+// touching slots and carry its shear over; anything else starts at zero.
+__global__ void __launch_bounds__(kBlock) k_history_remap(tmps_nlist o, tmps_nlist nw,
+                                                          const int32_t* __restrict__ order) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = nw.n;
+    if (p >= n) return;
+    const int po = order[p];
+    const uint64_t otouch = o.touch[po];
+    const int onn = o.nnb[po];
+    const int nn = nw.nnb[p];
+    uint64_t bits = 0;
+    for (int k = 0; k < nn; ++k) {
+        const int qo = order[nw.nbr[(size_t)k * n + p] & kNbrIndexMask];
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        if (otouch) {
+            for (int ko = 0; ko < onn; ++ko) {
+                if (!((otouch >> ko) & 1ull)) continue;
+                if ((o.nbr[(size_t)ko * n + po] & kNbrIndexMask) != qo) continue;
+                const size_t ss = (size_t)o.slots * n;
+                s0 = o.shear[(size_t)ko * n + po];
+                s1 = o.shear[ss + (size_t)ko * n + po];
+                s2 = o.shear[2 * ss + (size_t)ko * n + po];
+                bits |= 1ull << k;
+                break;
+            }
+        }
+        const size_t ns = (size_t)nw.slots * n;
+        nw.shear[(size_t)k * n + p] = s0;
+        nw.shear[ns + (size_t)k * n + p] = s1;
+        nw.shear[2 * ns + (size_t)k * n + p] = s2;
+    }
+    nw.touch[p] = bits;
+}
+
+bool launch_ok() { return cudaPeekAtLastError() == cudaSuccess; }
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" {
+
+int64_t tmps_nlist_workspace_bytes(int32_t n, int32_t ncell) {
+    if (n < 0 || ncell < 0) return -1;
+    // count[ncell], start[ncell+1], fill[ncell], old_cell[n]
+    return (int64_t)(align256((size_t)ncell * 4) + align256((size_t)(ncell + 1) * 4) +
+                     align256((size_t)ncell * 4) + align256((size_t)n * 4));
+}
+
+int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_box* d_box,
+                     int32_t ncell, double skin, const int32_t* cell_rank, int32_t* order,
+                     int32_t* cell_of, const tmps_nlist* nl, void* workspace,
+                     int64_t workspace_bytes, int32_t* d_status, void* stream) {
+    if (!src || !dst || !d_box || !cell_rank || !order || !cell_of || !nl || !workspace || !d_status)
+        return TMPS_ERR_BAD_ARG;
+    const int n = src->n;
+    if (n < 0 || dst->n != n || nl->n != n || nl->slots < 1 || nl->slots > kMaxSlots ||
+        n > kNbrIndexMask || !dst->x0)
+        return TMPS_ERR_BAD_ARG;
+    if (n == 0) return TMPS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int m = ncell;
+    if (m < 1 || workspace_bytes < tmps_nlist_workspace_bytes(n, m)) return TMPS_ERR_BAD_ARG;
+    char* w = (char*)workspace;
+    int32_t* count = (int32_t*)w;
+    w += align256((size_t)m * 4);
+    int32_t* start = (int32_t*)w;
+    w += align256((size_t)(m + 1) * 4);
+    int32_t* fill = (int32_t*)w;
+    w += align256((size_t)m * 4);
+    int32_t* old_cell = (int32_t*)w;
+
+    if (cudaMemsetAsync(count, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
+    if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
+    const int gb = grid_for(n, kBlock);
+    k_bin<<<gb, kBlock, 0, s>>>(*src, d_box, cell_rank, old_cell, count, d_status);
+    k_scan<<<1, kScanBlock, 0, s>>>(count, start, m);
+    k_scatter<<<gb, kBlock, 0, s>>>(n, cell_rank, old_cell, start, fill, order);
+    k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
+    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, order, old_cell, cell_of);
+    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, d_status);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_history_remap(const tmps_nlist* old_nl, const tmps_nlist* new_nl, const int32_t* order,
+                       void* stream) {
+    if (!old_nl || !new_nl || !order || old_nl->n != new_nl->n) return TMPS_ERR_BAD_ARG;
+    if (new_nl->n == 0) return TMPS_OK;
+    k_history_remap<<<grid_for(new_nl->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*old_nl, *new_nl,
+                                                                                     order);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,89 @@
+"""
+Seeded packings of polydisperse spheres in a periodic cube.
+
+Random sequential insertion stalls near solid fraction 0.38, below the 0.40 and
+0.45 the benchmark configurations ask for, so packings are made this way:
+
+1. diameters drawn uniform in [dmin, dmax] (numpy PCG64, fixed seed);
+2. the cube edge L set so that sum(pi d^3 / 6) / L^3 equals the target fraction;
+3. centres placed on randomly chosen sites of the smallest FCC lattice with at
+   least n sites, each jittered by up to `jitter` of the lattice constant;
+4. remaining overlaps removed by repeatedly pushing each overlapping pair apart
+   along its line of centres (periodic minimum image) until none is left.
+
+The result has no overlapping pair, so it starts with no contacts.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _fcc_sites(m: int) -> np.ndarray:
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 3)
+    return (g[:, None, :] + base[None, :, :]).reshape(-1, 3)
+
+
+def remove_overlaps(x: np.ndarray, radius: np.ndarray, L: float, max_iter: int = 200, margin: float = 1e-9):
+    """Push overlapping pairs apart until none overlaps (periodic cube of edge L)."""
+    from scipy.spatial import cKDTree
+
+    x = np.mod(x, L)
+    rmax = float(radius.max())
+    for _ in range(max_iter):
+        tree = cKDTree(x, boxsize=L)
+        pairs = tree.query_pairs(r=2.0 * rmax, output_type="ndarray")
+        if len(pairs) == 0:
+            return x
+        i, j = pairs[:, 0], pairs[:, 1]
+        d = x[i] - x[j]
+        d -= L * np.round(d / L)
+        r = np.sqrt((d * d).sum(1))
+        need = radius[i] + radius[j] + margin
+        bad = r < need
+        if not bad.any():
+            return x
+        i, j, d, r, need = i[bad], j[bad], d[bad], r[bad], need[bad]
+        r = np.maximum(r, 1e-12)
+        push = (0.5 * (need - r) * 1.05 + margin)[:, None] * (d / r[:, None])
+        delta = np.zeros_like(x)
+        np.add.at(delta, i, push)
+        np.add.at(delta, j, -push)
+        x = np.mod(x + delta, L)
+    raise RuntimeError("overlap removal did not converge")
+
+
+def make_packing(n: int, dmin: float, dmax: float, phi: float, seed: int, jitter: float = 0.05,
+                 vel_sigma: float = 0.0):
+    """Returns dict(x, radius, L, v) for n spheres at solid fraction phi."""
+    rng = np.random.default_rng(seed)
+    d = rng.uniform(dmin, dmax, size=n)
+    L = float((np.sum(math.pi / 6.0 * d ** 3) / phi) ** (1.0 / 3.0))
+    m = int(math.ceil((n / 4.0) ** (1.0 / 3.0)))
+    while 4 * m ** 3 < n:
+        m += 1
+    sites = _fcc_sites(m)
+    pick = rng.choice(len(sites), size=n, replace=False)
+    a = L / m
+    x = (sites[pick] + 0.25) * a + rng.uniform(-jitter, jitter, size=(n, 3)) * a
+    radius = 0.5 * d
+    x = remove_overlaps(x, radius, L)
+    v = rng.normal(0.0, vel_sigma, size=(n, 3)) if vel_sigma > 0.0 else np.zeros((n, 3))
+    return {"x": x, "radius": radius, "L": L, "v": v}
+
+
+def config1(seed: int = 1, n: int = 4000):
+    """4,000 spheres, d ~ U[0.9, 1.1], phi 0.40, v ~ N(0, 0.1^2), rho 2.5."""
+    p = make_packing(n, 0.9, 1.1, 0.40, seed, vel_sigma=0.1)
+    p["density"] = 2.5
+    return p
+
+
+def config2(seed: int = 2, n: int = 1_000_000):
+    """1,000,000 spheres, d ~ U[0.8, 1.2], phi 0.45, at rest, rho 2.5."""
+    p = make_packing(n, 0.8, 1.2, 0.45, seed)
+    p["density"] = 2.5
+    return p

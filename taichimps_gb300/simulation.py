@@ -1,0 +1,163 @@
+"""
+The step orchestrator: LAMMPS Verlet order over the GB300 kernels.
+
+Mirrors taichimps ``Simulation`` (src/taichimps/simulation.py:21-332) -- the
+same constructor, hooks and step order:
+
+  1. fix nve/sphere initial_integrate
+  2. reneighbor if needed (save history -> pbc -> build -> restore history)
+  3. clear forces                   } one kernel: the contact kernel writes
+  4. pair compute                   } f / torque / virial instead of adding
+  5. fix post_force (Cundall damping ...)
+  6. fix nve/sphere final_integrate
+  7. fix end_of_step (deform/pressure servo ...)
+
+The setup force evaluation at the start of every run uses shearupdate=False
+(simulation.py:170-203).  Device-side errors (a box driven non-positive, a
+neighbor overflow) are raised at synchronisation points: rebuilds and the
+end of a run.
+"""
+
+from __future__ import annotations
+
+from typing import Any
+
+from .atom import AtomSystem
+from .computes.thermo import Computes
+from .contact_history import ContactHistory
+from .EXTRA_FIX.base import Fix
+from .EXTRA_FIX.nve_sphere import FixNVESphere
+from .GRANULAR.base import GranularPair
+from .neighbor import NeighborList
+
+
+class Simulation:
+    def __init__(self, domain, atom: AtomSystem | None = None, neighbor: NeighborList | None = None,
+                 history: ContactHistory | None = None, pair: GranularPair | None = None,
+                 max_atoms: int = 100000, max_neighbors_per_atom: int = 64, skin: float = 0.001,
+                 dt: float = 1e-4, thermo_freq: int = 100, float_type: Any = None) -> None:
+        self.domain = domain
+        self.dt = dt
+        self.float_type = float_type
+        self.timestep = 0
+        self.atom = atom if atom is not None else AtomSystem(max_atoms=max_atoms, float_type=float_type)
+        self.neighbor = neighbor if neighbor is not None else NeighborList(
+            domain=domain, max_atoms=max_atoms, max_neighbors_per_atom=max_neighbors_per_atom, skin=skin,
+            float_type=float_type)
+        self.history = history if history is not None else ContactHistory(
+            max_atoms=max_atoms, max_neighbors=max_neighbors_per_atom, float_type=float_type)
+        self.pair_style: GranularPair | None = pair
+        self.integrator: FixNVESphere | None = None
+        self.fixes: list[Fix] = []
+        self.dumps: list = []
+        self.restart_every = 0
+        self.restart_file = None
+        self.restart_writer = None
+        self.setup_done = False
+        self.run_pre = True
+        self.thermo_freq = thermo_freq
+        self.computes = Computes(float_type=float_type)
+
+    def add_dump(self, dump, freq: int = 100) -> None:
+        raise NotImplementedError("dump output is outside the GB300 contact path")
+
+    def set_restart(self, every: int, path, writer) -> None:
+        raise NotImplementedError("restart output is outside the GB300 contact path")
+
+    def set_pair_style(self, pair: GranularPair) -> None:
+        self.pair_style = pair
+
+    def add_fix(self, fix: Fix) -> None:
+        if isinstance(fix, FixNVESphere):
+            self.integrator = fix
+        else:
+            self.fixes.append(fix)
+
+    def remove_fix(self, fix: Fix) -> None:
+        if fix in self.fixes:
+            self.fixes.remove(fix)
+        elif self.integrator is fix:
+            self.integrator = None
+
+    def check_device_status(self) -> None:
+        for fix in self.fixes:
+            fix.check_status()
+
+    def reneighbor_if_needed(self, force: bool = False) -> bool:
+        """simulation.py:122-159: save -> pbc -> pull -> build -> restore."""
+        if self.neighbor is None:
+            return False
+        forced = force
+        for fix in self.fixes:
+            if fix.force_reneighbor:
+                forced = True
+                fix.force_reneighbor = False
+        if not self.neighbor.decide(self.atom, self.timestep) and not forced:
+            return False
+        self.check_device_status()
+        if self.history is not None:
+            self.history.save_state(self.atom, self.neighbor)
+        self.domain.pbc(self.atom)
+        self.domain.pull()
+        self.neighbor.build(self.atom)
+        if self.history is not None:
+            self.history.restore_state(self.atom, self.neighbor)
+        return True
+
+    def setup_run(self, nsteps_total: int) -> None:
+        for fix in self.fixes:
+            if hasattr(fix, "note_atom_count"):
+                fix.note_atom_count(self.atom.nlocal)
+            fix.setup(nsteps_total, self.dt)
+        if self.integrator is not None:
+            self.integrator.setup(nsteps_total, self.dt)
+
+    def init_simulation(self) -> None:
+        """Verlet::setup(): rebuild and evaluate forces without advancing history."""
+        self.setup_done = True
+        self.atom.clear_forces()
+        if self.pair_style is not None:
+            self.reneighbor_if_needed(force=True)
+            self.pair_style.compute(self.atom, self.neighbor, self.history, self.dt, shearupdate=False)
+        for fix in self.fixes:
+            fix.history_update = False
+        for fix in self.fixes:
+            fix.post_force(self.atom, self.dt)
+        for fix in self.fixes:
+            fix.history_update = True
+
+    def _sub_step_inner(self) -> None:
+        self.timestep += 1
+        for fix in self.fixes:
+            fix.timestep = self.timestep
+        if self.integrator is not None:
+            self.integrator.timestep = self.timestep
+            self.integrator.initial_integrate(self.atom, self.dt)
+        self.reneighbor_if_needed()
+        if self.pair_style is not None and self.neighbor is not None:
+            # clear_forces fused into the contact kernel (it writes, not adds)
+            self.pair_style._launch(self.atom, self.neighbor, self.history, self.dt, True, accumulate=False)
+        else:
+            self.atom.clear_forces()
+        for fix in self.fixes:
+            fix.post_force(self.atom, self.dt)
+        if self.integrator is not None:
+            self.integrator.final_integrate(self.atom, self.dt)
+        for fix in self.fixes:
+            fix.end_of_step(self.atom, self.dt)
+
+    def step(self) -> None:
+        self._sub_step_inner()
+
+    def run(self, steps: int) -> None:
+        self.setup_run(steps)
+        if self.run_pre or not self.setup_done:
+            self.init_simulation()
+        for _ in range(steps):
+            self._sub_step_inner()
+        self.check_device_status()
+        self.domain.pull()
+
+    def run_gpu(self, steps: int) -> None:
+        """The reference's batched run; with no host I/O on this path it is run()."""
+        self.run(steps)
