@@ -136,6 +136,10 @@ typedef struct tmps_servo {
 /* Version and build identity; no reference counterpart. */
 const char* tmps_version(void);
 
+/* Kernels launched by this library since it was loaded (all entry points);
+ * no reference counterpart. */
+long long tmps_launch_count(void);
+
 /* Copies a host box into device memory (Domain._sync, domain.py:235-254). */
 int tmps_box_set(tmps_box* d_box, const tmps_box* h_box, void* stream);
 

@@ -21,5 +21,7 @@ class FixDampingCundall(Fix):
     def post_force(self, atom, dt: float) -> None:
         if atom.nlocal == 0:
             return
-        _lib.check(_device.lib().tmps_damping_cundall(atom.cstruct(), self.gamma_lin, self.gamma_ang,
-                                                      _device.stream()), "tmps_damping_cundall")
+        with _device.timed("cundall"):
+            rc = _device.lib().tmps_damping_cundall(atom.cstruct(), self.gamma_lin, self.gamma_ang,
+                                                    _device.stream())
+        _lib.check(rc, "tmps_damping_cundall")

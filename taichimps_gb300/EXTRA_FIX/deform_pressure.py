@@ -234,17 +234,21 @@ class FixDeformPressure(Fix):
         if self._ws.numel() < wsb:
             self._ws = torch.zeros(wsb, dtype=torch.uint8, device=self.dev)
         if atom.nlocal:
-            _lib.check(L.tmps_virial_reduce(atom.cstruct(), 1, self._virial.data_ptr(), self._ws.data_ptr(),
-                                            wsb, st), "tmps_virial_reduce")
+            with _device.timed("virial"):
+                rc = L.tmps_virial_reduce(atom.cstruct(), 1, self._virial.data_ptr(), self._ws.data_ptr(), wsb, st)
+            _lib.check(rc, "tmps_virial_reduce")
         else:
             self._virial.zero_()
         elapsed = self.nsteps * dt
         frac = self.nsteps / self.nsteps_total if self.nsteps_total > 0 else 0.0
-        _lib.check(L.tmps_servo_step(self.domain.dbox, self._dservo.data_ptr(), self._virial.data_ptr(),
-                                     float(elapsed), float(frac), float(dt), self.status.data_ptr(), st),
-                   "tmps_servo_step")
+        with _device.timed("servo"):
+            rc = L.tmps_servo_step(self.domain.dbox, self._dservo.data_ptr(), self._virial.data_ptr(),
+                                   float(elapsed), float(frac), float(dt), self.status.data_ptr(), st)
+        _lib.check(rc, "tmps_servo_step")
         if self.remap == "x":
-            _lib.check(L.tmps_remap_x(atom.cstruct(), self.domain.dbox, st), "tmps_remap_x")
+            with _device.timed("remap_x"):
+                rc = L.tmps_remap_x(atom.cstruct(), self.domain.dbox, st)
+            _lib.check(rc, "tmps_remap_x")
         self.domain.mark_device_authoritative()
 
     def check_status(self) -> None:

@@ -20,11 +20,13 @@ class FixNVESphere(Fix):
     def initial_integrate(self, atom, dt: float) -> None:
         if atom.nlocal == 0:
             return
-        _lib.check(_device.lib().tmps_verlet_initial(atom.cstruct(), float(dt), _device.stream()),
-                   "tmps_verlet_initial")
+        with _device.timed("verlet_initial"):
+            rc = _device.lib().tmps_verlet_initial(atom.cstruct(), float(dt), _device.stream())
+        _lib.check(rc, "tmps_verlet_initial")
 
     def final_integrate(self, atom, dt: float) -> None:
         if atom.nlocal == 0:
             return
-        _lib.check(_device.lib().tmps_verlet_final(atom.cstruct(), float(dt), _device.stream()),
-                   "tmps_verlet_final")
+        with _device.timed("verlet_final"):
+            rc = _device.lib().tmps_verlet_final(atom.cstruct(), float(dt), _device.stream())
+        _lib.check(rc, "tmps_verlet_final")

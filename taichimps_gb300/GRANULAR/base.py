@@ -42,6 +42,7 @@ class GranularPair(ABC):
             if history is None:
                 history = nlist._private_history = ContactHistory(nlist.max_atoms, nlist.max_neighbors_per_atom)
         nl = history.cstruct(nlist)
-        rc = _device.lib().tmps_contact(atom.cstruct(), nl, self.domain.dbox, self.params, float(dt),
-                                        1 if shearupdate else 0, 1 if accumulate else 0, _device.stream())
+        with _device.timed("contact"):
+            rc = _device.lib().tmps_contact(atom.cstruct(), nl, self.domain.dbox, self.params, float(dt),
+                                            1 if shearupdate else 0, 1 if accumulate else 0, _device.stream())
         _lib.check(rc, "tmps_contact")

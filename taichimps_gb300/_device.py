@@ -10,6 +10,32 @@ import torch
 from . import _lib
 
 
+# Optional per-launch CUDA-event timing, keyed by kernel name; None when off.
+# bench.py turns it on for the kernels whose roofline it reports.
+TIMED: dict[str, list] | None = None
+
+
+class timed:
+    """Record CUDA events around one launch when ``TIMED`` collects `name`."""
+
+    def __init__(self, name: str):
+        self.name = name
+        self.on = TIMED is not None and name in TIMED
+
+    def __enter__(self):
+        if self.on:
+            self.e0 = torch.cuda.Event(enable_timing=True)
+            self.e0.record()
+        return self
+
+    def __exit__(self, *exc):
+        if self.on:
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record()
+            TIMED[self.name].append((self.e0, e1))
+        return False
+
+
 def device() -> torch.device:
     if not torch.cuda.is_available():
         raise RuntimeError("taichimps_gb300 runs on a CUDA device (GB300, sm_103a); none is available")

@@ -81,6 +81,7 @@ STATUS_NLIST_OVERFLOW, STATUS_NONFINITE, STATUS_BOX_NONPOSITIVE, STATUS_CELL_OVE
 # Every entry point the header declares, with its ctypes signature.
 _SIGS = {
     "tmps_version": (ctypes.c_char_p, []),
+    "tmps_launch_count": (ctypes.c_longlong, []),
     "tmps_box_set": (c_i32, [c_vp, ctypes.POINTER(Box), c_vp]),
     "tmps_verlet_initial": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),
     "tmps_verlet_final": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),

@@ -17,6 +17,10 @@ constexpr int kMaxSlots = 64;  // one bit per slot in the touch mask
 
 namespace tmps {
 
+// Number of kernels this library has launched (all entry points, all
+// threads); read through tmps_launch_count().
+void note_launches(int k);
+
 inline int grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     return (int)(g < 1 ? 1 : g);

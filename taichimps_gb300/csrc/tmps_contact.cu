@@ -161,6 +161,7 @@ int tmps_contact(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
         case 3: k_contact64<3><<<g, kBlock, 0, s>>>(*a, *nl, *p, d_box, dt, shearupdate, accumulate); break;
         default: k_contact64<4><<<g, kBlock, 0, s>>>(*a, *nl, *p, d_box, dt, shearupdate, accumulate); break;
     }
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 

@@ -4,6 +4,7 @@
 //
 // Each kernel restates one reference loop; the arithmetic order of every
 // expression is kept so results agree with the reference to rounding.
+#include <atomic>
 #include <cstdio>
 
 #include "tmps_common.cuh"
@@ -305,11 +306,18 @@ bool launch_ok() { return cudaPeekAtLastError() == cudaSuccess; }
 
 }  // namespace
 
+namespace tmps {
+static std::atomic<long long> g_launches{0};
+void note_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+}  // namespace tmps
+
 // =================================================================== C ABI
 
 extern "C" {
 
 const char* tmps_version(void) { return "taichimps_gb300 0.1 (sm_103a)"; }
+
+long long tmps_launch_count(void) { return tmps::g_launches.load(std::memory_order_relaxed); }
 
 int tmps_box_set(tmps_box* d_box, const tmps_box* h_box, void* stream) {
     if (!d_box || !h_box) return TMPS_ERR_BAD_ARG;
@@ -322,6 +330,7 @@ int tmps_verlet_initial(const tmps_atoms* a, double dt, void* stream) {
     if (!a || a->n < 0) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
     k_verlet_initial<<<grid_for(a->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*a, dt);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -329,6 +338,7 @@ int tmps_verlet_final(const tmps_atoms* a, double dt, void* stream) {
     if (!a || a->n < 0) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
     k_verlet_final<<<grid_for(a->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*a, dt);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -347,6 +357,7 @@ int tmps_damping_cundall(const tmps_atoms* a, double gamma_lin, double gamma_ang
     if (!a || a->n < 0) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
     k_cundall<<<grid_for(a->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*a, gamma_lin, gamma_ang);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -356,6 +367,7 @@ int tmps_skin_check(const tmps_atoms* a, double trigger_sq, int32_t stamp, int32
     if (a->n == 0) return TMPS_OK;
     k_skin_check<<<grid_for(a->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*a, trigger_sq, stamp,
                                                                               d_flag);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -363,6 +375,7 @@ int tmps_pbc(const tmps_atoms* a, const tmps_box* d_box, void* stream) {
     if (!a || a->n < 0 || !d_box) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
     k_pbc<<<grid_for(a->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*a, d_box);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -381,6 +394,7 @@ int tmps_virial_reduce(const tmps_atoms* a, int32_t keflag, double* d_out, void*
     double* part = (double*)workspace;
     k_virial_partial<<<blocks, kBlock, 0, s>>>(*a, keflag, part);
     k_virial_final<<<1, kBlock, 0, s>>>(part, blocks, d_out);
+    note_launches(2);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -388,14 +402,19 @@ int tmps_servo_step(tmps_box* d_box, tmps_servo* d_servo, const double* d_virial
                     double frac, double dt, int32_t* d_status, void* stream) {
     if (!d_box || !d_servo || !d_virial || !d_status || !(dt > 0.0)) return TMPS_ERR_BAD_ARG;
     k_servo<<<1, 32, 0, (cudaStream_t)stream>>>(d_box, d_servo, d_virial, elapsed, frac, dt, d_status);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
 int tmps_remap_x(const tmps_atoms* a, tmps_box* d_box, void* stream) {
     if (!a || a->n < 0 || !d_box) return TMPS_ERR_BAD_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    if (a->n > 0) k_remap_x<<<grid_for(a->n, kBlock), kBlock, 0, s>>>(*a, d_box);
+    if (a->n > 0) {
+        k_remap_x<<<grid_for(a->n, kBlock), kBlock, 0, s>>>(*a, d_box);
+        note_launches(1);
+    }
     k_clear_remap_pending<<<1, 1, 0, s>>>(d_box);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 

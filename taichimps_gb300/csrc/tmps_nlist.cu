@@ -274,6 +274,7 @@ int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_bo
     k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
     k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, order, old_cell, cell_of);
     k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, d_status);
+    note_launches(6);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -283,6 +284,7 @@ int tmps_history_remap(const tmps_nlist* old_nl, const tmps_nlist* new_nl, const
     if (new_nl->n == 0) return TMPS_OK;
     k_history_remap<<<grid_for(new_nl->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*old_nl, *new_nl,
                                                                                      order);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 

@@ -212,8 +212,10 @@ class NeighborList:
 
     def check_displacement(self, atom, trigger_sq: float, stamp: int) -> None:
         L = _device.lib()
-        _lib.check(L.tmps_skin_check(atom.cstruct(), float(trigger_sq), int(stamp), self.flag.data_ptr(),
-                                     _device.stream()), "tmps_skin_check")
+        with _device.timed("skin_check"):
+            rc = L.tmps_skin_check(atom.cstruct(), float(trigger_sq), int(stamp), self.flag.data_ptr(),
+                                   _device.stream())
+        _lib.check(rc, "tmps_skin_check")
 
     def decide(self, atom, timestep: int | None = None) -> bool:
         """NeighborList.decide (neighbor.py:371-403), same rules and order."""
