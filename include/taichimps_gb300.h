@@ -36,7 +36,12 @@ enum {
     TMPS_OK = 0,
     TMPS_ERR_BAD_ARG = 1,
     TMPS_ERR_CUDA = 2,
+    TMPS_ERR_TOO_LARGE = 3,  /* beyond the fixed scratch of tmps_nlist_build_noalloc */
 };
+
+/* Size limits of tmps_nlist_build_noalloc's built-in scratch. */
+#define TMPS_NOALLOC_MAX_ATOMS 1048576
+#define TMPS_NOALLOC_MAX_CELLS 200000
 
 /* Bits of the device status word. */
 enum {
@@ -184,6 +189,25 @@ int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_bo
                      int32_t ncell, double skin, const int32_t* cell_rank, int32_t* order,
                      int32_t* cell_of, const tmps_nlist* nl, void* workspace,
                      int64_t workspace_bytes, int32_t* d_status, void* stream);
+
+/* No counterpart in the reference: tmps_nlist_build for callers that cannot
+ * allocate device memory at all -- a host whose device memory all belongs to
+ * its own fixed arena, code running while a CUDA graph is captured (no
+ * cudaMalloc allowed there), or a foreign-language host that can only pass
+ * the arrays it registered.  Same arguments and results as tmps_nlist_build
+ * minus the workspace: the scratch is one static device array built into the
+ * library (about 6.6 MB, held by every GPU that loads the library until the
+ * process exits), so it takes at most TMPS_NOALLOC_MAX_ATOMS atoms and
+ * TMPS_NOALLOC_MAX_CELLS grid cells (the reference's own cell cap) and returns
+ * TMPS_ERR_TOO_LARGE beyond that.  It calls no allocator.  The first call on
+ * a device looks up the scratch's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  Every call shares the one
+ * scratch (the counters are cleared at the start of each call): calls whose
+ * work overlaps on the GPU -- other streams, other host threads -- race; order
+ * them on one stream. */
+int tmps_nlist_build_noalloc(const tmps_atoms* src, const tmps_atoms* dst, const tmps_box* d_box,
+                             int32_t ncell, double skin, const int32_t* cell_rank, int32_t* order,
+                             int32_t* cell_of, const tmps_nlist* nl, int32_t* d_status, void* stream);
 
 /* ContactHistory.save_state + restore_state (src/taichimps/contact_history.py:91-153):
  * carries every touching contact of the old list onto the new list, keyed by

@@ -75,7 +75,8 @@ class Servo(ctypes.Structure):
     ]
 
 
-TMPS_OK, TMPS_ERR_BAD_ARG, TMPS_ERR_CUDA = 0, 1, 2
+TMPS_OK, TMPS_ERR_BAD_ARG, TMPS_ERR_CUDA, TMPS_ERR_TOO_LARGE = 0, 1, 2, 3
+NOALLOC_MAX_ATOMS, NOALLOC_MAX_CELLS = 1048576, 200000
 STATUS_NLIST_OVERFLOW, STATUS_NONFINITE, STATUS_BOX_NONPOSITIVE, STATUS_CELL_OVERFLOW = 1, 2, 4, 8
 
 # Every entry point the header declares, with its ctypes signature.
@@ -93,6 +94,8 @@ _SIGS = {
     "tmps_nlist_build": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(Atoms), c_vp, c_i32, c_f64,
                                  c_vp, c_vp, c_vp, ctypes.POINTER(NList), c_vp, ctypes.c_int64,
                                  c_vp, c_vp]),
+    "tmps_nlist_build_noalloc": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(Atoms), c_vp, c_i32, c_f64,
+                                         c_vp, c_vp, c_vp, ctypes.POINTER(NList), c_vp, c_vp]),
     "tmps_history_remap": (c_i32, [ctypes.POINTER(NList), ctypes.POINTER(NList), c_vp, c_vp]),
     "tmps_contact": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp,
                              ctypes.POINTER(PairParams), c_f64, c_i32, c_i32, c_vp]),
@@ -135,7 +138,8 @@ class TmpsError(RuntimeError):
 
 def check(rc: int, what: str) -> None:
     if rc != TMPS_OK:
-        kind = {TMPS_ERR_BAD_ARG: "bad argument", TMPS_ERR_CUDA: "CUDA launch failure"}.get(rc, str(rc))
+        kind = {TMPS_ERR_BAD_ARG: "bad argument", TMPS_ERR_CUDA: "CUDA launch failure",
+                TMPS_ERR_TOO_LARGE: "size beyond the fixed scratch"}.get(rc, str(rc))
         raise TmpsError(f"{what} failed: {kind}")
 
 

@@ -7,6 +7,8 @@
 // periodic-wrap and single-bin skip rules (neighbor.py:329-351) and the exact
 // FP64 cut test (ri + rj + skin)^2 (neighbor.py:355-359), so the pair set is
 // bit-identical to the reference's half list on the same positions.
+#include <mutex>
+
 #include "tmps_common.cuh"
 
 using namespace tmps;
@@ -289,3 +291,77 @@ int tmps_history_remap(const tmps_nlist* old_nl, const tmps_nlist* new_nl, const
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Neighbor build without any allocation by anyone.
+//
+// tmps_nlist_build wants a scratch buffer from the caller.  Some callers have
+// no way to provide one: a host whose device memory all belongs to its own
+// fixed arena, code that runs while a CUDA graph is being captured (where
+// cudaMalloc is not allowed), or a foreign-language host that can only hand
+// over the particle arrays it registered.  For them the scratch lives here, in
+// one static device array of fixed size that every GPU which loads this
+// library keeps until the process exits.  Its limits are stated in the header
+// (TMPS_NOALLOC_MAX_ATOMS, TMPS_NOALLOC_MAX_CELLS).
+namespace {
+
+constexpr size_t kWords(size_t b) { return (b + 255) / 256 * 64; }  // 256-byte aligned, in int32 words
+constexpr size_t kCountWords = kWords((size_t)TMPS_NOALLOC_MAX_CELLS * 4);
+constexpr size_t kStartWords = kWords(((size_t)TMPS_NOALLOC_MAX_CELLS + 1) * 4);
+constexpr size_t kFillWords = kWords((size_t)TMPS_NOALLOC_MAX_CELLS * 4);
+constexpr size_t kCellWords = kWords((size_t)TMPS_NOALLOC_MAX_ATOMS * 4);
+constexpr size_t kScratchWords = kCountWords + kStartWords + kFillWords + kCellWords;
+
+static __device__ __align__(256) int32_t g_build_scratch[kScratchWords];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+int32_t* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_build_scratch on the current device, looked up once per
+// device (the host-side name is only a stand-in, not a device address).
+int32_t* scratch_on_current_device() {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_build_scratch) != cudaSuccess) return nullptr;
+        g_scratch_ptr[dev] = static_cast<int32_t*>(p);
+    }
+    return g_scratch_ptr[dev];
+}
+
+}  // namespace
+
+extern "C" int tmps_nlist_build_noalloc(const tmps_atoms* src, const tmps_atoms* dst, const tmps_box* d_box,
+                                        int32_t ncell, double skin, const int32_t* cell_rank, int32_t* order,
+                                        int32_t* cell_of, const tmps_nlist* nl, int32_t* d_status,
+                                        void* stream) {
+    if (!src || !dst || !d_box || !cell_rank || !order || !cell_of || !nl || !d_status) return TMPS_ERR_BAD_ARG;
+    const int n = src->n;
+    if (n < 0 || dst->n != n || nl->n != n || nl->slots < 1 || nl->slots > kMaxSlots || !dst->x0 || ncell < 1)
+        return TMPS_ERR_BAD_ARG;
+    if (n > TMPS_NOALLOC_MAX_ATOMS || ncell > TMPS_NOALLOC_MAX_CELLS) return TMPS_ERR_TOO_LARGE;
+    if (n == 0) return TMPS_OK;
+    int32_t* base = scratch_on_current_device();
+    if (!base) return TMPS_ERR_CUDA;
+    int32_t* count = base;
+    int32_t* start = count + kCountWords;
+    int32_t* fill = start + kStartWords;
+    int32_t* old_cell = fill + kFillWords;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int m = ncell;
+    // the previous call left its counts behind: both counters must start at zero
+    if (cudaMemsetAsync(count, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
+    if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
+    const int gb = grid_for(n, kBlock);
+    k_bin<<<gb, kBlock, 0, s>>>(*src, d_box, cell_rank, old_cell, count, d_status);
+    k_scan<<<1, kScanBlock, 0, s>>>(count, start, m);
+    k_scatter<<<gb, kBlock, 0, s>>>(n, cell_rank, old_cell, start, fill, order);
+    k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
+    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, order, old_cell, cell_of);
+    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, d_status);
+    note_launches(6);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
