@@ -95,7 +95,7 @@ def make_packing(n: int, dmin: float, dmax: float, phi: float, seed: int, jitter
 
 def config1(seed: int = 1, n: int = 4000):
     """4,000 spheres, d ~ U[0.9, 1.1], phi 0.40, v ~ N(0, 0.1^2), rho 2.5."""
-    p = make_packing(n, 0.9, 1.1, 0.40, seed, vel_sigma=0.1)
+    p = make_packing(n, 0.9, 1.1, 0.40, seed, jitter=0.05, vel_sigma=0.1)
     p["density"] = 2.5
     return p
 
