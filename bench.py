@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--seed", type=int, default=2)
-    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"])
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -119,7 +119,7 @@ def make_sim(G, p, n, precision):
     nl = G.NeighborList(domain=dom, skin=SKIN, max_atoms=n, max_neighbors_per_atom=32)
     hist = G.ContactHistory(max_atoms=n, max_neighbors=32)
     pair = G.GranHertzHistory(domain=dom, **PAIR)
-    sim = G.Simulation(domain=dom, atom=atom, neighbor=nl, history=hist, pair=pair, dt=DT)
+    sim = G.Simulation(domain=dom, atom=atom, neighbor=nl, history=hist, pair=pair, dt=DT, precision=precision)
     sim.add_fix(G.FixNVESphere(domain=dom))
     sim.add_fix(G.FixDampingCundall(domain=dom, gamma_lin=CUNDALL[0], gamma_ang=CUNDALL[1]))
     sim.add_fix(G.FixDeformPressure(domain=dom, **DEFORM))
@@ -134,48 +134,57 @@ def list_stats(sim):
     return nnb, bits / max(sim.atom.nlocal, 1)
 
 
-def contact_bytes_fp64(n_nb: float, n_c: float) -> float:
-    """Algorithmic HBM bytes per atom of one FP64 contact launch: own state xr/vm/om (96), row length
-    and touch mask (4 + 8 read + 8 write), f and torque (48) and the per-atom virial (48) written,
-    4 per neighbor index, 48 per touching slot (FP64 shear read + write).  Neighbor state gathers are
-    L2 reuse after the cell re-sort and are not counted."""
-    return 96 + 4 + 16 + 48 + 48 + 4.0 * n_nb + 48.0 * n_c
+def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float) -> float:
+    """HBM bytes per atom a launch must move (reads + writes of per-atom and per-slot arrays; gathers of
+    neighbor state are L2 reuse after the cell re-sort and are not counted).
+
+    fused_a  FP64: x/v/omega records 96 r + 96 w, f/torque 48 r, 1/m 1/I 16 r, x0 24 r
+             mixed: records 96 r + 96 w, FP32 force/torque 24 r, 1/m 1/I 16 r, FP32 offset-at-build 12 r,
+                    cell 4 r, FP32 copies (pos, vel, omega) 48 w
+    fused_c  FP64: own records 96 r, 1/m 8 r, row length 4 + touch 8 r, f/torque 48 w
+             mixed: own FP32 copies 48 r, 1/m 8 r, row length 4 + touch 8 r, FP32 force/torque 24 w
+             both: 4 per neighbor index, 48 per touching slot (FP64 shear read + write)"""
+    if kernel == "fused_a":
+        return 280.0 if precision == "fp64" else 296.0
+    if kernel == "fused_c":
+        base = 164.0 if precision == "fp64" else 92.0
+        return base + 4.0 * n_nb + 48.0 * n_c
+    return 0.0
 
 
-def run_gpu_arm(args, rank, world):
+def run_gpu_arm(args, p, precision, rank, world):
+    """W warm-up + K timed steps of one run through Simulation (the fused step), one precision."""
     import torch
     import taichimps_gb300 as G
     from taichimps_gb300 import _device, _lib
-    from taichimps_gb300.packing import config2
 
     L = _lib.load()
-    p = config2(seed=args.seed + rank, n=args.n)
     n = len(p["x"])
     K, W = args.steps, args.warmup
-    sim = make_sim(G, p, n, args.precision)
-    sim.setup_run(W + K)
-    sim.init_simulation()
-    for _ in range(W):
-        sim._sub_step_inner()
+    sim = make_sim(G, p, n, precision)
+    sim.run(W)                      # setup (build + setup forces) + W warm-up steps
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    _device.TIMED = {"contact": [], "verlet_initial": [], "verlet_final": [], "cundall": [], "virial": [],
-                     "servo": [], "remap_x": [], "skin_check": []}
+    names = ["fused_a", "fused_c", "fused_s"]
     clocks = ClockSampler(torch.cuda.current_device())
+    # the timed run continues the warm-up run: the engine is re-entered without a second setup
+    eng = sim.last_engine
+    eng.begin()
+    _device.TIMED = {k: [] for k in names}
     l0 = L.tmps_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record()
-    for _ in range(K):
-        sim._sub_step_inner()
+    eng.run(K)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     launches = L.tmps_launch_count() - l0
-    clk = clocks.stop()
     timed = {k: [a.elapsed_time(b) for a, b in v] for k, v in _device.TIMED.items()}
     _device.TIMED = None
+    clk = clocks.stop()
+    eng.finish()
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -186,15 +195,18 @@ def run_gpu_arm(args, rank, world):
     sim.domain.pull()
     pressure = sim.fixes[-1].last_pressure()
     kern = {k: (sum(v) / len(v) if v else None) for k, v in timed.items()}
-    return dict(sim=sim, p=p, n=n, ms=ms, launches=launches, clocks=clk, kern_ms=kern, n_nb=n_nb, n_c=n_c,
-                pressure=pressure, builds=sim.neighbor.build_count)
+    return dict(sim=sim, n=n, ms=ms, launches=launches, clocks=clk, kern_ms=kern, n_nb=n_nb, n_c=n_c,
+                pressure=pressure, builds=sim.neighbor.build_count, rebuilds_timed=eng.rebuilds)
 
 
-def run_e2e(args, p):
-    """The same metric through the public API, from host arrays."""
+def run_e2e(args, p, precision):
+    """The same metric through the public API, from host arrays (pinned): upload, setup, K steps with a
+    read-back of the servo's pressure tensor after every step (what the reference's host servo path reads
+    each step), download of positions and velocities.  Steps are queued one at a time, so every step
+    pays a host round trip as the reference's does."""
     import torch
     import taichimps_gb300 as G
-    from taichimps_gb300.packing import config2  # noqa: F401
+    from taichimps_gb300.engine import FusedEngine
 
     n = len(p["x"])
     K = args.steps
@@ -202,22 +214,25 @@ def run_e2e(args, p):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim = make_sim(G, {"x": host["x"].numpy(), "radius": host["radius"].numpy(), "v": host["v"].numpy(),
-                       "density": p["density"], "L": p["L"]}, n, args.precision)
+                       "density": p["density"], "L": p["L"]}, n, precision)
     fix = sim.fixes[-1]
     sim.setup_run(K)
     sim.init_simulation()
+    eng = FusedEngine(sim, precision, chunk=1)
+    eng.begin()
     for _ in range(K):
-        sim._sub_step_inner()
-        fix.last_pressure()  # the per-step pressure read-back of the reference's host servo path
+        eng.run(1)
+        fix.last_pressure()
+    eng.finish()
     x = sim.atom.x.to_numpy()
     v = sim.atom.v.to_numpy()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     assert np.isfinite(x).all() and np.isfinite(v).all()
     up = n * (3 * 8 + 8 + 8 + 3 * 8)           # positions, radius, density-derived mass, velocities
-    down = n * 2 * 3 * 8 + K * (48 + 4)         # final x and v; per step pressure tensor + rebuild flag
+    down = n * 2 * 3 * 8 + K * (48 + 4 + 160)   # final x, v; per step pressure, status, engine state
     return {"value": n * K / dt, "unit": UNIT, "h2d_bytes_per_step": up / K, "d2h_bytes_per_step": down / K,
-            "seconds": dt}
+            "seconds": dt, "precision": precision}
 
 
 # ----------------------------------------------------------------- CPU (oracle)
@@ -287,6 +302,20 @@ def reference_arm(args, rank, world):
 # ----------------------------------------------------------------- main
 
 
+def oracle_pressure(p, steps):
+    """Mean pressure of the oracle after the same number of steps (same run, FP64, all cores)."""
+    from oracle import oracle as O
+    O.build()
+    sim = oracle_sim(O, p, os.cpu_count() or 1)
+    sim.run(steps)
+    return sim.last_pressure
+
+
+def rel(a, b):
+    a, b = float(a), float(b)
+    return abs(a - b) / abs(b) if b != 0.0 else (0.0 if a == 0.0 else float("inf"))
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -298,43 +327,65 @@ def main():
             print(json.dumps(out), flush=True)
         return
     import torch
+    from taichimps_gb300.packing import config2
     torch.cuda.set_device(local)
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
-    r = run_gpu_arm(args, rank, world)
+    p = config2(seed=args.seed + rank, n=args.n)
+    forms = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
+    runs = {}
+    for prec in forms:
+        runs[prec] = run_gpu_arm(args, p, prec, rank, world)
+        del runs[prec]["sim"]
+        torch.cuda.empty_cache()
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    n, K, W, ms = r["n"], args.steps, args.warmup, r["ms"]
-    value = world * n * K / (ms * 1e-3)
-    kern = r["kern_ms"]
-    dom_name = "contact"
-    bytes_atom = contact_bytes_fp64(r["n_nb"], r["n_c"])
+    head = forms[0]
+    r = runs[head]
+    n, K, W = r["n"], args.steps, args.warmup
+    values = {k: world * n * K / (v["ms"] * 1e-3) for k, v in runs.items()}
+    value = values[head]
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    peak = peaks.get("hbm_gbs", 6800.0)
+    peak = peaks.get("hbm_gbs", 6806.5)
+    kern = r["kern_ms"]
+    dom_name = max(("fused_a", "fused_c"), key=lambda k: kern.get(k) or 0.0)
+    bytes_atom = algorithmic_bytes(dom_name, head, r["n_nb"], r["n_c"])
     achieved = bytes_atom * n / (kern[dom_name] * 1e-3) / 1e9 if kern.get(dom_name) else None
-    step_share = {k: (v * K / ms if v else None) for k, v in kern.items()}
-    e2e = None if args.no_e2e else run_e2e(args, r["p"])
+    e2e = None if args.no_e2e else run_e2e(args, p, head)
     cpu = None
+    p_oracle = None
     if not args.no_cpu:
-        cpu, _ = cpu_baseline(r["p"], args.cpu_budget, K)
+        cpu, _ = cpu_baseline(p, args.cpu_budget, K)
+        p_oracle = oracle_pressure(p, W + K)
+    scal = lambda t: (t[0] + t[1] + t[2]) / 3.0
+    forms_out = {}
+    for k, v in runs.items():
+        kb = {kk: algorithmic_bytes(kk, k, v["n_nb"], v["n_c"]) for kk in ("fused_a", "fused_c")}
+        forms_out[k] = {
+            "value": values[k], "ms_per_step": v["ms"] / K, "kernel_ms": v["kern_ms"],
+            "kernel_gbs": {kk: (kb[kk] * n / (v["kern_ms"][kk] * 1e-3) / 1e9 if v["kern_ms"].get(kk) else None)
+                           for kk in kb},
+            "mean_pressure": scal(v["pressure"]), "pressure": list(map(float, v["pressure"])),
+            "mean_pressure_rel_err_vs_oracle": None if p_oracle is None else rel(scal(v["pressure"]), scal(p_oracle)),
+            "gpu_launches": v["launches"], "rebuilds_in_timed_steps": v["rebuilds_timed"]}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": r["ms"] / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / PUBLISHED_FP32,
-        "dtype": "f64", "data": "synthetic: seeded FCC-site packing, d~U[0.8,1.2], phi 0.45, at rest "
-                                "(taichimps_gb300.packing.config2)",
-        "config": {"workload": WORKLOAD, "n_atoms": n, "precision": args.precision, "parallelism": f"replicas{world}",
+        "dtype": "f32/f64 mixed" if head == "mixed" else "f64",
+        "data": "synthetic: seeded FCC-site packing, d~U[0.8,1.2], phi 0.45, at rest (taichimps_gb300.packing.config2)",
+        "config": {"workload": WORKLOAD, "n_atoms": n, "precision": head, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2: ~0.4 GB of per-atom and neighbor state per replica",
-                   "neighbors_per_atom": r["n_nb"], "contacts_per_atom": r["n_c"],
-                   "rebuilds_in_run": r["builds"]},
+                   "neighbors_per_atom": r["n_nb"], "contacts_per_atom": r["n_c"], "neighbor_builds": r["builds"]},
         "roofline": {"kernel": dom_name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": None,
                      "bytes_per_atom": bytes_atom, "kernel_ms": kern[dom_name], "peak_source": "measured"},
-        "kernel_ms": kern, "kernel_share_of_step": step_share,
+        "speedup_mixed_vs_fp64": (values["mixed"] / values["fp64"]) if len(values) == 2 else None,
+        "oracle_mean_pressure": None if p_oracle is None else scal(p_oracle),
+        "forms": forms_out,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r["launches"], "clocks": r["clocks"],
-        "pressure": list(map(float, r["pressure"])),
     }
     print(json.dumps(out), flush=True)
     if world > 1:

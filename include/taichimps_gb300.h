@@ -94,6 +94,14 @@ typedef struct tmps_atoms {
     float* om32;        /* float[n][4]: omega, inertia */
     float* f32;         /* float[3][n] contact force, mixed form */
     float* torque32;    /* float[3][n] */
+    float* o0_32;       /* float[3][n]: offsets at the last build (mixed skin check) */
+    double* rinv;       /* double[2][n]: 1/m, 1/I (fused FP64 step) */
+    /* Low words of the mixed form's double-word state: value = hi + lo with
+     * both FP32 (~48-bit significand).  pos32lo = (offset lo, radius lo),
+     * vel32lo = (v lo, 1/m), om32lo = (w lo, 1/I). */
+    float* pos32lo;
+    float* vel32lo;
+    float* om32lo;
 } tmps_atoms;
 
 /* Full neighbor list with its contact history. */
@@ -134,7 +142,48 @@ typedef struct tmps_servo {
     double lo_start[3], hi_start[3];
     double cum[3];      /* cumulative shift of pressure-controlled axes */
     double pressure[6]; /* last pressure tensor servoed on (output) */
+    /* counters used by the fused step (deform_pressure.py:1121-1123): */
+    int64_t nsteps;       /* updates since setup: elapsed = nsteps * dt */
+    int64_t nsteps_total; /* run length for final/delta/scale */
+    int64_t step_count;   /* end_of_step calls, for nevery */
+    int32_t nevery;
+    int32_t pad_;
 } tmps_servo;
+
+/* State of the fused step (tmps_fused_*), device-resident.  One step of
+ * Simulation._sub_step_inner (simulation.py:205-247) with fix nve/sphere,
+ * optional damping/cundall and optional deform/pressure is three launches:
+ *   A  second half-kick of the previous step + pending remap x + first
+ *      half-kick + drift + skin check
+ *   C  contact forces + Cundall damping + the virial (pair + kinetic) as
+ *      per-block partial sums
+ *   S  (with deform/pressure) virial total -> pressure -> servo -> new box
+ * A step whose skin check asks for a rebuild sets `aborted` in C; every
+ * later fused launch then returns at once, so many steps can be queued (or
+ * replayed as a CUDA graph) and the host rebuilds only when one does. */
+typedef struct tmps_engine {
+    int64_t step;            /* timestep of the last completed step */
+    int64_t last_build_step; /* timestep of the last neighbor build */
+    int32_t aborted;         /* a step needs a rebuild: later fused launches do nothing */
+    int32_t disp_stamp;      /* set to the step number when an atom moved more than skin/2 */
+    int32_t final_pending;   /* v holds v(t+dt/2): the last force's second half-kick is pending */
+    int32_t delay, every, check; /* neigh_modify (neighbor.py:88-95) */
+    int32_t cundall;         /* apply damping/cundall in C */
+    int32_t servo;           /* a deform/pressure fix is present */
+    int32_t mixed;           /* 1: split FP64 positions + FP32 contact arithmetic */
+    int32_t single_bin[3];   /* periodic dimension with one bin (FP32 image in C) */
+    int32_t nblocks;         /* C's grid size, = number of virial partials */
+    double dt, gamma_lin, gamma_ang, trigger_sq;
+    double lo0[3], h0[3];    /* box origin and bin size at the last build (mixed) */
+    float dlo32[4], dh32[4]; /* lo - lo0, h - h0 (mixed skin check) */
+    float h32[4], prd32[4], iprd32[4];
+    float hlo32[4], prdlo32[4]; /* low words: h = h32 + hlo32, prd = prd32 + prdlo32 */
+    double remap_scale[3];   /* new prd / old prd of the pending remap */
+    double pad2_;
+    /* FP32 copies of per-step constants, so no thread converts a double */
+    float dt_hi, dt_lo, trigger32, gamma_lin32, gamma_ang32, pad3_;
+    float eps_hi[4], eps_lo[4]; /* remap_scale - 1 as a double word (mixed) */
+} tmps_engine;
 
 /* ---- library ---------------------------------------------------------- */
 
@@ -246,6 +295,43 @@ int64_t tmps_virial_workspace_bytes(int32_t n);
  * d_box->old_lo/old_prd and remap_pending set for remap x). */
 int tmps_servo_step(tmps_box* d_box, tmps_servo* d_servo, const double* d_virial, double elapsed,
                     double frac, double dt, int32_t* d_status, void* stream);
+
+/* ---- fused step ---------------------------------------------------------
+ * The mixed form keeps positions split: an FP64 offset from the origin of
+ * the atom's cell at the last build (xr.xyz holds the offset, cell32 the
+ * cell as cx | cy << 10 | cz << 20), so an affine remap is a scale of the
+ * offset and the FP32 copies the contact kernel reads are exact to 1e-7 of a
+ * bin, not of the box.  pos32 = (offset, r), vel32 = (v, m), om32 = (w, I). */
+
+/* After a neighbor build: 1/m and 1/I for the fused step and, with
+ * d_eng->mixed, the split positions (offset from each atom's cell origin in
+ * xr, cell32, FP32 copies, o0_32).  `cell_of` is the linear cell id from
+ * tmps_nlist_build; records lo0 / h0 in d_eng. */
+int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* d_eng,
+                       const int32_t* cell_of, void* stream);
+
+/* Back from the mixed form to absolute FP64 positions in xr, and the FP32
+ * force and torque into f / torque. */
+int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream);
+
+/* Launch A (see tmps_engine). */
+int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* stream);
+
+/* Launch C: `vir_part` receives d_eng->nblocks x 6 partial sums (caller memory). */
+int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
+                 const tmps_pair_params* p, double* vir_part, void* stream);
+
+/* Launch S: pressure servo from the partial sums of C. */
+int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const double* vir_part,
+                     int32_t* d_status, void* stream);
+
+/* Grid size of launch C for n atoms (the number of virial partials). */
+int32_t tmps_fused_blocks(int32_t n);
+
+/* Applies what the fused step leaves pending -- the second half-kick of the
+ * last step and a remap x the servo asked for -- so the state is that of the
+ * reference at the end of a step. */
+int tmps_fused_settle(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* stream);
 
 /* FixDeformPressure.remap_positions (src/taichimps/EXTRA_FIX/deform_pressure.py:493-530):
  * x from the old box's lamda coordinates into the new box; clears

@@ -200,6 +200,7 @@ class FixDeformPressure(Fix):
         sv.normalize = 1 if self.normalize_pressure else 0
         sv.remap = REMAP_CODE[self.remap]
         sv.max_rate = self.max_rate
+        sv.nsteps, sv.nsteps_total, sv.step_count, sv.nevery = self.nsteps, self.nsteps_total, self.step_count, self.nevery
         return sv
 
     def setup(self, nsteps_total: int = 0, dt: float = 0.0) -> None:

@@ -39,7 +39,8 @@ class Atoms(ctypes.Structure):
         ("xr", c_vp), ("vm", c_vp), ("om", c_vp), ("f", c_vp), ("torque", c_vp), ("virial", c_vp),
         ("tag", c_vp), ("uid", c_vp), ("x0", c_vp),
         ("pos32", c_vp), ("cell32", c_vp), ("vel32", c_vp), ("om32", c_vp), ("f32", c_vp),
-        ("torque32", c_vp),
+        ("torque32", c_vp), ("o0_32", c_vp), ("rinv", c_vp), ("pos32lo", c_vp), ("vel32lo", c_vp),
+        ("om32lo", c_vp),
     ]
 
 
@@ -72,6 +73,28 @@ class Servo(ctypes.Structure):
         ("amp", c_f64 * 3), ("tper", c_f64 * 3), ("ptarget", c_f64 * 3), ("pgain", c_f64 * 3),
         ("lo_start", c_f64 * 3), ("hi_start", c_f64 * 3), ("cum", c_f64 * 3),
         ("pressure", c_f64 * 6),
+        ("nsteps", ctypes.c_int64), ("nsteps_total", ctypes.c_int64), ("step_count", ctypes.c_int64),
+        ("nevery", c_i32), ("pad_", c_i32),
+    ]
+
+
+class Engine(ctypes.Structure):
+    """tmps_engine"""
+
+    _fields_ = [
+        ("step", ctypes.c_int64), ("last_build_step", ctypes.c_int64),
+        ("aborted", c_i32), ("disp_stamp", c_i32), ("final_pending", c_i32),
+        ("delay", c_i32), ("every", c_i32), ("check", c_i32),
+        ("cundall", c_i32), ("servo", c_i32), ("mixed", c_i32), ("single_bin", c_i32 * 3), ("nblocks", c_i32),
+        ("dt", c_f64), ("gamma_lin", c_f64), ("gamma_ang", c_f64), ("trigger_sq", c_f64),
+        ("lo0", c_f64 * 3), ("h0", c_f64 * 3),
+        ("dlo32", ctypes.c_float * 4), ("dh32", ctypes.c_float * 4),
+        ("h32", ctypes.c_float * 4), ("prd32", ctypes.c_float * 4), ("iprd32", ctypes.c_float * 4),
+        ("hlo32", ctypes.c_float * 4), ("prdlo32", ctypes.c_float * 4),
+        ("remap_scale", c_f64 * 3), ("pad2_", c_f64),
+        ("dt_hi", ctypes.c_float), ("dt_lo", ctypes.c_float), ("trigger32", ctypes.c_float),
+        ("gamma_lin32", ctypes.c_float), ("gamma_ang32", ctypes.c_float), ("pad3_", ctypes.c_float),
+        ("eps_hi", ctypes.c_float * 4), ("eps_lo", ctypes.c_float * 4),
     ]
 
 
@@ -103,6 +126,14 @@ _SIGS = {
     "tmps_virial_workspace_bytes": (ctypes.c_int64, [c_i32]),
     "tmps_servo_step": (c_i32, [c_vp, c_vp, c_vp, c_f64, c_f64, c_f64, c_vp, c_vp]),
     "tmps_remap_x": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
+    "tmps_fused_prepare": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp, c_vp]),
+    "tmps_mixed_unpack": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
+    "tmps_fused_a": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp]),
+    "tmps_fused_c": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
+                             ctypes.POINTER(PairParams), c_vp, c_vp]),
+    "tmps_fused_servo": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "tmps_fused_blocks": (c_i32, [c_i32]),
+    "tmps_fused_settle": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp]),
 }
 
 _lib: ctypes.CDLL | None = None

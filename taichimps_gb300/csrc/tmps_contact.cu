@@ -62,6 +62,8 @@ __global__ void __launch_bounds__(kBlock)
         in.rb = xb.w;
         const double radsum = in.ra + in.rb;
         if (!(in.rsq < radsum * radsum && in.rsq > 1e-28)) continue;
+        in.r = sqrt(in.rsq);
+        in.delta = radsum - in.r;
         const double4 vj = ld4(A.vm, j), wj = ld4(A.om, j);
         const double4 va = lo ? vi : vj, vb = lo ? vj : vi, wa = lo ? wi : wj, wb = lo ? wj : wi;
         double dv[3] = {0, 0, 0};

@@ -42,6 +42,8 @@ template <typename T>
 struct PairIn {
     T d[3];      // x_a - x_b, minimum image
     T rsq;
+    T r;         // |d|
+    T delta;     // overlap ra + rb - r (the caller may form it more accurately than T allows)
     T ra, rb, ma, mb;
     T va[3], vb[3];  // vb already shifted by the remap-v image velocity
     T wa[3], wb[3];
@@ -54,17 +56,17 @@ struct PairOut {
     T arm_a, arm_b;
 };
 
-// Returns true when the pair is in contact.  `sh` (canonical sense) is read
-// and written only by history styles; `has_hist` says whether the slot held a
-// live contact before this call (the reference's partner == jtag test).
+// One contact (the caller has established rsq < (ra + rb)^2 and supplies r and
+// the overlap).  `sh` (canonical sense) is read and written only by history
+// styles; the caller passes zeros when the slot held no live contact (the
+// reference's partner != jtag reset).
 template <typename T, int STYLE>
 TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, const PairIn<T>& in,
                           double* sh, PairOut<T>& out) {
     using S = StyleTraits<STYLE>;
-    const T radsum = in.ra + in.rb;
     if constexpr (S::legacy) {
-        const T r = sqrt(in.rsq);
-        const T delta = radsum - r;
+        const T r = in.r;
+        const T delta = in.delta;
         T polyhertz = T(1);
         if constexpr (S::hertz) {
             const T reff = (in.ra * in.rb) / (in.ra + in.rb);
@@ -147,13 +149,13 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
         out.arm_a = -in.ra;
         out.arm_b = -in.rb;
     } else {
-        const T r = sqrt(in.rsq);
+        const T r = in.r;
         const T rinv = T(1) / r;
         T nv[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) nv[k] = in.d[k] * rinv;
-        const T delta = radsum - r;
-        const T reff = (in.ra * in.rb) / radsum;
+        const T delta = in.delta;
+        const T reff = (in.ra * in.rb) / (in.ra + in.rb);
         const T meff = (in.ma * in.mb) / (in.ma + in.mb);
         const T a = sqrt(delta * reff);
         T vr[3], vt[3], wr[3], cr[3], vtr[3];

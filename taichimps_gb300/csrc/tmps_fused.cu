@@ -1,0 +1,871 @@
+// The fused step: Simulation._sub_step_inner (simulation.py:205-247) for
+// fix nve/sphere + optional damping/cundall + optional deform/pressure, as
+// three launches per step with no host round trip (see tmps_engine in the
+// header).
+//
+//   A  final half-kick of the previous step, pending remap x, first
+//      half-kick, drift, skin check          (nve_sphere.py:114-153,
+//                                             deform_pressure.py:512-530,
+//                                             neighbor.py:242-245)
+//   C  contact law + Cundall damping + pair and kinetic virial
+//                                            (GRANULAR/*, damping_cundall.py:214-224,
+//                                             thermo.py:89-102)
+//   S  rebuild decision, virial total, servo (neighbor.py:371-403,
+//                                             deform_pressure.py:598-702)
+//
+// Two arithmetic forms share the launch structure:
+//   FP64:  absolute FP64 positions, every operation FP64 (divisions by m and
+//          I become products with 1/m, 1/I computed at each rebuild).
+//   mixed: split positions (FP64 offset from the atom's cell origin at the
+//          last build), FP32 contact arithmetic and FP32 per-atom force
+//          accumulation; FP64 kept for the velocity and position updates, the
+//          per-contact shear history and the virial reduction.
+#include "tmps_contact.cuh"
+
+using namespace tmps;
+
+namespace {
+
+constexpr int kBlockA = 256;
+constexpr int kBlockC = 128;
+
+// Error-free transformations in FP32 (Knuth's two-sum; FMA for products):
+// s + e == a + b exactly.  Used to form the separation and the overlap of a
+// near-contact pair to ~2^-48 relative precision out of FP32 words.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// hi + lo of a double as two floats
+__device__ __forceinline__ void split(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// |a| >= |b| (or a == 0): s + e == a + b exactly
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// (hi, lo) += b for a double-word value hi + lo
+__device__ __forceinline__ void dw_add(float& hi, float& lo, float b) {
+    float s, e;
+    two_sum(hi, b, s, e);
+    fast_two_sum(s, __fadd_rn(e, lo), hi, lo);
+}
+
+// (hi, lo) += (bh, bl)
+__device__ __forceinline__ void dw_add2(float& hi, float& lo, float bh, float bl) {
+    float s, e;
+    two_sum(hi, bh, s, e);
+    fast_two_sum(s, __fadd_rn(e, __fadd_rn(lo, bl)), hi, lo);
+}
+
+// (hi, lo) += (ah + al) * (bh + bl), dropping al * bl
+__device__ __forceinline__ void dw_add_prod(float& hi, float& lo, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    const float pe = __fmaf_rn(ah, bh, -p);  // exact error of the product
+    const float t = __fadd_rn(pe, __fadd_rn(__fmul_rn(ah, bl), __fmul_rn(al, bh)));
+    dw_add2(hi, lo, p, t);
+}
+
+__device__ __forceinline__ bool rebuild_due(const tmps_engine* __restrict__ e, int64_t s) {
+    const int64_t since = s - e->last_build_step;
+    if (since <= 0) return false;  // built in this very step already
+    if (since < e->delay) return false;
+    if (e->every > 0 && since % e->every != 0) return false;
+    if (!e->check) return true;
+    return e->disp_stamp == (int32_t)s;
+}
+
+// ------------------------------------------------------------------- A, FP64
+
+__global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                  tmps_engine* __restrict__ e) {
+    if (e->aborted) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    const int32_t s = (int32_t)(e->step + 1);
+    bool hit = false;
+    if (i < n) {
+        const double dt = e->dt, dtf = 0.5 * dt;
+        double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
+        const double im = a.rinv[i], iI = a.rinv[n + i];
+        const double f[3] = {a.f[i], a.f[n + i], a.f[2 * n + i]};
+        const double t[3] = {a.torque[i], a.torque[n + i], a.torque[2 * n + i]};
+        if (e->final_pending) {  // second half-kick of the previous step
+            v.x += dtf * (f[0] * im); v.y += dtf * (f[1] * im); v.z += dtf * (f[2] * im);
+            w.x += dtf * (t[0] * iI); w.y += dtf * (t[1] * iI); w.z += dtf * (t[2] * iI);
+        }
+        if (b->remap_pending) {  // remap x of the previous step's servo update
+            x.x = b->lo[0] + (x.x - b->old_lo[0]) * e->remap_scale[0];
+            x.y = b->lo[1] + (x.y - b->old_lo[1]) * e->remap_scale[1];
+            x.z = b->lo[2] + (x.z - b->old_lo[2]) * e->remap_scale[2];
+        }
+        v.x += dtf * (f[0] * im); v.y += dtf * (f[1] * im); v.z += dtf * (f[2] * im);
+        x.x = x.x + dt * v.x; x.y = x.y + dt * v.y; x.z = x.z + dt * v.z;
+        w.x += dtf * (t[0] * iI); w.y += dtf * (t[1] * iI); w.z += dtf * (t[2] * iI);
+        st4(a.xr, i, x);
+        st4(a.vm, i, v);
+        st4(a.om, i, w);
+        const double d0 = __dsub_rn(x.x, a.x0[i]), d1 = __dsub_rn(x.y, a.x0[n + i]),
+                     d2 = __dsub_rn(x.z, a.x0[2 * n + i]);
+        hit = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)) > e->trigger_sq;
+    }
+    if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) e->disp_stamp = s;
+}
+
+// ------------------------------------------------------------------ A, mixed
+
+__device__ __forceinline__ int cell_x(int32_t c) { return c & 1023; }
+__device__ __forceinline__ int cell_y(int32_t c) { return (c >> 10) & 1023; }
+__device__ __forceinline__ int cell_z(int32_t c) { return (c >> 20) & 1023; }
+
+__global__ void __launch_bounds__(kBlockA) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                  tmps_engine* __restrict__ e) {
+    // Double-word state (hi + lo, both FP32) updated with error-free FP32
+    // transforms: the FP64 pipe of this part is ~70x narrower than FP32, and
+    // a double<->float conversion costs as much as a DFMA, so this kernel
+    // issues no FP64 instruction at all.
+    if (e->aborted) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    const int32_t s = (int32_t)(e->step + 1);
+    bool hit = false;
+    if (i < n) {
+        const float dth = e->dt_hi, dtl = e->dt_lo;
+        // merged half-kicks: the previous step's second and this step's first
+        const float kick = e->final_pending ? dth : 0.5f * dth;
+        float4 p = ld4f(a.pos32, i), pl = ld4f(a.pos32lo, i);
+        float4 v = ld4f(a.vel32, i), vl = ld4f(a.vel32lo, i);
+        float4 w = ld4f(a.om32, i), wl = ld4f(a.om32lo, i);
+        const float km = kick * vl.w, kI = kick * wl.w;  // vel32lo.w = 1/m, om32lo.w = 1/I
+        dw_add(v.x, vl.x, km * a.f32[i]);
+        dw_add(v.y, vl.y, km * a.f32[n + i]);
+        dw_add(v.z, vl.z, km * a.f32[2 * n + i]);
+        dw_add(w.x, wl.x, kI * a.torque32[i]);
+        dw_add(w.y, wl.y, kI * a.torque32[n + i]);
+        dw_add(w.z, wl.z, kI * a.torque32[2 * n + i]);
+        if (b->remap_pending) {
+            // remap x scales a cell-relative offset with the box: o += o * eps
+            dw_add(p.x, pl.x, p.x * e->eps_hi[0] + (p.x * e->eps_lo[0] + pl.x * e->eps_hi[0]));
+            dw_add(p.y, pl.y, p.y * e->eps_hi[1] + (p.y * e->eps_lo[1] + pl.y * e->eps_hi[1]));
+            dw_add(p.z, pl.z, p.z * e->eps_hi[2] + (p.z * e->eps_lo[2] + pl.z * e->eps_hi[2]));
+        }
+        // drift o += dt * v in double words
+        dw_add_prod(p.x, pl.x, dth, dtl, v.x, vl.x);
+        dw_add_prod(p.y, pl.y, dth, dtl, v.y, vl.y);
+        dw_add_prod(p.z, pl.z, dth, dtl, v.z, vl.z);
+        st4f(a.pos32, i, p);
+        st4f(a.pos32lo, i, pl);
+        st4f(a.vel32, i, v);
+        st4f(a.vel32lo, i, vl);
+        st4f(a.om32, i, w);
+        st4f(a.om32lo, i, wl);
+        // displacement since the build: offset change + cell origin change
+        const int32_t c = a.cell32[i];
+        const float d0 = ((p.x - a.o0_32[i]) + pl.x) + (float)cell_x(c) * e->dh32[0] + e->dlo32[0];
+        const float d1 = ((p.y - a.o0_32[n + i]) + pl.y) + (float)cell_y(c) * e->dh32[1] + e->dlo32[1];
+        const float d2 = ((p.z - a.o0_32[2 * n + i]) + pl.z) + (float)cell_z(c) * e->dh32[2] + e->dlo32[2];
+        hit = (d0 * d0 + d1 * d1) + d2 * d2 > e->trigger32;
+    }
+    if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) e->disp_stamp = s;
+}
+
+// ---------------------------------------------------------------------- C
+
+template <int STYLE, bool MIXED>
+__global__ void __launch_bounds__(kBlockC)
+    k_c(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
+        tmps_engine* __restrict__ E, double* __restrict__ part) {
+    using T = typename std::conditional<MIXED, float, double>::type;
+    __shared__ double smem[6 * (kBlockC / 32)];
+    if (E->aborted) return;
+    const int64_t s = E->step + 1;
+    if (rebuild_due(E, s)) return;  // S marks the step aborted; the host rebuilds
+    constexpr bool kHist = STYLE == STYLE_HOOKE_HISTORY || STYLE == STYLE_HERTZ_HISTORY || STYLE == STYLE_GRANULAR;
+    const bool hist = kHist && (STYLE != STYLE_GRANULAR || P.tangential_id >= 2);
+    const int n = A.n;
+    T dt;
+    if constexpr (MIXED) dt = E->dt_hi;
+    else dt = E->dt;
+    double Vd[6] = {0, 0, 0, 0, 0, 0};
+    float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};  // mixed: per-thread double words
+    // grid-stride: the grid is sized to the GPU (tmps_fused_blocks), so the
+    // servo sums one virial partial per resident block, not per 128 atoms
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
+        T xi[3], ri, mi, vi[3], wi[3];
+        T hh[3] = {0, 0, 0}, prd[3], iprd[3];
+        int per[3], single[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            per[c] = B->per[c];
+            if constexpr (MIXED) {
+                hh[c] = E->h32[c];
+                prd[c] = E->prd32[c];
+                iprd[c] = E->iprd32[c];
+                single[c] = E->single_bin[c];
+            } else {
+                prd[c] = B->prd[c];
+                iprd[c] = B->inv_prd[c];
+                single[c] = 0;
+            }
+        }
+        int32_t ci = 0;
+        if constexpr (MIXED) {
+            const float4 p = ld4f(A.pos32, i), v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
+            xi[0] = p.x; xi[1] = p.y; xi[2] = p.z; ri = p.w;
+            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+            if (B->vremap) ci = A.cell32[i];
+        } else {
+            const double4 p = ld4(A.xr, i), v = ld4(A.vm, i), w = ld4(A.om, i);
+            xi[0] = p.x; xi[1] = p.y; xi[2] = p.z; ri = p.w;
+            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+        }
+        const int nn = L.nnb[i];
+        const uint64_t touch = hist ? L.touch[i] : 0ull;
+        uint64_t newtouch = 0ull;
+        const size_t ss = (size_t)L.slots * n;
+        for (int k = 0; k < nn; ++k) {
+            const int e = L.nbr[(size_t)k * n + i];
+            const int j = e & kNbrIndexMask;
+            const bool lo = i < j;
+            T xj[3], rj;
+            if constexpr (MIXED) {
+                const float4 p = ld4f(A.pos32, j);
+                xj[0] = p.x; xj[1] = p.y; xj[2] = p.z; rj = p.w;
+            } else {
+                const double4 p = ld4(A.xr, j);
+                xj[0] = p.x; xj[1] = p.y; xj[2] = p.z; rj = p.w;
+            }
+            // separation x_i - x_j
+            T d[3];
+            T nimg[3] = {0, 0, 0};
+            if constexpr (MIXED) {
+                // offsets are relative to each atom's own cell: j's cell is the
+                // stencil offset (ox, oy, oz) away from i's, so
+                // x_i - x_j = (o_i - o_j) - offset * h
+                const int code = (unsigned)e >> kNbrIndexBits;
+                const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    d[c] = (xi[c] - xj[c]) - (float)off[c] * hh[c];
+                    if (single[c]) {
+                        nimg[c] = rintf(d[c] * iprd[c]);
+                        d[c] -= nimg[c] * prd[c];
+                    }
+                }
+                if (B->vremap) {  // image count for the partner velocity shift
+                    const int32_t cj = A.cell32[j];
+                    const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
+                                       cell_z(ci) + off[2] - cell_z(cj)};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / B->g[c]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    d[c] = xi[c] - xj[c];
+                    if (per[c] == 1) {
+                        nimg[c] = rint(d[c] * iprd[c]);
+                        d[c] -= nimg[c] * prd[c];
+                    }
+                }
+            }
+            PairIn<T> in;
+            const T sg = lo ? T(1) : T(-1);
+            in.ra = lo ? ri : rj;
+            in.rb = lo ? rj : ri;
+            if constexpr (MIXED) {
+                // FP32 screen, with room for the FP32 rounding of the words
+                const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                const float rs = (ri + rj) * 1.00001f;
+                if (!(rq < rs * rs)) continue;
+                // near contact: separation, |d|^2, |d| and the overlap from the
+                // high and low FP32 words, so the overlap keeps ~2^-48 of |d|
+                // (an FP32 difference of two unit-size numbers would keep 2^-24)
+                const int code = (unsigned)e >> kNbrIndexBits;
+                const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+                const float4 il = ld4f(A.pos32lo, i), jl = ld4f(A.pos32lo, j);
+                const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
+                float dh[3], dl[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float s1, e1, s2, e2;
+                    two_sum(xi[c], -xj[c], s1, e1);
+                    two_sum(s1, -(float)off[c] * hh[c], s2, e2);
+                    const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), (float)off[c] * E->hlo32[c]),
+                                                __fadd_rn(e1, e2));
+                    two_sum(s2, low, dh[c], dl[c]);
+                    if (single[c]) {
+                        const float ni = rintf(dh[c] * iprd[c]);
+                        float s3, e3;
+                        two_sum(dh[c], -ni * prd[c], s3, e3);
+                        two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * E->prdlo32[c]), e3), dh[c], dl[c]);
+                    }
+                    dh[c] = sg * dh[c];
+                    dl[c] = sg * dl[c];
+                }
+                // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
+                float p[3], pe[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    p[c] = __fmul_rn(dh[c], dh[c]);
+                    pe[c] = __fmaf_rn(dh[c], dh[c], -p[c]);
+                }
+                float t1, te1, rh, re;
+                two_sum(p[0], p[1], t1, te1);
+                two_sum(t1, p[2], rh, re);
+                const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]), __fmul_rn(dh[1], dl[1])),
+                                                             __fmul_rn(dh[2], dl[2])));
+                const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])), cross);
+                float rsh, rsl;
+                two_sum(rh, rl0, rsh, rsl);
+                const float r_hi = __fsqrt_rn(rsh);
+                const float res = __fmaf_rn(-r_hi, r_hi, rsh);  // exact
+                const float r_lo = __fdiv_rn(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
+                // ra + rb, both words
+                const float4 al = lo ? il : jl, bl = lo ? jl : il;
+                float sh_, se_;
+                two_sum(in.ra, in.rb, sh_, se_);
+                const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
+                const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
+                if (!(delta > 0.0f && rsh > 1e-28f)) continue;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
+                in.rsq = rsh;
+                in.r = r_hi;
+                in.delta = delta;
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
+                in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
+                const T radsum = in.ra + in.rb;
+                if (!(in.rsq < radsum * radsum && in.rsq > T(1e-28))) continue;
+                in.r = sqrt(in.rsq);
+                in.delta = radsum - in.r;
+            }
+            T vj[3], wj[3], mj;
+            if constexpr (MIXED) {
+                const float4 v = ld4f(A.vel32, j), w = ld4f(A.om32, j);
+                vj[0] = v.x; vj[1] = v.y; vj[2] = v.z; mj = v.w;
+                wj[0] = w.x; wj[1] = w.y; wj[2] = w.z;
+            } else {
+                const double4 v = ld4(A.vm, j), w = ld4(A.om, j);
+                vj[0] = v.x; vj[1] = v.y; vj[2] = v.z; mj = v.w;
+                wj[0] = w.x; wj[1] = w.y; wj[2] = w.z;
+            }
+            T dv[3] = {0, 0, 0};
+            if (B->vremap) {
+                // image count of x_a - x_b, then n . h_rate for partner b
+                T na[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
+                const double* h = B->h_rate;
+                dv[0] = (T)((na[0] * (T)h[0] + na[1] * (T)h[5]) + na[2] * (T)h[4]);
+                dv[1] = (T)(na[1] * (T)h[1] + na[2] * (T)h[3]);
+                dv[2] = (T)(na[2] * (T)h[2]);
+            }
+            in.ma = lo ? mi : mj;
+            in.mb = lo ? mj : mi;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                in.va[c] = lo ? vi[c] : vj[c];
+                in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
+                in.wa[c] = lo ? wi[c] : wj[c];
+                in.wb[c] = lo ? wj[c] : wi[c];
+            }
+            double sh[3] = {0, 0, 0};
+            const size_t so = (size_t)k * n + i;
+            if (hist && ((touch >> k) & 1ull)) {
+                const double sgd = lo ? 1.0 : -1.0;
+                sh[0] = sgd * L.shear[so];
+                sh[1] = sgd * L.shear[ss + so];
+                sh[2] = sgd * L.shear[2 * ss + so];
+            }
+            PairOut<T> out;
+            contact_law<T, STYLE>(P, dt, 1, in, sh, out);
+            if (hist) {
+                const double sgd = lo ? 1.0 : -1.0;
+                L.shear[so] = sgd * sh[0];
+                L.shear[ss + so] = sgd * sh[1];
+                L.shear[2 * ss + so] = sgd * sh[2];
+                newtouch |= 1ull << k;
+            }
+            const T arm = lo ? out.arm_a : out.arm_b;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                F[c] += sg * out.f[c];
+                Tq[c] += arm * out.tor[c];
+            }
+            V[0] += T(0.5) * (in.d[0] * out.f[0]);
+            V[1] += T(0.5) * (in.d[1] * out.f[1]);
+            V[2] += T(0.5) * (in.d[2] * out.f[2]);
+            V[3] += T(0.5) * (in.d[0] * out.f[1]);
+            V[4] += T(0.5) * (in.d[0] * out.f[2]);
+            V[5] += T(0.5) * (in.d[1] * out.f[2]);
+        }
+        if (hist && newtouch != touch) L.touch[i] = newtouch;
+        if (E->cundall) {  // FixDampingCundall.post_force_kernel
+            T gl, ga;
+            if constexpr (MIXED) {
+                gl = E->gamma_lin32;
+                ga = E->gamma_ang32;
+            } else {
+                gl = E->gamma_lin;
+                ga = E->gamma_ang;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T sf = F[c] * vi[c] >= T(0) ? T(1) : T(-1);
+                F[c] *= T(1) - gl * sf;
+                const T st = Tq[c] * wi[c] >= T(0) ? T(1) : T(-1);
+                Tq[c] *= T(1) - ga * st;
+            }
+        }
+        if constexpr (MIXED) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                A.f32[c * n + i] = F[c];
+                A.torque32[c * n + i] = Tq[c];
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                A.f[c * n + i] = F[c];
+                A.torque[c * n + i] = Tq[c];
+            }
+        }
+        // kinetic part of the virial with the end-of-step velocity
+        // v(t+dt) = v(t+dt/2) + dt/2 f/m (thermo.py:94-101)
+        T im;
+        if constexpr (MIXED) im = 1.0f / mi;
+        else im = A.rinv[i];
+        const T hdt = T(0.5) * dt;
+        T vf[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vf[c] = vi[c] + hdt * (F[c] * im);
+        const T kin[6] = {(mi * vf[0]) * vf[0], (mi * vf[1]) * vf[1], (mi * vf[2]) * vf[2],
+                          (mi * vf[0]) * vf[1], (mi * vf[0]) * vf[2], (mi * vf[1]) * vf[2]};
+        if constexpr (MIXED) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                dw_add(Vh[c], Vl[c], V[c]);
+                dw_add(Vh[c], Vl[c], kin[c]);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) Vd[c] += V[c] + kin[c];
+        }
+    }
+    if constexpr (MIXED) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) Vd[c] = (double)Vh[c] + (double)Vl[c];
+    }
+    block_sum<6, kBlockC>(Vd, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = Vd[c];
+        if (blockIdx.x == 0) E->final_pending = 1;
+    }
+}
+
+// ---------------------------------------------------------------------- S
+
+__device__ double limit_rate_f(double rate, double ptarget, int normalize, double max_rate) {
+    double out = rate;
+    if (normalize) {
+        if (ptarget == 0.0) {
+            if (out != 0.0) out = copysign(max_rate, out);
+        } else {
+            out = out / fabs(ptarget);
+        }
+    }
+    if (max_rate != 0.0 && fabs(out) > max_rate) out = copysign(max_rate, out);
+    return out;
+}
+
+constexpr int kBlockS = 256;
+
+__global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps_engine* e, const double* part,
+                                               int32_t* status) {
+    __shared__ double smem[6 * (kBlockS / 32)];
+    if (e->aborted) return;
+    const int64_t s = e->step + 1;
+    if (rebuild_due(e, s)) {
+        if (threadIdx.x == 0) e->aborted = 1;
+        return;
+    }
+    const bool servo_now = e->servo && ((sv->step_count + 1) % sv->nevery == 0);
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    if (servo_now) {
+        const int np = e->nblocks;
+        for (int p = threadIdx.x; p < np; p += blockDim.x)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] += part[(size_t)p * 6 + c];
+        block_sum<6, kBlockS>(acc, smem);
+    }
+    if (threadIdx.x != 0) return;
+    e->step = s;
+    b->remap_pending = 0;
+    if (!e->servo) return;
+    sv->step_count += 1;
+    sv->nsteps += 1;
+    if (!servo_now) return;
+    const double dt = e->dt;
+    const double elapsed = (double)sv->nsteps * dt;
+    const double frac = sv->nsteps_total > 0 ? (double)sv->nsteps / (double)sv->nsteps_total : 0.0;
+    double lo[3], hi[3], prd[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = b->lo[d];
+        hi[d] = b->hi[d];
+        prd[d] = b->prd[d];
+    }
+    const double vol = prd[0] * prd[1] * prd[2];
+    double t[6];
+    for (int k = 0; k < 6; ++k) t[k] = vol > 0.0 ? acc[k] / vol : 0.0;
+    for (int k = 0; k < 6; ++k) sv->pressure[k] = t[k];
+    const double scalar = ((t[0] + t[1]) + t[2]) / 3.0;
+    double p[3] = {t[0], t[1], t[2]};
+    if (sv->couple == 1) {
+        p[0] = p[1] = p[2] = scalar;
+    } else if (sv->couple == 2) {
+        const double m = (t[0] + t[1]) / 2.0; p[0] = m; p[1] = m;
+    } else if (sv->couple == 3) {
+        const double m = (t[1] + t[2]) / 2.0; p[1] = m; p[2] = m;
+    } else if (sv->couple == 4) {
+        const double m = (t[0] + t[2]) / 2.0; p[0] = m; p[2] = m;
+    }
+    double nlo[3], nhi[3];
+    for (int d = 0; d < 3; ++d) {
+        const int st = sv->style[d];
+        const double ls = sv->lo_start[d], hs = sv->hi_start[d];
+        nlo[d] = lo[d];
+        nhi[d] = hi[d];
+        if (st == 1) {
+            const double shift = ((0.5 * elapsed) * sv->rate[d]) * (hs - ls);
+            nlo[d] = ls - shift; nhi[d] = hs + shift;
+        } else if (st == 2) {
+            const double mid = 0.5 * (ls + hs);
+            const double half = (0.5 * (hs - ls)) * exp(sv->rate[d] * elapsed);
+            nlo[d] = mid - half; nhi[d] = mid + half;
+        } else if (st == 3) {
+            const double shift = (0.5 * elapsed) * sv->vel[d];
+            nlo[d] = ls - shift; nhi[d] = hs + shift;
+        } else if (st == 4) {
+            const double shift = (0.5 * sv->amp[d]) * sin(((2.0 * 3.14159265358979323846) * elapsed) / sv->tper[d]);
+            nlo[d] = ls - shift; nhi[d] = hs + shift;
+        } else if (st == 5) {
+            nlo[d] = ls + frac * (sv->flo[d] - ls);
+            nhi[d] = hs + frac * (sv->fhi[d] - hs);
+        } else if (st == 6) {
+            const double lo_stop = ls + sv->dlo[d], hi_stop = hs + sv->dhi[d];
+            nlo[d] = ls + frac * (lo_stop - ls);
+            nhi[d] = hs + frac * (hi_stop - hs);
+        } else if (st == 7) {
+            const double mid = 0.5 * (ls + hs);
+            const double half = (0.5 * sv->scale[d]) * (hs - ls);
+            nlo[d] = ls + frac * ((mid - half) - ls);
+            nhi[d] = hs + frac * ((mid + half) - hs);
+        } else if (st == 8 || st == 9) {
+            const double pd = (sv->couple == 0 && st == 9) ? scalar : p[d];
+            const double tgt = sv->ptarget[d];
+            const double rate = limit_rate_f(sv->pgain[d] * (pd - tgt), tgt, sv->normalize, sv->max_rate);
+            sv->cum[d] += (dt * rate) * prd[d];
+            nlo[d] = ls - 0.5 * sv->cum[d];
+            nhi[d] = hs + 0.5 * sv->cum[d];
+        }
+    }
+    double nprd[3];
+    bool bad = false;
+    for (int d = 0; d < 3; ++d) {
+        nprd[d] = nhi[d] - nlo[d];
+        bad = bad || !(nprd[d] > 0.0);
+    }
+    if (bad) {
+        *status |= TMPS_STATUS_BOX_NONPOSITIVE;
+        return;
+    }
+    for (int d = 0; d < 3; ++d) {
+        b->old_lo[d] = lo[d];
+        b->old_prd[d] = prd[d];
+        b->lo[d] = nlo[d];
+        b->hi[d] = nhi[d];
+        b->prd[d] = nprd[d];
+        b->inv_prd[d] = 1.0 / nprd[d];
+        b->hcell[d] = nprd[d] / (double)b->g[d];
+        b->h_rate[d] = (nprd[d] - prd[d]) / dt;
+        b->h_rate[3 + d] = 0.0;
+        e->remap_scale[d] = nprd[d] / prd[d];
+        split((nprd[d] - prd[d]) / prd[d], e->eps_hi[d], e->eps_lo[d]);
+        split(b->hcell[d], e->h32[d], e->hlo32[d]);
+        split(nprd[d], e->prd32[d], e->prdlo32[d]);
+        e->iprd32[d] = (float)(1.0 / nprd[d]);
+        e->dlo32[d] = (float)(nlo[d] - e->lo0[d]);
+        e->dh32[d] = (float)(b->hcell[d] - e->h0[d]);
+    }
+    b->vremap = sv->remap == 2 ? 1 : 0;
+    b->remap_pending = sv->remap == 1 ? 1 : 0;
+}
+
+// -------------------------------------------------------- prepare / unpack
+
+__global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                      const tmps_engine* __restrict__ e, const int32_t* cell_of) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    if (i >= n) return;
+    const double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
+    if (a.rinv) {
+        a.rinv[i] = 1.0 / v.w;
+        a.rinv[n + i] = 1.0 / w.w;
+    }
+    if (!e->mixed) return;
+    const int gx = b->g[0], gxy = b->g[0] * b->g[1];
+    const int lin = cell_of[i];
+    const int cz = lin / gxy, cy = (lin - cz * gxy) / gx, cx = lin - cz * gxy - cy * gx;
+    const int cc[3] = {cx, cy, cz};
+    const double xx[3] = {x.x, x.y, x.z};
+    float oh[3], ol[3];
+    for (int k = 0; k < 3; ++k) {
+        const double origin = b->lo[k] + (double)cc[k] * b->hcell[k];
+        split(xx[k] - origin, oh[k], ol[k]);
+        // the skin check's reference: the position at the last build, as an
+        // offset from the same origin (x0 is kept by the build in FP64)
+        a.o0_32[k * n + i] = (float)(a.x0[k * n + i] - origin);
+    }
+    a.cell32[i] = cx | (cy << 10) | (cz << 20);
+    float rh, rl;
+    split(x.w, rh, rl);
+    st4f(a.pos32, i, make_float4(oh[0], oh[1], oh[2], rh));
+    st4f(a.pos32lo, i, make_float4(ol[0], ol[1], ol[2], rl));
+    float vh[3], vlo[3], wh[3], wlo[3];
+    split(v.x, vh[0], vlo[0]); split(v.y, vh[1], vlo[1]); split(v.z, vh[2], vlo[2]);
+    split(w.x, wh[0], wlo[0]); split(w.y, wh[1], wlo[1]); split(w.z, wh[2], wlo[2]);
+    st4f(a.vel32, i, make_float4(vh[0], vh[1], vh[2], (float)v.w));
+    st4f(a.vel32lo, i, make_float4(vlo[0], vlo[1], vlo[2], (float)(1.0 / v.w)));
+    st4f(a.om32, i, make_float4(wh[0], wh[1], wh[2], (float)w.w));
+    st4f(a.om32lo, i, make_float4(wlo[0], wlo[1], wlo[2], (float)(1.0 / w.w)));
+}
+
+__global__ void k_prepare_engine(const tmps_box* __restrict__ b, tmps_engine* e) {
+    if (threadIdx.x || blockIdx.x) return;
+    for (int d = 0; d < 3; ++d) {
+        e->lo0[d] = b->lo[d];
+        e->h0[d] = b->hcell[d];
+        e->dlo32[d] = 0.0f;
+        e->dh32[d] = 0.0f;
+        split(b->hcell[d], e->h32[d], e->hlo32[d]);
+        split(b->prd[d], e->prd32[d], e->prdlo32[d]);
+        e->iprd32[d] = (float)b->inv_prd[d];
+        e->single_bin[d] = (b->per[d] == 1 && b->g[d] == 1) ? 1 : 0;
+        e->eps_hi[d] = 0.0f;
+        e->eps_lo[d] = 0.0f;
+    }
+    split(e->dt, e->dt_hi, e->dt_lo);
+    e->trigger32 = (float)e->trigger_sq;
+    e->gamma_lin32 = (float)e->gamma_lin;
+    e->gamma_ang32 = (float)e->gamma_ang;
+}
+
+__global__ void __launch_bounds__(kBlockA) k_unpack(tmps_atoms a, const tmps_box* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    if (i >= n) return;
+    double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
+    const float4 p = ld4f(a.pos32, i), pl = ld4f(a.pos32lo, i);
+    const float4 vv = ld4f(a.vel32, i), vl = ld4f(a.vel32lo, i);
+    const float4 ww = ld4f(a.om32, i), wl = ld4f(a.om32lo, i);
+    const int32_t c = a.cell32[i];
+    const int cc[3] = {cell_x(c), cell_y(c), cell_z(c)};
+    const float oh[3] = {p.x, p.y, p.z}, ol[3] = {pl.x, pl.y, pl.z};
+    double xx[3];
+    for (int k = 0; k < 3; ++k) xx[k] = (b->lo[k] + (double)cc[k] * b->hcell[k]) + ((double)oh[k] + (double)ol[k]);
+    x.x = xx[0]; x.y = xx[1]; x.z = xx[2];
+    v.x = (double)vv.x + (double)vl.x; v.y = (double)vv.y + (double)vl.y; v.z = (double)vv.z + (double)vl.z;
+    w.x = (double)ww.x + (double)wl.x; w.y = (double)ww.y + (double)wl.y; w.z = (double)ww.z + (double)wl.z;
+    st4(a.xr, i, x);
+    st4(a.vm, i, v);
+    st4(a.om, i, w);
+    for (int k = 0; k < 3; ++k) {
+        a.f[k * n + i] = (double)a.f32[k * n + i];
+        a.torque[k * n + i] = (double)a.torque32[k * n + i];
+    }
+}
+
+// Settle: the pending second half-kick and remap.
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlockA) k_settle(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                     const tmps_engine* __restrict__ e) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    if (i >= n) return;
+    if constexpr (MIXED) {
+        float4 p = ld4f(a.pos32, i), pl = ld4f(a.pos32lo, i);
+        float4 v = ld4f(a.vel32, i), vl = ld4f(a.vel32lo, i);
+        float4 w = ld4f(a.om32, i), wl = ld4f(a.om32lo, i);
+        if (e->final_pending) {
+            const float dtf = 0.5f * e->dt_hi;
+            const float km = dtf * vl.w, kI = dtf * wl.w;
+            dw_add(v.x, vl.x, km * a.f32[i]);
+            dw_add(v.y, vl.y, km * a.f32[n + i]);
+            dw_add(v.z, vl.z, km * a.f32[2 * n + i]);
+            dw_add(w.x, wl.x, kI * a.torque32[i]);
+            dw_add(w.y, wl.y, kI * a.torque32[n + i]);
+            dw_add(w.z, wl.z, kI * a.torque32[2 * n + i]);
+        }
+        if (b->remap_pending) {
+            dw_add(p.x, pl.x, p.x * e->eps_hi[0] + (p.x * e->eps_lo[0] + pl.x * e->eps_hi[0]));
+            dw_add(p.y, pl.y, p.y * e->eps_hi[1] + (p.y * e->eps_lo[1] + pl.y * e->eps_hi[1]));
+            dw_add(p.z, pl.z, p.z * e->eps_hi[2] + (p.z * e->eps_lo[2] + pl.z * e->eps_hi[2]));
+        }
+        st4f(a.pos32, i, p);
+        st4f(a.pos32lo, i, pl);
+        st4f(a.vel32, i, v);
+        st4f(a.vel32lo, i, vl);
+        st4f(a.om32, i, w);
+        st4f(a.om32lo, i, wl);
+        return;
+    }
+    double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
+    if (e->final_pending) {
+        {
+            const double dtf = 0.5 * e->dt, im = a.rinv[i], iI = a.rinv[n + i];
+            v.x += dtf * (a.f[i] * im); v.y += dtf * (a.f[n + i] * im); v.z += dtf * (a.f[2 * n + i] * im);
+            w.x += dtf * (a.torque[i] * iI); w.y += dtf * (a.torque[n + i] * iI);
+            w.z += dtf * (a.torque[2 * n + i] * iI);
+        }
+    }
+    if (b->remap_pending) {
+        x.x = b->lo[0] + (x.x - b->old_lo[0]) * e->remap_scale[0];
+        x.y = b->lo[1] + (x.y - b->old_lo[1]) * e->remap_scale[1];
+        x.z = b->lo[2] + (x.z - b->old_lo[2]) * e->remap_scale[2];
+    }
+    st4(a.xr, i, x);
+    st4(a.vm, i, v);
+    st4(a.om, i, w);
+}
+
+__global__ void k_settle_flags(tmps_box* b, tmps_engine* e) {
+    if (threadIdx.x || blockIdx.x) return;
+    e->final_pending = 0;
+    b->remap_pending = 0;
+}
+
+bool launch_ok() { return cudaPeekAtLastError() == cudaSuccess; }
+
+bool mixed_ok(const tmps_atoms* a) {
+    return a->pos32 && a->pos32lo && a->vel32 && a->vel32lo && a->om32 && a->om32lo && a->cell32 && a->f32 &&
+           a->torque32 && a->o0_32;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t tmps_fused_blocks(int32_t n) {
+    // one wave of resident blocks: up to 8 per SM (the contact kernel's
+    // register use allows 4-5), never more blocks than 128-atom groups
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            sms = v;
+        else
+            sms = 152;
+    }
+    const int by_atoms = n <= 0 ? 1 : grid_for(n, kBlockC);
+    return (int32_t)(by_atoms < 8 * sms ? by_atoms : 8 * sms);
+}
+
+int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* d_eng, const int32_t* cell_of,
+                       void* stream) {
+    if (!a || !d_box || !d_eng || !cell_of || a->n < 0) return TMPS_ERR_BAD_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (a->n > 0) {
+        k_prepare<<<grid_for(a->n, kBlockA), kBlockA, 0, s>>>(*a, d_box, d_eng, cell_of);
+        note_launches(1);
+    }
+    k_prepare_engine<<<1, 32, 0, s>>>(d_box, d_eng);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream) {
+    if (!a || !d_box || a->n < 0 || !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
+    if (a->n == 0) return TMPS_OK;
+    k_unpack<<<grid_for(a->n, kBlockA), kBlockA, 0, (cudaStream_t)stream>>>(*a, d_box);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* stream) {
+    if (!a || !d_box || !d_eng || a->n < 0) return TMPS_ERR_BAD_ARG;
+    if (!a->pos32 && (!a->rinv || !a->x0)) return TMPS_ERR_BAD_ARG;
+    if (a->n == 0) return TMPS_OK;
+    const int g = grid_for(a->n, kBlockA);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (a->pos32) {
+        if (!mixed_ok(a)) return TMPS_ERR_BAD_ARG;
+        k_a32<<<g, kBlockA, 0, s>>>(*a, d_box, d_eng);
+    } else {
+        k_a64<<<g, kBlockA, 0, s>>>(*a, d_box, d_eng);
+    }
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
+                 const tmps_pair_params* p, double* vir_part, void* stream) {
+    if (!a || !nl || !d_box || !d_eng || !p || !vir_part || a->n < 0 || nl->n != a->n) return TMPS_ERR_BAD_ARG;
+    if (!a->pos32 && !a->rinv) return TMPS_ERR_BAD_ARG;
+    if (p->style < 0 || p->style > 4 || nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
+    const int g = tmps_fused_blocks(a->n);
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool mixed = a->pos32 != nullptr;
+    if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
+#define TMPS_LAUNCH_C(ST)                                                                    \
+    if (mixed) k_c<ST, true><<<g, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, vir_part);      \
+    else k_c<ST, false><<<g, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, vir_part);
+    switch (p->style) {
+        case 0: TMPS_LAUNCH_C(0) break;
+        case 1: TMPS_LAUNCH_C(1) break;
+        case 2: TMPS_LAUNCH_C(2) break;
+        case 3: TMPS_LAUNCH_C(3) break;
+        default: TMPS_LAUNCH_C(4) break;
+    }
+#undef TMPS_LAUNCH_C
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const double* vir_part,
+                     int32_t* d_status, void* stream) {
+    if (!d_box || !d_servo || !d_eng || !vir_part || !d_status) return TMPS_ERR_BAD_ARG;
+    k_s<<<1, kBlockS, 0, (cudaStream_t)stream>>>(d_box, d_servo, d_eng, vir_part, d_status);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_fused_settle(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* stream) {
+    if (!a || !d_box || !d_eng || a->n < 0 || (!a->pos32 && !a->rinv)) return TMPS_ERR_BAD_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (a->n > 0) {
+        if (a->pos32) k_settle<true><<<grid_for(a->n, kBlockA), kBlockA, 0, s>>>(*a, d_box, d_eng);
+        else k_settle<false><<<grid_for(a->n, kBlockA), kBlockA, 0, s>>>(*a, d_box, d_eng);
+        note_launches(1);
+    }
+    k_settle_flags<<<1, 1, 0, s>>>(d_box, d_eng);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+}  // extern "C"

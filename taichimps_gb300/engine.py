@@ -1,0 +1,244 @@
+"""
+The fused step engine behind ``Simulation.run``.
+
+One step of Simulation._sub_step_inner (simulation.py:205-247) with fix
+nve/sphere, optionally damping/cundall and deform/pressure, becomes three
+launches (tmps_fused_a, tmps_fused_c, tmps_fused_servo) that decide on the
+device whether the step needs a neighbor rebuild.  Steps are queued in chunks
+with one host synchronisation per chunk.  When a step finds it needs a
+rebuild, every later launch of the chunk does nothing; the host then rebuilds
+exactly as the reference does at that step (save history, wrap, build,
+restore history), finishes the step, and carries on.
+
+Two precisions:
+  "fp64"  every operation FP64 (the plain FP64 form);
+  "mixed" FP32 contact arithmetic and per-atom force accumulation, FP64
+          for the velocity/position updates (split positions: FP64 offsets
+          from each atom's cell origin), the shear history and the virial
+          reduction that drives the servo.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _device, _lib
+from .EXTRA_FIX.damping_cundall import FixDampingCundall
+from .EXTRA_FIX.deform_pressure import FixDeformPressure
+
+
+def fusable(sim) -> bool:
+    """The configurations the fused step covers."""
+    if sim.integrator is None or sim.pair_style is None or sim.neighbor is None or sim.history is None:
+        return False
+    kinds = [type(f) for f in sim.fixes]
+    if any(k not in (FixDampingCundall, FixDeformPressure) for k in kinds):
+        return False
+    if kinds.count(FixDampingCundall) > 1 or kinds.count(FixDeformPressure) > 1:
+        return False
+    # damping must act on the pair force before the servo reads the virial: the
+    # reference calls post_force hooks (Cundall) and end_of_step hooks (servo) in
+    # that order regardless of insertion order, so any order is fine here.
+    return True
+
+
+class FusedEngine:
+    def __init__(self, sim, precision: str = "fp64", chunk: int = 64) -> None:
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.sim = sim
+        self.precision = precision
+        self.mixed = precision == "mixed"
+        self.chunk = int(chunk)
+        self.dev = _device.device()
+        self.cundall = next((f for f in sim.fixes if isinstance(f, FixDampingCundall)), None)
+        self.deform = next((f for f in sim.fixes if isinstance(f, FixDeformPressure)), None)
+        self._eng = _device.struct_buffer(_lib.Engine())
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self._dummy_servo = _device.struct_buffer(_lib.Servo())
+        self._n = -1
+        self.rebuilds = 0
+
+    # ------------------------------------------------------------ storage
+
+    def _alloc(self, n: int) -> None:
+        if n == self._n:
+            return
+        f64 = dict(dtype=torch.float64, device=self.dev)
+        f32 = dict(dtype=torch.float32, device=self.dev)
+        self.rinv = None if self.mixed else torch.zeros((2, n), **f64)
+        self.part = torch.zeros(int(_device.lib().tmps_fused_blocks(n)) * 6, **f64)
+        if self.mixed:
+            self.pos32 = torch.zeros((n, 4), **f32)
+            self.pos32lo = torch.zeros((n, 4), **f32)
+            self.vel32lo = torch.zeros((n, 4), **f32)
+            self.om32lo = torch.zeros((n, 4), **f32)
+            self.vel32 = torch.zeros((n, 4), **f32)
+            self.om32 = torch.zeros((n, 4), **f32)
+            self.f32 = torch.zeros((3, n), **f32)
+            self.t32 = torch.zeros((3, n), **f32)
+            self.o0 = torch.zeros((3, n), **f32)
+            self.cell32 = torch.zeros(n, dtype=torch.int32, device=self.dev)
+        self._n = n
+
+    def atoms(self) -> _lib.Atoms:
+        s = self.sim.atom.cstruct()
+        s.rinv = None if self.rinv is None else self.rinv.data_ptr()
+        if self.mixed:
+            s.pos32, s.vel32, s.om32 = self.pos32.data_ptr(), self.vel32.data_ptr(), self.om32.data_ptr()
+            s.f32, s.torque32, s.o0_32 = self.f32.data_ptr(), self.t32.data_ptr(), self.o0.data_ptr()
+            s.cell32 = self.cell32.data_ptr()
+            s.pos32lo = self.pos32lo.data_ptr()
+            s.vel32lo, s.om32lo = self.vel32lo.data_ptr(), self.om32lo.data_ptr()
+        return s
+
+    def _servo_ptr(self) -> int:
+        return self.deform._dservo.data_ptr() if self.deform is not None else self._dummy_servo.data_ptr()
+
+    # ------------------------------------------------------------ lifecycle
+
+    def begin(self) -> None:
+        """After Simulation.init_simulation(): hand the state to the fused step."""
+        sim = self.sim
+        atom, nl = sim.atom, sim.neighbor
+        n = atom.nlocal
+        self._alloc(n)
+        if self.mixed:
+            g = nl.grid_dim
+            if np.any(g > 1023):
+                raise NotImplementedError("the mixed form packs cell coordinates in 10 bits (<= 1023 bins per axis)")
+        e = _lib.Engine()
+        e.step = sim.timestep
+        e.last_build_step = nl.last_build_step
+        e.delay, e.every, e.check = int(nl.delay), max(1, int(nl.every)), 1 if nl.check else 0
+        e.cundall = 1 if self.cundall is not None else 0
+        e.servo = 1 if self.deform is not None else 0
+        e.mixed = 1 if self.mixed else 0
+        e.nblocks = int(_device.lib().tmps_fused_blocks(n))
+        e.dt = float(sim.dt)
+        if self.cundall is not None:
+            e.gamma_lin, e.gamma_ang = self.cundall.gamma_lin, self.cundall.gamma_ang
+        e.trigger_sq = 0.25 * nl.skin * nl.skin
+        e.remap_scale[0] = e.remap_scale[1] = e.remap_scale[2] = 1.0
+        _device.push_struct(self._eng, e)
+        if self.deform is not None:
+            fx = self.deform
+            sv = _device.pull_struct(fx._dservo, _lib.Servo)
+            sv.nsteps, sv.nsteps_total, sv.step_count, sv.nevery = fx.nsteps, fx.nsteps_total, fx.step_count, fx.nevery
+            _device.push_struct(fx._dservo, sv)
+        self._prepare()
+        if self.mixed:
+            # the setup forces (FP64) seed the first half-kick
+            b = atom.buffers
+            self.f32.copy_(b.f)
+            self.t32.copy_(b.torque)
+        self.status.zero_()
+
+    def _prepare(self) -> None:
+        nl = self.sim.neighbor
+        rc = _device.lib().tmps_fused_prepare(self.atoms(), self.sim.domain.dbox, self._eng.data_ptr(),
+                                              nl.cell_of.data_ptr(), _device.stream())
+        _lib.check(rc, "tmps_fused_prepare")
+
+    def _launch_step(self, L, st, atoms, nl_struct, params) -> None:
+        dbox, eng = self.sim.domain.dbox, self._eng.data_ptr()
+        with _device.timed("fused_a"):
+            rc = L.tmps_fused_a(atoms, dbox, eng, st)
+        _lib.check(rc, "tmps_fused_a")
+        with _device.timed("fused_c"):
+            rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.part.data_ptr(), st)
+        _lib.check(rc, "tmps_fused_c")
+        with _device.timed("fused_s"):
+            rc = L.tmps_fused_servo(dbox, self._servo_ptr(), eng, self.part.data_ptr(), self.status.data_ptr(), st)
+        _lib.check(rc, "tmps_fused_servo")
+
+    def _engine_state(self) -> _lib.Engine:
+        return _device.pull_struct(self._eng, _lib.Engine)
+
+    def run(self, nsteps: int) -> None:
+        """Advance `nsteps` steps."""
+        sim = self.sim
+        L = _device.lib()
+        st = _device.stream()
+        start = sim.timestep
+        target = start + int(nsteps)
+        while True:
+            e = self._engine_state()
+            done = int(e.step)
+            if e.aborted:
+                self._rebuild_step(done + 1)
+                continue
+            if done >= target:
+                break
+            atoms = self.atoms()
+            nl_struct = sim.history.cstruct(sim.neighbor)
+            params = sim.pair_style.params
+            for _ in range(min(self.chunk, target - done)):
+                self._launch_step(L, st, atoms, nl_struct, params)
+            self._check_status()
+        sim.timestep = target
+
+    def _check_status(self) -> None:
+        st = int(self.status.item())
+        if st & _lib.STATUS_BOX_NONPOSITIVE and self.deform is not None:
+            self.deform.status.fill_(st)
+            self.deform.check_status()
+
+    def _rebuild_step(self, s: int) -> None:
+        """Step `s` has had its first half-kick and drift; rebuild, then finish it."""
+        sim = self.sim
+        L = _device.lib()
+        st = _device.stream()
+        atom, nl = sim.atom, sim.neighbor
+        self.rebuilds += 1
+        sim.timestep = s
+        nl.current_step = s
+        if self.mixed:
+            _lib.check(L.tmps_mixed_unpack(self.atoms(), sim.domain.dbox, st), "tmps_mixed_unpack")
+        sim.domain.mark_device_authoritative()
+        sim.domain.pull()
+        sim.history.save_state(atom, nl)
+        sim.domain.pbc(atom)
+        nl.build(atom)
+        sim.history.restore_state(atom, nl)
+        e = self._engine_state()
+        e.aborted = 0
+        e.disp_stamp = 0
+        e.last_build_step = s
+        _device.push_struct(self._eng, e)
+        if atom.nlocal != self._n:
+            raise RuntimeError("atom count changed during a fused run")
+        self._prepare()
+        atoms = self.atoms()
+        nl_struct = sim.history.cstruct(nl)
+        dbox, eng = sim.domain.dbox, self._eng.data_ptr()
+        _lib.check(L.tmps_fused_c(atoms, nl_struct, dbox, eng, sim.pair_style.params, self.part.data_ptr(), st),
+                   "tmps_fused_c")
+        _lib.check(L.tmps_fused_servo(dbox, self._servo_ptr(), eng, self.part.data_ptr(), self.status.data_ptr(),
+                                      st), "tmps_fused_servo")
+
+    def finish(self) -> None:
+        """Settle pending updates and hand the state back to the per-hook path."""
+        sim = self.sim
+        L = _device.lib()
+        st = _device.stream()
+        atoms = self.atoms()
+        _lib.check(L.tmps_fused_settle(atoms, sim.domain.dbox, self._eng.data_ptr(), st), "tmps_fused_settle")
+        if self.mixed:
+            _lib.check(L.tmps_mixed_unpack(atoms, sim.domain.dbox, st), "tmps_mixed_unpack")
+        sim.domain.mark_device_authoritative()
+        e = self._engine_state()
+        sim.timestep = int(e.step)
+        sim.neighbor.current_step = int(e.step)
+        sim.neighbor.last_build_step = int(e.last_build_step)
+        for fx in sim.fixes:
+            fx.timestep = sim.timestep
+        if self.deform is not None:
+            sv = _device.pull_struct(self.deform._dservo, _lib.Servo)
+            self.deform.nsteps, self.deform.step_count = int(sv.nsteps), int(sv.step_count)
+        if sim.integrator is not None:
+            sim.integrator.timestep = sim.timestep
+        self._check_status()

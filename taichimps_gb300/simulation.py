@@ -35,8 +35,14 @@ class Simulation:
     def __init__(self, domain, atom: AtomSystem | None = None, neighbor: NeighborList | None = None,
                  history: ContactHistory | None = None, pair: GranularPair | None = None,
                  max_atoms: int = 100000, max_neighbors_per_atom: int = 64, skin: float = 0.001,
-                 dt: float = 1e-4, thermo_freq: int = 100, float_type: Any = None) -> None:
+                 dt: float = 1e-4, thermo_freq: int = 100, float_type: Any = None,
+                 precision: str = "fp64", fused: bool = True) -> None:
         self.domain = domain
+        # run() executes supported configurations through the fused step
+        # (engine.py); `precision` picks its arithmetic ("fp64" or "mixed").
+        self.precision = precision
+        self.fused = fused
+        self.last_engine = None
         self.dt = dt
         self.float_type = float_type
         self.timestep = 0
@@ -150,11 +156,25 @@ class Simulation:
         self._sub_step_inner()
 
     def run(self, steps: int) -> None:
+        from .engine import FusedEngine, fusable
+
         self.setup_run(steps)
         if self.run_pre or not self.setup_done:
             self.init_simulation()
-        for _ in range(steps):
-            self._sub_step_inner()
+        if self.precision == "mixed" and not (self.fused and fusable(self)):
+            raise NotImplementedError("the mixed form runs through the fused step: fix nve/sphere with "
+                                      "optional damping/cundall and deform/pressure")
+        if self.fused and steps > 0 and fusable(self) and self.atom.nlocal > 0:
+            eng = FusedEngine(self, self.precision)
+            self.last_engine = eng
+            eng.begin()
+            try:
+                eng.run(steps)
+            finally:
+                eng.finish()
+        else:
+            for _ in range(steps):
+                self._sub_step_inner()
         self.check_device_status()
         self.domain.pull()
 

@@ -1,0 +1,113 @@
+"""
+The fused step (engine.py): FP64 form against the per-hook path and the oracle,
+and the mixed form against the oracle with its error stated as a tolerance.
+
+Mixed-form tolerances: the contact arithmetic is FP32, so the overlap
+delta = radsum - r carries an absolute error of ~1e-7 (one FP32 ulp of r ~ 1);
+at the overlaps used here (~0.02-0.1) forces are good to ~1e-5 relative.
+"""
+
+import numpy as np
+import pytest
+
+from _twin import dense_packing, gpu_state, make_twin, oracle_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+MIXED_F = 5e-4     # forces / torques, max-abs normalised
+MIXED_V = 5e-4     # velocities after the run
+MIXED_X = 1e-9     # positions (relative to the box)
+MIXED_P = 1e-5     # pressure tensor driving the servo
+
+
+def _servo_twin(oracle, precision, n=512, box=8.2, steps=60, seed=21, fused=True, remap="x"):
+    rng = np.random.default_rng(seed)
+    x, r = dense_packing(rng, n, box, 0.48, 0.56)
+    deform = dict(axes={d: {"style": "pressure", "ptarget": 1.0, "pgain": 1e-3} for d in "xyz"}, couple="xyz",
+                  max_rate=1e-1, remap=remap)
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [box] * 3, pair="hertz/history", dt=5e-5,
+                          cundall=(0.7, 0.7), deform=deform)
+    sim.precision = precision
+    sim.fused = fused
+    sim.run(steps)
+    osim.run(steps)
+    return sim, osim
+
+
+def test_fused_fp64_matches_per_hook_and_oracle(gpu, oracle):
+    sim_f, osim = _servo_twin(oracle, "fp64", fused=True)
+    sim_h, _ = _servo_twin(oracle, "fp64", fused=False)
+    assert sim_f.last_engine is not None and sim_h.last_engine is None
+    gf, gh, o = gpu_state(sim_f), gpu_state(sim_h), oracle_state(osim)
+    for k in ("x", "v", "omega", "f", "torque"):
+        assert rel_err(gf[k], o[k]) < 1e-10, (k, rel_err(gf[k], o[k]))
+        assert rel_err(gf[k], gh[k]) < 1e-10, (k, rel_err(gf[k], gh[k]))
+    np.testing.assert_allclose(sim_f.domain.prd, osim.domain.prd, rtol=1e-13)
+    assert rel_err(sim_f.fixes[-1].last_pressure(), osim.last_pressure) < 1e-10
+    assert sim_f.timestep == osim.timestep == 60
+
+
+def test_mixed_matches_oracle_within_stated_error(gpu, oracle):
+    sim, osim = _servo_twin(oracle, "mixed")
+    assert sim.last_engine.mixed
+    g, o = gpu_state(sim), oracle_state(osim)
+    assert np.abs(o["f"]).max() > 0
+    L = osim.domain.prd.max()
+    assert np.abs(g["x"] - o["x"]).max() / L < MIXED_X, np.abs(g["x"] - o["x"]).max() / L
+    assert rel_err(g["v"], o["v"]) < MIXED_V, rel_err(g["v"], o["v"])
+    assert rel_err(g["f"], o["f"]) < MIXED_F, rel_err(g["f"], o["f"])
+    assert rel_err(g["torque"], o["torque"]) < MIXED_F, rel_err(g["torque"], o["torque"])
+    assert rel_err(sim.fixes[-1].last_pressure(), osim.last_pressure) < MIXED_P
+    np.testing.assert_allclose(sim.domain.prd, osim.domain.prd, rtol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_rebuild_every_step(gpu, oracle, precision):
+    """check no: every step aborts the queued launches and rebuilds on the host."""
+    rng = np.random.default_rng(11)
+    x, r = dense_packing(rng, 343, 7.0, 0.5, 0.56)
+    v = rng.normal(scale=0.05, size=x.shape)
+    w = rng.normal(scale=0.5, size=x.shape)
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [7.0] * 3, v=v, w=w, pair="granular/mindlin", dt=5e-5)
+    sim.precision = precision
+    sim.neighbor.check = False
+    osim.neighbor.check = False
+    sim.run(12)
+    osim.run(12)
+    assert sim.neighbor.build_count == osim.neighbor.build_count == 13
+    g, o = gpu_state(sim), oracle_state(osim)
+    tol = 1e-10 if precision == "fp64" else MIXED_V
+    assert rel_err(g["v"], o["v"]) < tol, rel_err(g["v"], o["v"])
+    assert rel_err(g["f"], o["f"]) < (1e-9 if precision == "fp64" else MIXED_F)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_skin_triggered_rebuilds(gpu, oracle, precision):
+    """Fast particles: the skin check fires every few steps inside queued chunks."""
+    rng = np.random.default_rng(5)
+    x, r = dense_packing(rng, 216, 7.5, 0.45, 0.5)
+    v = rng.normal(scale=20.0, size=x.shape)
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [7.5] * 3, v=v, pair="hooke/history", dt=2e-4,
+                          skin=0.1)
+    sim.precision = precision
+    sim.run(80)
+    osim.run(80)
+    assert osim.neighbor.build_count > 5
+    assert sim.neighbor.build_count == osim.neighbor.build_count
+    g, o = gpu_state(sim), oracle_state(osim)
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    assert rel_err(g["x"], o["x"]) < tol, rel_err(g["x"], o["x"])
+
+
+def test_fused_second_run_continues(gpu, oracle):
+    """Two run() calls: the setup evaluation between them (shearupdate off) as in the reference."""
+    rng = np.random.default_rng(8)
+    x, r = dense_packing(rng, 216, 6.2, 0.5, 0.56)
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [6.2] * 3, pair="hertz/history", dt=5e-5,
+                          cundall=(0.7, 0.7))
+    for _ in range(2):
+        sim.run(15)
+        osim.run(15)
+    g, o = gpu_state(sim), oracle_state(osim)
+    assert sim.timestep == 30
+    assert rel_err(g["v"], o["v"]) < 1e-10 and rel_err(g["f"], o["f"]) < 1e-9
