@@ -168,22 +168,29 @@ def run_gpu_arm(args, p, precision, rank, world):
         torch.distributed.barrier()
     names = ["fused_a", "fused_c", "fused_s"]
     clocks = ClockSampler(torch.cuda.current_device())
-    # the timed run continues the warm-up run: the engine is re-entered without a second setup
+    # the timed run continues the warm-up run: the engine is re-entered without a second setup;
+    # steps run as replays of a captured CUDA graph (chunks of eng.chunk steps)
     eng = sim.last_engine
     eng.begin()
-    _device.TIMED = {k: [] for k in names}
-    l0 = L.tmps_launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    eng.run(eng.chunk)                       # captures the graph (untimed, counts as warm-up)
     torch.cuda.synchronize()
+    l0 = L.tmps_launch_count()
+    g0 = eng.graph_kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     eng.run(K)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    launches = L.tmps_launch_count() - l0
+    clk = clocks.stop()
+    # graph replays do not pass through the host entry points, so count the launches the graph holds
+    launches = (L.tmps_launch_count() - l0) + (eng.graph_kernel_launches - g0)
+    # per-kernel CUDA-event timings: the next K steps launched one by one (same run, same state)
+    _device.TIMED = {k: [] for k in names}
+    eng.run(K)
+    torch.cuda.synchronize()
     timed = {k: [a.elapsed_time(b) for a, b in v] for k, v in _device.TIMED.items()}
     _device.TIMED = None
-    clk = clocks.stop()
     eng.finish()
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -196,7 +203,8 @@ def run_gpu_arm(args, p, precision, rank, world):
     pressure = sim.fixes[-1].last_pressure()
     kern = {k: (sum(v) / len(v) if v else None) for k, v in timed.items()}
     return dict(sim=sim, n=n, ms=ms, launches=launches, clocks=clk, kern_ms=kern, n_nb=n_nb, n_c=n_c,
-                pressure=pressure, builds=sim.neighbor.build_count, rebuilds_timed=eng.rebuilds)
+                pressure=pressure, builds=sim.neighbor.build_count, rebuilds_timed=eng.rebuilds,
+                steps_run=sim.timestep)
 
 
 def run_e2e(args, p, precision):
@@ -358,7 +366,11 @@ def main():
     p_oracle = None
     if not args.no_cpu:
         cpu, _ = cpu_baseline(p, args.cpu_budget, K)
-        p_oracle = oracle_pressure(p, W + K)
+        # the oracle runs as many steps as each GPU form ran in all (warm-up, graph capture, timed
+        # replays and the per-kernel timing pass); every form runs the same count
+        steps_run = {v["steps_run"] for v in runs.values()}
+        assert len(steps_run) == 1, steps_run
+        p_oracle = oracle_pressure(p, steps_run.pop())
     scal = lambda t: (t[0] + t[1] + t[2]) / 3.0
     forms_out = {}
     for k, v in runs.items():
@@ -384,6 +396,7 @@ def main():
                      "bytes_per_atom": bytes_atom, "kernel_ms": kern[dom_name], "peak_source": "measured"},
         "speedup_mixed_vs_fp64": (values["mixed"] / values["fp64"]) if len(values) == 2 else None,
         "oracle_mean_pressure": None if p_oracle is None else scal(p_oracle),
+        "pressure_compared_after_steps": r["steps_run"],
         "forms": forms_out,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r["launches"], "clocks": r["clocks"],
     }

@@ -317,16 +317,24 @@ int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream);
 /* Launch A (see tmps_engine). */
 int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* stream);
 
-/* Launch C: `vir_part` receives d_eng->nblocks x 6 partial sums (caller memory). */
+/* Launch C, two kernels: a screen over all atoms (finishes contact-free ones,
+ * flags the rest) and the contact law over the flagged ones.  `scratch`
+ * (tmps_fused_scratch_bytes(n), caller memory) receives the virial partial
+ * sums (d_eng->nblocks = tmps_fused_blocks(n) of them) and the flags. */
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
-                 const tmps_pair_params* p, double* vir_part, void* stream);
+                 const tmps_pair_params* p, void* scratch, void* stream);
 
-/* Launch S: pressure servo from the partial sums of C. */
-int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const double* vir_part,
+/* Launch S: rebuild decision, virial total (from C's scratch), servo. */
+int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const void* scratch,
                      int32_t* d_status, void* stream);
 
-/* Grid size of launch C for n atoms (the number of virial partials). */
-int32_t tmps_fused_blocks(int32_t n);
+/* Number of virial partial sums C writes for n atoms with this pair style
+ * (tmps_pair_params.style) in this form (mixed 0/1): one per block of
+ * one resident wave of each of its two kernels. */
+int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed);
+
+/* Scratch bytes tmps_fused_c / tmps_fused_servo need (same arguments). */
+int64_t tmps_fused_scratch_bytes(int32_t n, int32_t style, int32_t mixed);
 
 /* Applies what the fused step leaves pending -- the second half-kick of the
  * last step and a remap x the servo asked for -- so the state is that of the

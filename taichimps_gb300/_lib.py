@@ -132,7 +132,8 @@ _SIGS = {
     "tmps_fused_c": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
                              ctypes.POINTER(PairParams), c_vp, c_vp]),
     "tmps_fused_servo": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
-    "tmps_fused_blocks": (c_i32, [c_i32]),
+    "tmps_fused_blocks": (c_i32, [c_i32, c_i32, c_i32]),
+    "tmps_fused_scratch_bytes": (ctypes.c_int64, [c_i32, c_i32, c_i32]),
     "tmps_fused_settle": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp]),
 }
 

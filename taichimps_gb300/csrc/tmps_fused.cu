@@ -28,6 +28,7 @@ namespace {
 
 constexpr int kBlockA = 256;
 constexpr int kBlockC = 128;
+constexpr int kBlockScreen = 256;
 
 // Error-free transformations in FP32 (Knuth's two-sum; FMA for products):
 // s + e == a + b exactly.  Used to form the separation and the overlap of a
@@ -70,6 +71,38 @@ __device__ __forceinline__ void dw_add_prod(float& hi, float& lo, float ah, floa
     const float pe = __fmaf_rn(ah, bh, -p);  // exact error of the product
     const float t = __fadd_rn(pe, __fadd_rn(__fmul_rn(ah, bl), __fmul_rn(al, bh)));
     dw_add2(hi, lo, p, t);
+}
+
+// Block-wide double-word sum of NV values per thread, fixed tree order; the
+// result lands in (h, l) of thread 0.  The mixed form reduces its virial
+// partials this way: an FP64 warp shuffle tree costs more issue slots on this
+// part's narrow FP64 pipe than the rest of the pass.
+template <int NV, int BLOCK>
+__device__ __forceinline__ void block_sum_dw(float (&h)[NV], float (&l)[NV], float2* smem /* [NV][BLOCK/32] */) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float bh = __shfl_down_sync(0xffffffffu, h[c], o), bl = __shfl_down_sync(0xffffffffu, l[c], o);
+            dw_add2(h[c], l[c], bh, bl);
+        }
+        if (lane == 0) smem[c * (BLOCK / 32) + warp] = make_float2(h[c], l[c]);
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            const float2 q = lane < BLOCK / 32 ? smem[c * (BLOCK / 32) + lane] : make_float2(0.0f, 0.0f);
+            h[c] = q.x;
+            l[c] = q.y;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float bh = __shfl_down_sync(0xffffffffu, h[c], o), bl = __shfl_down_sync(0xffffffffu, l[c], o);
+                dw_add2(h[c], l[c], bh, bl);
+            }
+        }
+    }
 }
 
 __device__ __forceinline__ bool rebuild_due(const tmps_engine* __restrict__ e, int64_t s) {
@@ -124,7 +157,7 @@ __device__ __forceinline__ int cell_x(int32_t c) { return c & 1023; }
 __device__ __forceinline__ int cell_y(int32_t c) { return (c >> 10) & 1023; }
 __device__ __forceinline__ int cell_z(int32_t c) { return (c >> 20) & 1023; }
 
-__global__ void __launch_bounds__(kBlockA) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
+__global__ void __launch_bounds__(kBlockA, 5) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
                                                   tmps_engine* __restrict__ e) {
     // Double-word state (hi + lo, both FP32) updated with error-free FP32
     // transforms: the FP64 pipe of this part is ~70x narrower than FP32, and
@@ -177,10 +210,148 @@ __global__ void __launch_bounds__(kBlockA) k_a32(tmps_atoms a, const tmps_box* _
 
 // ---------------------------------------------------------------------- C
 
+// C, first pass (all atoms): is any neighbor within reach of contact?  The
+// test is the contact test itself in the FP64 form and a conservative FP32
+// version of it in the mixed form (the second pass decides exactly).  Atoms
+// with no such neighbor are finished here -- zero force and torque, their
+// contact history cleared, the kinetic virial term -- and the rest are
+// flagged, one ballot word per 32-atom group, for the second pass.  This
+// pass holds few registers, so it runs at high occupancy over the many
+// contact-free atoms of a loose packing.
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlockScreen)
+    k_screen(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B, tmps_engine* __restrict__ E, int hist,
+             uint32_t* __restrict__ flags, double* __restrict__ part) {
+    __shared__ double smem[6 * (kBlockScreen / 32)];
+    if (E->aborted) return;
+    const int64_t s = E->step + 1;
+    if (rebuild_due(E, s)) return;
+    const int n = A.n;
+    const int lane = threadIdx.x & 31;
+    const int ngroups = (n + 31) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    float hh[3], prd32[3], iprd32[3];
+    double prd64[3], iprd64[3];
+    int per[3], single[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        per[c] = B->per[c];
+        if constexpr (MIXED) {
+            hh[c] = E->h32[c];
+            prd32[c] = E->prd32[c];
+            iprd32[c] = E->iprd32[c];
+            single[c] = E->single_bin[c];
+        } else {
+            prd64[c] = B->prd[c];
+            iprd64[c] = B->inv_prd[c];
+        }
+    }
+    float Kh[6] = {0, 0, 0, 0, 0, 0}, Kl[6] = {0, 0, 0, 0, 0, 0};
+    double Kd[6] = {0, 0, 0, 0, 0, 0};
+    const bool two = L.slots > 1;
+    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += nwarps) {
+        const int i = (g << 5) + lane;
+        const bool valid = i < n;
+        bool cand = false;
+        if (valid) {
+            // every load that does not depend on another is issued at once:
+            // row length, own position, the first two neighbor entries (read
+            // whatever the row length; used only below it)
+            const int nn = L.nnb[i];
+            const int e0 = L.nbr[i];
+            const int e1 = two ? L.nbr[(size_t)n + i] : 0;
+            if constexpr (MIXED) {
+                const float4 pi = ld4f(A.pos32, i);
+                auto reach = [&](int e) {
+                    const float4 pj = ld4f(A.pos32, e & kNbrIndexMask);
+                    const int code = (unsigned)e >> kNbrIndexBits;
+                    const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1), (float)(code / 9 - 1)};
+                    const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj.x, pj.y, pj.z};
+                    float d[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
+                        if (single[c]) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
+                    }
+                    const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                    const float rs = (pi.w + pj.w) * 1.00001f;
+                    return rq < rs * rs;
+                };
+                const bool c0 = nn > 0 && reach(e0);
+                const bool c1 = nn > 1 && reach(e1);
+                cand = c0 || c1;
+                for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
+            } else {
+                const double4 pi = ld4(A.xr, i);
+                auto reach = [&](int e) {
+                    const double4 pj = ld4(A.xr, e & kNbrIndexMask);
+                    double d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        if (per[c] == 1) d[c] -= rint(d[c] * iprd64[c]) * prd64[c];
+                    const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                    const double radsum = pi.w + pj.w;
+                    return rsq < radsum * radsum && rsq > 1e-28;
+                };
+                const bool c0 = nn > 0 && reach(e0);
+                const bool c1 = nn > 1 && reach(e1);
+                cand = c0 || c1;
+                for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
+            }
+        }
+        const uint32_t word = __ballot_sync(0xffffffffu, cand);
+        if (lane == 0) flags[g] = word;
+        if (valid && !cand) {
+            if (hist && L.touch[i] != 0ull) L.touch[i] = 0ull;
+            if constexpr (MIXED) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    A.f32[c * n + i] = 0.0f;
+                    A.torque32[c * n + i] = 0.0f;
+                }
+                const float4 v = ld4f(A.vel32, i);
+                const float kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
+                                      (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
+#pragma unroll
+                for (int c = 0; c < 6; ++c) dw_add(Kh[c], Kl[c], kin[c]);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    A.f[c * n + i] = 0.0;
+                    A.torque[c * n + i] = 0.0;
+                }
+                const double4 v = ld4(A.vm, i);
+                const double kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
+                                       (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
+#pragma unroll
+                for (int c = 0; c < 6; ++c) Kd[c] += kin[c];
+            }
+        }
+    }
+    if constexpr (MIXED) {
+        // partials as double words (hi, lo), summed the same way by S
+        block_sum_dw<6, kBlockScreen>(Kh, Kl, reinterpret_cast<float2*>(smem));
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) reinterpret_cast<float2*>(part)[(size_t)blockIdx.x * 6 + c] = make_float2(Kh[c], Kl[c]);
+        }
+    } else {
+        block_sum<6, kBlockScreen>(Kd, smem);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = Kd[c];
+        }
+    }
+}
+
+// C, second pass: the atoms the screen flagged (some neighbor within reach
+// of contact), with the full contact law.  Warps walk 32-atom groups in a
+// fixed order and skip groups whose flag word is zero, so the per-block
+// virial partials do not depend on scheduling.
 template <int STYLE, bool MIXED>
 __global__ void __launch_bounds__(kBlockC)
     k_c(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
-        tmps_engine* __restrict__ E, double* __restrict__ part) {
+        tmps_engine* __restrict__ E, const uint32_t* __restrict__ flags, double* __restrict__ part) {
     using T = typename std::conditional<MIXED, float, double>::type;
     __shared__ double smem[6 * (kBlockC / 32)];
     if (E->aborted) return;
@@ -194,9 +365,24 @@ __global__ void __launch_bounds__(kBlockC)
     else dt = E->dt;
     double Vd[6] = {0, 0, 0, 0, 0, 0};
     float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};  // mixed: per-thread double words
-    // grid-stride: the grid is sized to the GPU (tmps_fused_blocks), so the
-    // servo sums one virial partial per resident block, not per 128 atoms
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int ngroups = (n + 31) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    // groups are dealt to warps round-robin (warp w owns w, w + nwarps, ...),
+    // so a run of flagged neighbouring groups -- contacts cluster in space,
+    // and atoms are in Morton order -- spreads over many warps and SMs; a
+    // lane reads one flag word, the warp visits only the nonzero ones
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int base = gw; base < ngroups; base += 32 * nwarps) {
+    const int mine = base + lane * nwarps;
+    const uint32_t myword = mine < ngroups ? flags[mine] : 0u;
+    uint32_t pending = __ballot_sync(0xffffffffu, myword != 0u);
+    while (pending) {
+        const int src = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t word = __shfl_sync(0xffffffffu, myword, src);
+        if (!((word >> lane) & 1u)) continue;
+        const int i = ((base + src * nwarps) << 5) + lane;
         T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
         T xi[3], ri, mi, vi[3], wi[3];
         T hh[3] = {0, 0, 0}, prd[3], iprd[3];
@@ -465,16 +651,21 @@ __global__ void __launch_bounds__(kBlockC)
             for (int c = 0; c < 6; ++c) Vd[c] += V[c] + kin[c];
         }
     }
+    }
     if constexpr (MIXED) {
+        block_sum_dw<6, kBlockC>(Vh, Vl, reinterpret_cast<float2*>(smem));
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) Vd[c] = (double)Vh[c] + (double)Vl[c];
-    }
-    block_sum<6, kBlockC>(Vd, smem);
-    if (threadIdx.x == 0) {
+            for (int c = 0; c < 6; ++c) reinterpret_cast<float2*>(part)[(size_t)blockIdx.x * 6 + c] = make_float2(Vh[c], Vl[c]);
+        }
+    } else {
+        block_sum<6, kBlockC>(Vd, smem);
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = Vd[c];
-        if (blockIdx.x == 0) E->final_pending = 1;
+            for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = Vd[c];
+        }
     }
+    if (threadIdx.x == 0 && blockIdx.x == 0) E->final_pending = 1;
 }
 
 // ---------------------------------------------------------------------- S
@@ -492,127 +683,206 @@ __device__ double limit_rate_f(double rate, double ptarget, int normalize, doubl
     return out;
 }
 
-constexpr int kBlockS = 256;
+constexpr int kBlockS = 192;  // a multiple of 6 and of 32
 
+// The servo's arithmetic on staged copies of the three structs, run by one
+// warp: lane k < 6 forms pressure component k, lane d < 3 updates dimension
+// d.  Each value is the same FP64 expression as in the one-thread form; the
+// lanes only put the independent divisions into one warp instruction each.
+__device__ void servo_update_warp(tmps_box& b, tmps_servo& sv, tmps_engine& e, const double* acc, int32_t* status) {
+    const int lane = threadIdx.x & 31;
+    const double dt = e.dt;
+    const double vol = b.prd[0] * b.prd[1] * b.prd[2];
+    double t = 0.0;
+    if (lane < 6) {
+        t = vol > 0.0 ? acc[lane] / vol : 0.0;
+        sv.pressure[lane] = t;
+    }
+    const double t0 = __shfl_sync(0xffffffffu, t, 0), t1 = __shfl_sync(0xffffffffu, t, 1),
+                 t2 = __shfl_sync(0xffffffffu, t, 2);
+    const int d = lane;
+    double lo = 0.0, prd = 0.0, nlo = 0.0, nhi = 0.0, nprd = 1.0;
+    if (lane < 3) {
+        lo = b.lo[d];
+        prd = b.prd[d];
+        nlo = lo;
+        nhi = b.hi[d];
+        const int st = sv.style[d];
+        const double ls = sv.lo_start[d], hs = sv.hi_start[d];
+        if (st >= 1 && st <= 4) {
+            const double elapsed = (double)sv.nsteps * dt;
+            if (st == 1) {
+                const double shift = ((0.5 * elapsed) * sv.rate[d]) * (hs - ls);
+                nlo = ls - shift; nhi = hs + shift;
+            } else if (st == 2) {
+                const double mid = 0.5 * (ls + hs);
+                const double half = (0.5 * (hs - ls)) * exp(sv.rate[d] * elapsed);
+                nlo = mid - half; nhi = mid + half;
+            } else if (st == 3) {
+                const double shift = (0.5 * elapsed) * sv.vel[d];
+                nlo = ls - shift; nhi = hs + shift;
+            } else {
+                const double shift = (0.5 * sv.amp[d]) * sin(((2.0 * 3.14159265358979323846) * elapsed) / sv.tper[d]);
+                nlo = ls - shift; nhi = hs + shift;
+            }
+        } else if (st >= 5 && st <= 7) {
+            const double frac = sv.nsteps_total > 0 ? (double)sv.nsteps / (double)sv.nsteps_total : 0.0;
+            if (st == 5) {
+                nlo = ls + frac * (sv.flo[d] - ls);
+                nhi = hs + frac * (sv.fhi[d] - hs);
+            } else if (st == 6) {
+                const double lo_stop = ls + sv.dlo[d], hi_stop = hs + sv.dhi[d];
+                nlo = ls + frac * (lo_stop - ls);
+                nhi = hs + frac * (hi_stop - hs);
+            } else {
+                const double mid = 0.5 * (ls + hs);
+                const double half = (0.5 * sv.scale[d]) * (hs - ls);
+                nlo = ls + frac * ((mid - half) - ls);
+                nhi = hs + frac * ((mid + half) - hs);
+            }
+        } else if (st == 8 || st == 9) {
+            // coupled axes share their mean pressure; style 9 (pressure/scalar)
+            // with no coupling uses the scalar pressure
+            const double scalar = ((t0 + t1) + t2) / 3.0;
+            double pd = d == 0 ? t0 : (d == 1 ? t1 : t2);
+            if (sv.couple == 1) pd = scalar;
+            else if (sv.couple == 2 && d < 2) pd = (t0 + t1) / 2.0;
+            else if (sv.couple == 3 && d > 0) pd = (t1 + t2) / 2.0;
+            else if (sv.couple == 4 && d != 1) pd = (t0 + t2) / 2.0;
+            if (sv.couple == 0 && st == 9) pd = scalar;
+            const double tgt = sv.ptarget[d];
+            const double rate = limit_rate_f(sv.pgain[d] * (pd - tgt), tgt, sv.normalize, sv.max_rate);
+            sv.cum[d] += (dt * rate) * prd;
+            nlo = ls - 0.5 * sv.cum[d];
+            nhi = hs + 0.5 * sv.cum[d];
+        }
+        nprd = nhi - nlo;
+    }
+    if (__any_sync(0xffffffffu, !(nprd > 0.0))) {
+        if (lane == 0) atomicOr(status, TMPS_STATUS_BOX_NONPOSITIVE);
+        return;
+    }
+    if (lane < 3) {
+        b.old_lo[d] = lo;
+        b.old_prd[d] = prd;
+        b.lo[d] = nlo;
+        b.hi[d] = nhi;
+        b.prd[d] = nprd;
+        b.inv_prd[d] = 1.0 / nprd;
+        const double hc = nprd / (double)b.g[d];
+        b.hcell[d] = hc;
+        b.h_rate[d] = (nprd - prd) / dt;
+        b.h_rate[3 + d] = 0.0;
+        if (e.mixed) {
+            split((nprd - prd) / prd, e.eps_hi[d], e.eps_lo[d]);
+            split(hc, e.h32[d], e.hlo32[d]);
+            split(nprd, e.prd32[d], e.prdlo32[d]);
+            e.iprd32[d] = (float)b.inv_prd[d];
+            e.dlo32[d] = (float)(nlo - e.lo0[d]);
+            e.dh32[d] = (float)(hc - e.h0[d]);
+        } else {
+            e.remap_scale[d] = nprd / prd;
+        }
+    }
+    if (lane == 0) {
+        b.vremap = sv.remap == 2 ? 1 : 0;
+        b.remap_pending = sv.remap == 1 ? 1 : 0;
+    }
+}
+
+template <typename S>
+__device__ __forceinline__ void copy_words(S* dst, const S* src) {
+    static_assert(sizeof(S) % 4 == 0, "struct size");
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* o = reinterpret_cast<uint32_t*>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(S) / 4); k += blockDim.x) o[k] = a[k];
+}
+
+// S: finish the step.  Decide the rebuild, sum the virial partials of C in a
+// fixed order, run the servo.  The three structs are staged through shared
+// memory; the partial sums are read component-major by 192 threads (thread t
+// always adds component t % 6), so every load is coalesced and independent.
+// The mixed form's partials are double words and are summed as such; only
+// the six totals become FP64.
 __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps_engine* e, const double* part,
                                                int32_t* status) {
-    __shared__ double smem[6 * (kBlockS / 32)];
-    if (e->aborted) return;
-    const int64_t s = e->step + 1;
-    if (rebuild_due(e, s)) {
+    __shared__ double red[kBlockS];
+    __shared__ float2 redf[kBlockS];
+    __shared__ double tot[6];
+    __shared__ tmps_box sb;
+    __shared__ tmps_servo ssv;
+    __shared__ tmps_engine se;
+    copy_words(&se, e);
+    __syncthreads();
+    if (se.aborted) return;
+    const int64_t s = se.step + 1;
+    if (rebuild_due(&se, s)) {
         if (threadIdx.x == 0) e->aborted = 1;
         return;
     }
-    const bool servo_now = e->servo && ((sv->step_count + 1) % sv->nevery == 0);
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    copy_words(&sb, b);
+    copy_words(&ssv, sv);
+    __syncthreads();
+    const bool servo_now = se.servo && ((ssv.step_count + 1) % ssv.nevery == 0);
     if (servo_now) {
-        const int np = e->nblocks;
-        for (int p = threadIdx.x; p < np; p += blockDim.x)
-#pragma unroll
-            for (int c = 0; c < 6; ++c) acc[c] += part[(size_t)p * 6 + c];
-        block_sum<6, kBlockS>(acc, smem);
-    }
-    if (threadIdx.x != 0) return;
-    e->step = s;
-    b->remap_pending = 0;
-    if (!e->servo) return;
-    sv->step_count += 1;
-    sv->nsteps += 1;
-    if (!servo_now) return;
-    const double dt = e->dt;
-    const double elapsed = (double)sv->nsteps * dt;
-    const double frac = sv->nsteps_total > 0 ? (double)sv->nsteps / (double)sv->nsteps_total : 0.0;
-    double lo[3], hi[3], prd[3];
-    for (int d = 0; d < 3; ++d) {
-        lo[d] = b->lo[d];
-        hi[d] = b->hi[d];
-        prd[d] = b->prd[d];
-    }
-    const double vol = prd[0] * prd[1] * prd[2];
-    double t[6];
-    for (int k = 0; k < 6; ++k) t[k] = vol > 0.0 ? acc[k] / vol : 0.0;
-    for (int k = 0; k < 6; ++k) sv->pressure[k] = t[k];
-    const double scalar = ((t[0] + t[1]) + t[2]) / 3.0;
-    double p[3] = {t[0], t[1], t[2]};
-    if (sv->couple == 1) {
-        p[0] = p[1] = p[2] = scalar;
-    } else if (sv->couple == 2) {
-        const double m = (t[0] + t[1]) / 2.0; p[0] = m; p[1] = m;
-    } else if (sv->couple == 3) {
-        const double m = (t[1] + t[2]) / 2.0; p[1] = m; p[2] = m;
-    } else if (sv->couple == 4) {
-        const double m = (t[0] + t[2]) / 2.0; p[0] = m; p[2] = m;
-    }
-    double nlo[3], nhi[3];
-    for (int d = 0; d < 3; ++d) {
-        const int st = sv->style[d];
-        const double ls = sv->lo_start[d], hs = sv->hi_start[d];
-        nlo[d] = lo[d];
-        nhi[d] = hi[d];
-        if (st == 1) {
-            const double shift = ((0.5 * elapsed) * sv->rate[d]) * (hs - ls);
-            nlo[d] = ls - shift; nhi[d] = hs + shift;
-        } else if (st == 2) {
-            const double mid = 0.5 * (ls + hs);
-            const double half = (0.5 * (hs - ls)) * exp(sv->rate[d] * elapsed);
-            nlo[d] = mid - half; nhi[d] = mid + half;
-        } else if (st == 3) {
-            const double shift = (0.5 * elapsed) * sv->vel[d];
-            nlo[d] = ls - shift; nhi[d] = hs + shift;
-        } else if (st == 4) {
-            const double shift = (0.5 * sv->amp[d]) * sin(((2.0 * 3.14159265358979323846) * elapsed) / sv->tper[d]);
-            nlo[d] = ls - shift; nhi[d] = hs + shift;
-        } else if (st == 5) {
-            nlo[d] = ls + frac * (sv->flo[d] - ls);
-            nhi[d] = hs + frac * (sv->fhi[d] - hs);
-        } else if (st == 6) {
-            const double lo_stop = ls + sv->dlo[d], hi_stop = hs + sv->dhi[d];
-            nlo[d] = ls + frac * (lo_stop - ls);
-            nhi[d] = hs + frac * (hi_stop - hs);
-        } else if (st == 7) {
-            const double mid = 0.5 * (ls + hs);
-            const double half = (0.5 * sv->scale[d]) * (hs - ls);
-            nlo[d] = ls + frac * ((mid - half) - ls);
-            nhi[d] = hs + frac * ((mid + half) - hs);
-        } else if (st == 8 || st == 9) {
-            const double pd = (sv->couple == 0 && st == 9) ? scalar : p[d];
-            const double tgt = sv->ptarget[d];
-            const double rate = limit_rate_f(sv->pgain[d] * (pd - tgt), tgt, sv->normalize, sv->max_rate);
-            sv->cum[d] += (dt * rate) * prd[d];
-            nlo[d] = ls - 0.5 * sv->cum[d];
-            nhi[d] = hs + 0.5 * sv->cum[d];
+        const int total = se.nblocks * 6;
+        int k = threadIdx.x;
+        if (se.mixed) {
+            // double-word partials, summed in double words (two chains per thread)
+            const float2* pf = reinterpret_cast<const float2*>(part);
+            float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+            for (; k + kBlockS < total; k += 2 * kBlockS) {
+                const float2 q0 = pf[k], q1 = pf[k + kBlockS];
+                dw_add2(h0, l0, q0.x, q0.y);
+                dw_add2(h1, l1, q1.x, q1.y);
+            }
+            if (k < total) {
+                const float2 q0 = pf[k];
+                dw_add2(h0, l0, q0.x, q0.y);
+            }
+            dw_add2(h0, l0, h1, l1);
+            redf[threadIdx.x] = make_float2(h0, l0);
+            __syncthreads();
+            if (threadIdx.x < 6) {
+                float h = 0.0f, l = 0.0f;
+                for (int q = threadIdx.x; q < kBlockS; q += 6) dw_add2(h, l, redf[q].x, redf[q].y);
+                tot[threadIdx.x] = (double)h + (double)l;
+            }
+        } else {
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            for (; k + 3 * kBlockS < total; k += 4 * kBlockS) {
+                a0 += part[k];
+                a1 += part[k + kBlockS];
+                a2 += part[k + 2 * kBlockS];
+                a3 += part[k + 3 * kBlockS];
+            }
+            for (; k < total; k += kBlockS) a0 += part[k];
+            red[threadIdx.x] = (a0 + a1) + (a2 + a3);
+            __syncthreads();
+            if (threadIdx.x < 6) {
+                double t = 0.0;
+                for (int q = threadIdx.x; q < kBlockS; q += 6) t += red[q];
+                tot[threadIdx.x] = t;
+            }
         }
+        __syncthreads();
     }
-    double nprd[3];
-    bool bad = false;
-    for (int d = 0; d < 3; ++d) {
-        nprd[d] = nhi[d] - nlo[d];
-        bad = bad || !(nprd[d] > 0.0);
+    if (threadIdx.x < 32) {
+        if (threadIdx.x == 0) {
+            se.step = s;
+            sb.remap_pending = 0;
+            if (se.servo) {
+                ssv.step_count += 1;
+                ssv.nsteps += 1;
+            }
+        }
+        __syncwarp();
+        if (servo_now) servo_update_warp(sb, ssv, se, tot, status);
     }
-    if (bad) {
-        *status |= TMPS_STATUS_BOX_NONPOSITIVE;
-        return;
-    }
-    for (int d = 0; d < 3; ++d) {
-        b->old_lo[d] = lo[d];
-        b->old_prd[d] = prd[d];
-        b->lo[d] = nlo[d];
-        b->hi[d] = nhi[d];
-        b->prd[d] = nprd[d];
-        b->inv_prd[d] = 1.0 / nprd[d];
-        b->hcell[d] = nprd[d] / (double)b->g[d];
-        b->h_rate[d] = (nprd[d] - prd[d]) / dt;
-        b->h_rate[3 + d] = 0.0;
-        e->remap_scale[d] = nprd[d] / prd[d];
-        split((nprd[d] - prd[d]) / prd[d], e->eps_hi[d], e->eps_lo[d]);
-        split(b->hcell[d], e->h32[d], e->hlo32[d]);
-        split(nprd[d], e->prd32[d], e->prdlo32[d]);
-        e->iprd32[d] = (float)(1.0 / nprd[d]);
-        e->dlo32[d] = (float)(nlo[d] - e->lo0[d]);
-        e->dh32[d] = (float)(b->hcell[d] - e->h0[d]);
-    }
-    b->vremap = sv->remap == 2 ? 1 : 0;
-    b->remap_pending = sv->remap == 1 ? 1 : 0;
+    __syncthreads();
+    copy_words(e, &se);
+    copy_words(b, &sb);
+    copy_words(sv, &ssv);
 }
 
 // -------------------------------------------------------- prepare / unpack
@@ -766,13 +1036,7 @@ bool mixed_ok(const tmps_atoms* a) {
            a->torque32 && a->o0_32;
 }
 
-}  // namespace
-
-extern "C" {
-
-int32_t tmps_fused_blocks(int32_t n) {
-    // one wave of resident blocks: up to 8 per SM (the contact kernel's
-    // register use allows 4-5), never more blocks than 128-atom groups
+int sm_count() {
     static int sms = 0;
     if (sms == 0) {
         int dev = 0, v = 0;
@@ -782,8 +1046,58 @@ int32_t tmps_fused_blocks(int32_t n) {
         else
             sms = 152;
     }
-    const int by_atoms = n <= 0 ? 1 : grid_for(n, kBlockC);
-    return (int32_t)(by_atoms < 8 * sms ? by_atoms : 8 * sms);
+    return sms;
+}
+// Grids of the two passes of C: exactly one wave of resident blocks each
+// (occupancy of the kernel instance x SMs), so the static grid-stride split
+// leaves no partial second wave.
+template <typename K>
+int wave_blocks(K kernel, int block) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, block, 0) != cudaSuccess || occ < 1) occ = 1;
+    return occ * sm_count();
+}
+int screen_wave(bool mixed) {
+    static int w[2] = {0, 0};
+    int& v = w[mixed ? 1 : 0];
+    if (!v) v = mixed ? wave_blocks(k_screen<true>, kBlockScreen) : wave_blocks(k_screen<false>, kBlockScreen);
+    return v;
+}
+int contact_wave(int style, bool mixed) {
+    static int w[5][2] = {};
+    if (style < 0 || style > 4) style = 4;
+    int& v = w[style][mixed ? 1 : 0];
+    if (!v) {
+        switch (style) {
+            case 0: v = mixed ? wave_blocks(k_c<0, true>, kBlockC) : wave_blocks(k_c<0, false>, kBlockC); break;
+            case 1: v = mixed ? wave_blocks(k_c<1, true>, kBlockC) : wave_blocks(k_c<1, false>, kBlockC); break;
+            case 2: v = mixed ? wave_blocks(k_c<2, true>, kBlockC) : wave_blocks(k_c<2, false>, kBlockC); break;
+            case 3: v = mixed ? wave_blocks(k_c<3, true>, kBlockC) : wave_blocks(k_c<3, false>, kBlockC); break;
+            default: v = mixed ? wave_blocks(k_c<4, true>, kBlockC) : wave_blocks(k_c<4, false>, kBlockC); break;
+        }
+    }
+    return v;
+}
+int screen_blocks(int n, bool mixed) { const int b = grid_for(n, kBlockScreen); return b < screen_wave(mixed) ? b : screen_wave(mixed); }
+int contact_blocks(int n, int style, bool mixed) {
+    const int b = grid_for(n, kBlockC);
+    return b < contact_wave(style, mixed) ? b : contact_wave(style, mixed);
+}
+size_t flags_offset(int n, int style, bool mixed) {
+    return ((size_t)(screen_blocks(n, mixed) + contact_blocks(n, style, mixed)) * 6 * sizeof(double) + 255) &
+           ~size_t(255);
+}
+}  // namespace
+
+extern "C" {
+
+int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed) {
+    return screen_blocks(n, mixed != 0) + contact_blocks(n, style, mixed != 0);
+}
+
+int64_t tmps_fused_scratch_bytes(int32_t n, int32_t style, int32_t mixed) {
+    if (n < 0) return -1;
+    return (int64_t)(flags_offset(n, style, mixed != 0) + (size_t)((n + 31) / 32 + 1) * sizeof(uint32_t));
 }
 
 int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* d_eng, const int32_t* cell_of,
@@ -824,17 +1138,24 @@ int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void*
 }
 
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
-                 const tmps_pair_params* p, double* vir_part, void* stream) {
-    if (!a || !nl || !d_box || !d_eng || !p || !vir_part || a->n < 0 || nl->n != a->n) return TMPS_ERR_BAD_ARG;
+                 const tmps_pair_params* p, void* scratch, void* stream) {
+    if (!a || !nl || !d_box || !d_eng || !p || !scratch || a->n < 0 || nl->n != a->n) return TMPS_ERR_BAD_ARG;
     if (!a->pos32 && !a->rinv) return TMPS_ERR_BAD_ARG;
     if (p->style < 0 || p->style > 4 || nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
-    const int g = tmps_fused_blocks(a->n);
-    cudaStream_t s = (cudaStream_t)stream;
+    const int n = a->n;
     const bool mixed = a->pos32 != nullptr;
+    const int g1 = screen_blocks(n, mixed), g2 = contact_blocks(n, p->style, mixed);
+    double* part1 = (double*)scratch;
+    double* part2 = part1 + (size_t)g1 * 6;
+    uint32_t* flags = (uint32_t*)((char*)scratch + flags_offset(n, p->style, mixed));
+    cudaStream_t s = (cudaStream_t)stream;
     if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-#define TMPS_LAUNCH_C(ST)                                                                    \
-    if (mixed) k_c<ST, true><<<g, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, vir_part);      \
-    else k_c<ST, false><<<g, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, vir_part);
+    const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
+    if (mixed) k_screen<true><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, part1);
+    else k_screen<false><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, part1);
+#define TMPS_LAUNCH_C(ST)                                                                          \
+    if (mixed) k_c<ST, true><<<g2, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, flags, part2);       \
+    else k_c<ST, false><<<g2, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, flags, part2);
     switch (p->style) {
         case 0: TMPS_LAUNCH_C(0) break;
         case 1: TMPS_LAUNCH_C(1) break;
@@ -843,14 +1164,14 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
         default: TMPS_LAUNCH_C(4) break;
     }
 #undef TMPS_LAUNCH_C
-    note_launches(1);
+    note_launches(2);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
-int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const double* vir_part,
+int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const void* scratch,
                      int32_t* d_status, void* stream) {
-    if (!d_box || !d_servo || !d_eng || !vir_part || !d_status) return TMPS_ERR_BAD_ARG;
-    k_s<<<1, kBlockS, 0, (cudaStream_t)stream>>>(d_box, d_servo, d_eng, vir_part, d_status);
+    if (!d_box || !d_servo || !d_eng || !scratch || !d_status) return TMPS_ERR_BAD_ARG;
+    k_s<<<1, kBlockS, 0, (cudaStream_t)stream>>>(d_box, d_servo, d_eng, (const double*)scratch, d_status);
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }

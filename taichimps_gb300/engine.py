@@ -46,7 +46,10 @@ def fusable(sim) -> bool:
 
 
 class FusedEngine:
-    def __init__(self, sim, precision: str = "fp64", chunk: int = 64) -> None:
+    # kernels per step: A, the two passes of C, S
+    LAUNCHES_PER_STEP = 4
+
+    def __init__(self, sim, precision: str = "fp64", chunk: int = 64, graphs: bool = True) -> None:
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.sim = sim
@@ -61,6 +64,13 @@ class FusedEngine:
         self._dummy_servo = _device.struct_buffer(_lib.Servo())
         self._n = -1
         self.rebuilds = 0
+        # A chunk of `chunk` steps is captured once as a CUDA graph and replayed;
+        # a rebuild swaps buffers, so the graph is captured again after one.
+        self.graphs = bool(graphs)
+        self._graph = None
+        self._graph_key = None
+        self.graph_replays = 0
+        self.graph_kernel_launches = 0
 
     # ------------------------------------------------------------ storage
 
@@ -70,7 +80,10 @@ class FusedEngine:
         f64 = dict(dtype=torch.float64, device=self.dev)
         f32 = dict(dtype=torch.float32, device=self.dev)
         self.rinv = None if self.mixed else torch.zeros((2, n), **f64)
-        self.part = torch.zeros(int(_device.lib().tmps_fused_blocks(n)) * 6, **f64)
+        style, mixed = int(self.sim.pair_style.params.style), 1 if self.mixed else 0
+        self.nblocks = int(_device.lib().tmps_fused_blocks(n, style, mixed))
+        self.part = torch.zeros(int(_device.lib().tmps_fused_scratch_bytes(n, style, mixed)), dtype=torch.uint8,
+                                device=self.dev)
         if self.mixed:
             self.pos32 = torch.zeros((n, 4), **f32)
             self.pos32lo = torch.zeros((n, 4), **f32)
@@ -117,7 +130,7 @@ class FusedEngine:
         e.cundall = 1 if self.cundall is not None else 0
         e.servo = 1 if self.deform is not None else 0
         e.mixed = 1 if self.mixed else 0
-        e.nblocks = int(_device.lib().tmps_fused_blocks(n))
+        e.nblocks = self.nblocks
         e.dt = float(sim.dt)
         if self.cundall is not None:
             e.gamma_lin, e.gamma_ang = self.cundall.gamma_lin, self.cundall.gamma_ang
@@ -176,10 +189,35 @@ class FusedEngine:
             atoms = self.atoms()
             nl_struct = sim.history.cstruct(sim.neighbor)
             params = sim.pair_style.params
-            for _ in range(min(self.chunk, target - done)):
-                self._launch_step(L, st, atoms, nl_struct, params)
+            count = min(self.chunk, target - done)
+            if self.graphs and count == self.chunk and _device.TIMED is None:
+                self._replay_chunk(L, atoms, nl_struct, params)
+            else:
+                for _ in range(count):
+                    self._launch_step(L, st, atoms, nl_struct, params)
             self._check_status()
         sim.timestep = target
+
+    def _replay_chunk(self, L, atoms, nl_struct, params) -> None:
+        """One chunk of steps as a CUDA graph (captured on first use and after a rebuild)."""
+        sim = self.sim
+        key = (sim.neighbor.build_count, sim.atom.buffers.xr.data_ptr(), sim.history.touch.data_ptr(),
+               sim.neighbor.nbr.data_ptr())
+        if self._graph is None or self._graph_key != key:
+            self._graph = None
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.graph(g, stream=side):
+                st = _device.stream()
+                for _ in range(self.chunk):
+                    self._launch_step(L, st, atoms, nl_struct, params)
+            torch.cuda.current_stream().wait_stream(side)
+            self._graph, self._graph_key = g, key
+        self._graph.replay()
+        self.graph_replays += 1
+        self.graph_kernel_launches += self.chunk * self.LAUNCHES_PER_STEP
 
     def _check_status(self) -> None:
         st = int(self.status.item())
