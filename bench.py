@@ -185,6 +185,7 @@ def run_gpu_arm(args, p, precision, rank, world):
     clk = clocks.stop()
     # graph replays do not pass through the host entry points, so count the launches the graph holds
     launches = (L.tmps_launch_count() - l0) + (eng.graph_kernel_launches - g0)
+    cull = eng.cull_stats()
     # per-kernel CUDA-event timings: the next K steps launched one by one (same run, same state)
     _device.TIMED = {k: [] for k in names}
     eng.run(K)
@@ -204,7 +205,7 @@ def run_gpu_arm(args, p, precision, rank, world):
     kern = {k: (sum(v) / len(v) if v else None) for k, v in timed.items()}
     return dict(sim=sim, n=n, ms=ms, launches=launches, clocks=clk, kern_ms=kern, n_nb=n_nb, n_c=n_c,
                 pressure=pressure, builds=sim.neighbor.build_count, rebuilds_timed=eng.rebuilds,
-                steps_run=sim.timestep)
+                steps_run=sim.timestep, cull=cull)
 
 
 def run_e2e(args, p, precision):
@@ -381,7 +382,8 @@ def main():
                            for kk in kb},
             "mean_pressure": scal(v["pressure"]), "pressure": list(map(float, v["pressure"])),
             "mean_pressure_rel_err_vs_oracle": None if p_oracle is None else rel(scal(v["pressure"]), scal(p_oracle)),
-            "gpu_launches": v["launches"], "rebuilds_in_timed_steps": v["rebuilds_timed"]}
+            "gpu_launches": v["launches"], "rebuilds_in_timed_steps": v["rebuilds_timed"],
+            "groups_culled": {"groups": v["cull"][0], "culled_after_timed_steps": v["cull"][1]}}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": r["ms"] / K, "higher_is_better": True, "scaling": "weak",

@@ -183,6 +183,16 @@ typedef struct tmps_engine {
     /* FP32 copies of per-step constants, so no thread converts a double */
     float dt_hi, dt_lo, trigger32, gamma_lin32, gamma_ang32, pad3_;
     float eps_hi[4], eps_lo[4]; /* remap_scale - 1 as a double word (mixed) */
+    /* Exact culling of contact-free atom groups in C's first pass (set by
+     * tmps_fused_bounds): a group whose smallest gap at the reference
+     * positions exceeds 2 sqrt(maxd2) + shift_bound + cull_tol holds no
+     * contact. */
+    double prd_ref[3];       /* box lengths at the reference */
+    int64_t part_off;        /* byte offset of the virial partials in the scratch */
+    float shift_bound;       /* running max of sum_d |prd_d - prd_ref_d| */
+    uint32_t maxd2_bits;     /* running max of |x - x0|^2 over atoms and steps, FP32 bits */
+    int32_t cull;            /* 1: the per-group gaps in the scratch are valid */
+    float cull_tol;          /* absolute slack for the FP32 rounding of the test */
 } tmps_engine;
 
 /* ---- library ---------------------------------------------------------- */
@@ -314,13 +324,25 @@ int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* 
  * force and torque into f / torque. */
 int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream);
 
-/* Launch A (see tmps_engine). */
-int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* stream);
+/* After tmps_fused_prepare, with the list of the last build: per 32-atom
+ * group, the smallest gap |d| - (ri + rj) at the build positions x0 (into
+ * `scratch`), and every flag word set.  Resets the running bounds in d_eng;
+ * cull = 0 leaves culling off (C then screens every group).  No reference
+ * counterpart: it lets C skip groups that cannot touch without changing any
+ * result. */
+int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
+                      const tmps_pair_params* p, int32_t cull, void* scratch, void* stream);
+
+/* Launch A (see tmps_engine).  `scratch` is C's: A reads the flag words of
+ * the last C (an unflagged atom's force and torque are exact zeros and are
+ * not loaded) and writes the first virial partials, the kinetic term
+ * sum m v v of every atom at mid-step velocity. */
+int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* scratch, void* stream);
 
 /* Launch C, two kernels: a screen over all atoms (finishes contact-free ones,
  * flags the rest) and the contact law over the flagged ones.  `scratch`
- * (tmps_fused_scratch_bytes(n), caller memory) receives the virial partial
- * sums (d_eng->nblocks = tmps_fused_blocks(n) of them) and the flags. */
+ * (tmps_fused_scratch_bytes(n), caller memory: flag words, per-group gaps,
+ * then the d_eng->nblocks = tmps_fused_blocks(n) virial partial sums). */
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
                  const tmps_pair_params* p, void* scratch, void* stream);
 
@@ -328,9 +350,9 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
 int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const void* scratch,
                      int32_t* d_status, void* stream);
 
-/* Number of virial partial sums C writes for n atoms with this pair style
- * (tmps_pair_params.style) in this form (mixed 0/1): one per block of
- * one resident wave of each of its two kernels. */
+/* Number of virial partial sums A and C write for n atoms with this pair
+ * style (tmps_pair_params.style) in this form (mixed 0/1): one per block of
+ * one resident wave of A and of C's contact pass. */
 int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed);
 
 /* Scratch bytes tmps_fused_c / tmps_fused_servo need (same arguments). */

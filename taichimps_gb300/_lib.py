@@ -95,6 +95,9 @@ class Engine(ctypes.Structure):
         ("dt_hi", ctypes.c_float), ("dt_lo", ctypes.c_float), ("trigger32", ctypes.c_float),
         ("gamma_lin32", ctypes.c_float), ("gamma_ang32", ctypes.c_float), ("pad3_", ctypes.c_float),
         ("eps_hi", ctypes.c_float * 4), ("eps_lo", ctypes.c_float * 4),
+        ("prd_ref", c_f64 * 3), ("part_off", ctypes.c_int64),
+        ("shift_bound", ctypes.c_float), ("maxd2_bits", ctypes.c_uint32), ("cull", c_i32),
+        ("cull_tol", ctypes.c_float),
     ]
 
 
@@ -128,7 +131,9 @@ _SIGS = {
     "tmps_remap_x": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
     "tmps_fused_prepare": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp, c_vp]),
     "tmps_mixed_unpack": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
-    "tmps_fused_a": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp]),
+    "tmps_fused_bounds": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
+                                  ctypes.POINTER(PairParams), c_i32, c_vp, c_vp]),
+    "tmps_fused_a": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp, c_vp]),
     "tmps_fused_c": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
                              ctypes.POINTER(PairParams), c_vp, c_vp]),
     "tmps_fused_servo": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -116,24 +116,53 @@ __device__ __forceinline__ bool rebuild_due(const tmps_engine* __restrict__ e, i
 
 // ------------------------------------------------------------------- A, FP64
 
+// Running maximum of |x - x0|^2 since the reference of the contact bounds
+// (non-negative FP32 values order as their bit patterns; NaN above all).
+__device__ __forceinline__ void note_displacement(tmps_engine* __restrict__ e, float dd) {
+    const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(dd));
+    if ((threadIdx.x & 31) == 0 && m > *(volatile uint32_t*)&e->maxd2_bits) atomicMax(&e->maxd2_bits, m);
+}
+
+// Bit of atom i in the flag words: its force and torque may be nonzero (the
+// words of C's first pass; all ones before the first pass after a build).
+__device__ __forceinline__ bool force_live(const uint32_t* __restrict__ flags, int i) {
+    return flags == nullptr || ((flags[i >> 5] >> (i & 31)) & 1u);
+}
+
+// A runs as one resident wave striding over the atoms; besides the update
+// it sums the kinetic part of the virial, sum m v(t+dt/2) v(t+dt/2), over
+// every atom into per-block partials: an atom C finds contact-free ends the
+// step with that velocity, and C adds m (v(t+dt) v(t+dt) - v(t+dt/2)
+// v(t+dt/2)) for the rest (thermo.py:94-101).
 __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* __restrict__ b,
-                                                  tmps_engine* __restrict__ e) {
+                                                  tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
+                                                  double* __restrict__ part) {
+    __shared__ double smem[6 * (kBlockA / 32)];
     if (e->aborted) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = a.n;
+    const int lane = threadIdx.x & 31;
     const int32_t s = (int32_t)(e->step + 1);
+    const double dt = e->dt, dtf = 0.5 * dt;
+    const bool fin = e->final_pending != 0, remap = b->remap_pending != 0;
     bool hit = false;
-    if (i < n) {
-        const double dt = e->dt, dtf = 0.5 * dt;
+    float dd = 0.0f;
+    double K[6] = {0, 0, 0, 0, 0, 0};
+    const int stride = gridDim.x * blockDim.x;
+    for (int b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); b0 < n; b0 += stride) {
+        const int i = b0 + lane;
+        if (i >= n) continue;
         double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
         const double im = a.rinv[i], iI = a.rinv[n + i];
-        const double f[3] = {a.f[i], a.f[n + i], a.f[2 * n + i]};
-        const double t[3] = {a.torque[i], a.torque[n + i], a.torque[2 * n + i]};
-        if (e->final_pending) {  // second half-kick of the previous step
+        double f[3] = {0.0, 0.0, 0.0}, t[3] = {0.0, 0.0, 0.0};
+        if (force_live(flags, i)) {
+            f[0] = a.f[i]; f[1] = a.f[n + i]; f[2] = a.f[2 * n + i];
+            t[0] = a.torque[i]; t[1] = a.torque[n + i]; t[2] = a.torque[2 * n + i];
+        }
+        if (fin) {  // second half-kick of the previous step
             v.x += dtf * (f[0] * im); v.y += dtf * (f[1] * im); v.z += dtf * (f[2] * im);
             w.x += dtf * (t[0] * iI); w.y += dtf * (t[1] * iI); w.z += dtf * (t[2] * iI);
         }
-        if (b->remap_pending) {  // remap x of the previous step's servo update
+        if (remap) {  // remap x of the previous step's servo update
             x.x = b->lo[0] + (x.x - b->old_lo[0]) * e->remap_scale[0];
             x.y = b->lo[1] + (x.y - b->old_lo[1]) * e->remap_scale[1];
             x.z = b->lo[2] + (x.z - b->old_lo[2]) * e->remap_scale[2];
@@ -146,9 +175,21 @@ __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* _
         st4(a.om, i, w);
         const double d0 = __dsub_rn(x.x, a.x0[i]), d1 = __dsub_rn(x.y, a.x0[n + i]),
                      d2 = __dsub_rn(x.z, a.x0[2 * n + i]);
-        hit = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)) > e->trigger_sq;
+        const double q = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+        hit = hit || q > e->trigger_sq;
+        dd = fmaxf(dd, __double2float_ru(q));
+        const double kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
+                               (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
+#pragma unroll
+        for (int c = 0; c < 6; ++c) K[c] += kin[c];
     }
-    if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) e->disp_stamp = s;
+    if (__any_sync(0xffffffffu, hit) && lane == 0) e->disp_stamp = s;
+    note_displacement(e, dd);
+    block_sum<6, kBlockA>(K, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = K[c];
+    }
 }
 
 // ------------------------------------------------------------------ A, mixed
@@ -157,32 +198,42 @@ __device__ __forceinline__ int cell_x(int32_t c) { return c & 1023; }
 __device__ __forceinline__ int cell_y(int32_t c) { return (c >> 10) & 1023; }
 __device__ __forceinline__ int cell_z(int32_t c) { return (c >> 20) & 1023; }
 
-__global__ void __launch_bounds__(kBlockA, 5) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
-                                                  tmps_engine* __restrict__ e) {
+__global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                     tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
+                                                     double* __restrict__ part) {
     // Double-word state (hi + lo, both FP32) updated with error-free FP32
     // transforms: the FP64 pipe of this part is ~70x narrower than FP32, and
     // a double<->float conversion costs as much as a DFMA, so this kernel
     // issues no FP64 instruction at all.
+    __shared__ float2 smem[6 * (kBlockA / 32)];
     if (e->aborted) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = a.n;
+    const int lane = threadIdx.x & 31;
     const int32_t s = (int32_t)(e->step + 1);
+    const float dth = e->dt_hi, dtl = e->dt_lo;
+    // merged half-kicks: the previous step's second and this step's first
+    const float kick = e->final_pending ? dth : 0.5f * dth;
+    const bool remap = b->remap_pending != 0;
     bool hit = false;
-    if (i < n) {
-        const float dth = e->dt_hi, dtl = e->dt_lo;
-        // merged half-kicks: the previous step's second and this step's first
-        const float kick = e->final_pending ? dth : 0.5f * dth;
+    float dd = 0.0f;
+    float Kh[6] = {0, 0, 0, 0, 0, 0}, Kl[6] = {0, 0, 0, 0, 0, 0};
+    const int stride = gridDim.x * blockDim.x;
+    for (int b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); b0 < n; b0 += stride) {
+        const int i = b0 + lane;
+        if (i >= n) continue;
         float4 p = ld4f(a.pos32, i), pl = ld4f(a.pos32lo, i);
         float4 v = ld4f(a.vel32, i), vl = ld4f(a.vel32lo, i);
         float4 w = ld4f(a.om32, i), wl = ld4f(a.om32lo, i);
-        const float km = kick * vl.w, kI = kick * wl.w;  // vel32lo.w = 1/m, om32lo.w = 1/I
-        dw_add(v.x, vl.x, km * a.f32[i]);
-        dw_add(v.y, vl.y, km * a.f32[n + i]);
-        dw_add(v.z, vl.z, km * a.f32[2 * n + i]);
-        dw_add(w.x, wl.x, kI * a.torque32[i]);
-        dw_add(w.y, wl.y, kI * a.torque32[n + i]);
-        dw_add(w.z, wl.z, kI * a.torque32[2 * n + i]);
-        if (b->remap_pending) {
+        if (force_live(flags, i)) {  // an unflagged atom's force is an exact zero: nothing to add
+            const float km = kick * vl.w, kI = kick * wl.w;  // vel32lo.w = 1/m, om32lo.w = 1/I
+            dw_add(v.x, vl.x, km * a.f32[i]);
+            dw_add(v.y, vl.y, km * a.f32[n + i]);
+            dw_add(v.z, vl.z, km * a.f32[2 * n + i]);
+            dw_add(w.x, wl.x, kI * a.torque32[i]);
+            dw_add(w.y, wl.y, kI * a.torque32[n + i]);
+            dw_add(w.z, wl.z, kI * a.torque32[2 * n + i]);
+        }
+        if (remap) {
             // remap x scales a cell-relative offset with the box: o += o * eps
             dw_add(p.x, pl.x, p.x * e->eps_hi[0] + (p.x * e->eps_lo[0] + pl.x * e->eps_hi[0]));
             dw_add(p.y, pl.y, p.y * e->eps_hi[1] + (p.y * e->eps_lo[1] + pl.y * e->eps_hi[1]));
@@ -203,26 +254,66 @@ __global__ void __launch_bounds__(kBlockA, 5) k_a32(tmps_atoms a, const tmps_box
         const float d0 = ((p.x - a.o0_32[i]) + pl.x) + (float)cell_x(c) * e->dh32[0] + e->dlo32[0];
         const float d1 = ((p.y - a.o0_32[n + i]) + pl.y) + (float)cell_y(c) * e->dh32[1] + e->dlo32[1];
         const float d2 = ((p.z - a.o0_32[2 * n + i]) + pl.z) + (float)cell_z(c) * e->dh32[2] + e->dlo32[2];
-        hit = (d0 * d0 + d1 * d1) + d2 * d2 > e->trigger32;
+        const float q = (d0 * d0 + d1 * d1) + d2 * d2;
+        hit = hit || q > e->trigger32;
+        dd = fmaxf(dd, q);
+        // kinetic term from the high words (vel32.w = m)
+        const float kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
+                              (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dw_add(Kh[k], Kl[k], kin[k]);
     }
-    if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) e->disp_stamp = s;
+    if (__any_sync(0xffffffffu, hit) && lane == 0) e->disp_stamp = s;
+    note_displacement(e, dd);
+    block_sum_dw<6, kBlockA>(Kh, Kl, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) reinterpret_cast<float2*>(part)[(size_t)blockIdx.x * 6 + k] = make_float2(Kh[k], Kl[k]);
+    }
 }
 
 // ---------------------------------------------------------------------- C
 
-// C, first pass (all atoms): is any neighbor within reach of contact?  The
+template <bool MIXED>
+__device__ __forceinline__ void zero_force(const tmps_atoms& A, int i) {
+    const int n = A.n;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if constexpr (MIXED) {
+            A.f32[c * n + i] = 0.0f;
+            A.torque32[c * n + i] = 0.0f;
+        } else {
+            A.f[c * n + i] = 0.0;
+            A.torque[c * n + i] = 0.0;
+        }
+    }
+}
+
+// C, first pass: is any neighbor of an atom within reach of contact?  The
 // test is the contact test itself in the FP64 form and a conservative FP32
 // version of it in the mixed form (the second pass decides exactly).  Atoms
 // with no such neighbor are finished here -- zero force and torque, their
-// contact history cleared, the kinetic virial term -- and the rest are
-// flagged, one ballot word per 32-atom group, for the second pass.  This
-// pass holds few registers, so it runs at high occupancy over the many
-// contact-free atoms of a loose packing.
+// contact history cleared; their kinetic virial term is A's -- and the rest
+// are flagged, one ballot word per 32-atom group, for the second pass.
+//
+// Two economies, neither of which changes a result:
+//  * a whole group is finished without reading its rows when its smallest
+//    gap |d| - (ri + rj) at the reference positions (tmps_fused_bounds)
+//    exceeds 2 max|x - x0| + the change of the periodic image shifts + a
+//    rounding slack: by the triangle inequality none of its pairs can touch.
+//    Both running maxima only grow, so such a group has had no contact since
+//    the reference either, and its contact history is already clear.
+//  * the flag words double as "force may be nonzero": an atom's force and
+//    torque are written (as zeros) only when it was flagged the step
+//    before, so every unflagged atom holds an exact zero, which A relies on
+//    to skip loading them.
+// This pass writes no sums, so which warp handles which group is free: a
+// warp takes 32 groups strided over the system (one per lane) and checks
+// their bounds at once, then screens the live ones.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlockScreen)
     k_screen(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B, tmps_engine* __restrict__ E, int hist,
-             uint32_t* __restrict__ flags, double* __restrict__ part) {
-    __shared__ double smem[6 * (kBlockScreen / 32)];
+             uint32_t* __restrict__ flags, const float* __restrict__ gap) {
     if (E->aborted) return;
     const int64_t s = E->step + 1;
     if (rebuild_due(E, s)) return;
@@ -230,6 +321,12 @@ __global__ void __launch_bounds__(kBlockScreen)
     const int lane = threadIdx.x & 31;
     const int ngroups = (n + 31) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const bool cull = E->cull != 0;
+    float thr = 0.0f;
+    if (cull) {
+        const float md = sqrtf(__uint_as_float(E->maxd2_bits));
+        thr = ((2.0f * md) * 1.0001f + E->shift_bound) + E->cull_tol;
+    }
     float hh[3], prd32[3], iprd32[3];
     double prd64[3], iprd64[3];
     int per[3], single[3];
@@ -246,114 +343,166 @@ __global__ void __launch_bounds__(kBlockScreen)
             iprd64[c] = B->inv_prd[c];
         }
     }
-    float Kh[6] = {0, 0, 0, 0, 0, 0}, Kl[6] = {0, 0, 0, 0, 0, 0};
-    double Kd[6] = {0, 0, 0, 0, 0, 0};
     const bool two = L.slots > 1;
-    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += nwarps) {
-        const int i = (g << 5) + lane;
-        const bool valid = i < n;
-        bool cand = false;
-        if (valid) {
-            // every load that does not depend on another is issued at once:
-            // row length, own position, the first two neighbor entries (read
-            // whatever the row length; used only below it)
-            const int nn = L.nnb[i];
-            const int e0 = L.nbr[i];
-            const int e1 = two ? L.nbr[(size_t)n + i] : 0;
-            if constexpr (MIXED) {
-                const float4 pi = ld4f(A.pos32, i);
-                auto reach = [&](int e) {
-                    const float4 pj = ld4f(A.pos32, e & kNbrIndexMask);
-                    const int code = (unsigned)e >> kNbrIndexBits;
-                    const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1), (float)(code / 9 - 1)};
-                    const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj.x, pj.y, pj.z};
-                    float d[3];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
-                        if (single[c]) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
-                    }
-                    const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-                    const float rs = (pi.w + pj.w) * 1.00001f;
-                    return rq < rs * rs;
-                };
-                const bool c0 = nn > 0 && reach(e0);
-                const bool c1 = nn > 1 && reach(e1);
-                cand = c0 || c1;
-                for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
-            } else {
-                const double4 pi = ld4(A.xr, i);
-                auto reach = [&](int e) {
-                    const double4 pj = ld4(A.xr, e & kNbrIndexMask);
-                    double d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
-#pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        if (per[c] == 1) d[c] -= rint(d[c] * iprd64[c]) * prd64[c];
-                    const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-                    const double radsum = pi.w + pj.w;
-                    return rsq < radsum * radsum && rsq > 1e-28;
-                };
-                const bool c0 = nn > 0 && reach(e0);
-                const bool c1 = nn > 1 && reach(e1);
-                cand = c0 || c1;
-                for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int base = gw; base < ngroups; base += 32 * nwarps) {
+        const int mygrp = base + lane * nwarps;
+        uint32_t myold = 0u;
+        bool live = false;
+        if (mygrp < ngroups) {
+            myold = flags[mygrp];
+            live = !(cull && gap[mygrp] > thr);
+            if (!live && myold != 0u) {
+                // culled now, flagged last step: clear the stale forces
+                for (uint32_t w = myold; w; w &= w - 1) zero_force<MIXED>(A, (mygrp << 5) + __ffs(w) - 1);
+                flags[mygrp] = 0u;
             }
         }
-        const uint32_t word = __ballot_sync(0xffffffffu, cand);
-        if (lane == 0) flags[g] = word;
-        if (valid && !cand) {
-            if (hist && L.touch[i] != 0ull) L.touch[i] = 0ull;
-            if constexpr (MIXED) {
+        uint32_t pending = __ballot_sync(0xffffffffu, live);
+        while (pending) {
+            const int src = __ffs(pending) - 1;
+            pending &= pending - 1;
+            const int g = base + src * nwarps;
+            const uint32_t old = __shfl_sync(0xffffffffu, myold, src);
+            const int i = (g << 5) + lane;
+            const bool valid = i < n;
+            bool cand = false;
+            if (valid) {
+                // every load that does not depend on another is issued at once:
+                // row length, own position, the first two neighbor entries (read
+                // whatever the row length; used only below it)
+                const int nn = L.nnb[i];
+                const int e0 = L.nbr[i];
+                const int e1 = two ? L.nbr[(size_t)n + i] : 0;
+                if constexpr (MIXED) {
+                    const float4 pi = ld4f(A.pos32, i);
+                    auto reach = [&](int e) {
+                        const float4 pj = ld4f(A.pos32, e & kNbrIndexMask);
+                        const int code = (unsigned)e >> kNbrIndexBits;
+                        const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1), (float)(code / 9 - 1)};
+                        const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj.x, pj.y, pj.z};
+                        float d[3];
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    A.f32[c * n + i] = 0.0f;
-                    A.torque32[c * n + i] = 0.0f;
+                        for (int c = 0; c < 3; ++c) {
+                            d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
+                            if (single[c]) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
+                        }
+                        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                        const float rs = (pi.w + pj.w) * 1.00001f;
+                        return rq < rs * rs;
+                    };
+                    const bool c0 = nn > 0 && reach(e0);
+                    const bool c1 = nn > 1 && reach(e1);
+                    cand = c0 || c1;
+                    for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
+                } else {
+                    const double4 pi = ld4(A.xr, i);
+                    auto reach = [&](int e) {
+                        const double4 pj = ld4(A.xr, e & kNbrIndexMask);
+                        double d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            if (per[c] == 1) d[c] -= rint(d[c] * iprd64[c]) * prd64[c];
+                        const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                        const double radsum = pi.w + pj.w;
+                        return rsq < radsum * radsum && rsq > 1e-28;
+                    };
+                    const bool c0 = nn > 0 && reach(e0);
+                    const bool c1 = nn > 1 && reach(e1);
+                    cand = c0 || c1;
+                    for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
                 }
-                const float4 v = ld4f(A.vel32, i);
-                const float kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
-                                      (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
-#pragma unroll
-                for (int c = 0; c < 6; ++c) dw_add(Kh[c], Kl[c], kin[c]);
-            } else {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    A.f[c * n + i] = 0.0;
-                    A.torque[c * n + i] = 0.0;
-                }
-                const double4 v = ld4(A.vm, i);
-                const double kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
-                                       (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
-#pragma unroll
-                for (int c = 0; c < 6; ++c) Kd[c] += kin[c];
             }
-        }
-    }
-    if constexpr (MIXED) {
-        // partials as double words (hi, lo), summed the same way by S
-        block_sum_dw<6, kBlockScreen>(Kh, Kl, reinterpret_cast<float2*>(smem));
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) reinterpret_cast<float2*>(part)[(size_t)blockIdx.x * 6 + c] = make_float2(Kh[c], Kl[c]);
-        }
-    } else {
-        block_sum<6, kBlockScreen>(Kd, smem);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = Kd[c];
+            const uint32_t word = __ballot_sync(0xffffffffu, cand);
+            if (lane == 0 && word != old) flags[g] = word;
+            if (valid && !cand) {
+                if (hist && L.touch[i] != 0ull) L.touch[i] = 0ull;
+                if ((old >> lane) & 1u) zero_force<MIXED>(A, i);
+            }
         }
     }
 }
 
+// Per-group contact bounds at the reference positions x0 (the positions of
+// the last build): the smallest gap |d| - (ri + rj) over the group's rows,
+// rounded down to FP32; -inf for a group holding a live contact or when a
+// periodic dimension has a single bin (the image is then not fixed by the
+// stencil).  Every flag word is set: each atom's force may be nonzero.
+__global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B,
+                                                     tmps_engine* __restrict__ E, int hist, int cull, uint32_t* flags,
+                                                     float* gap) {
+    const int n = A.n;
+    const int lane = threadIdx.x & 31;
+    const int ngroups = (n + 31) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    int per[3];
+    double prd[3], iprd[3];
+    bool single = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        per[c] = B->per[c];
+        prd[c] = B->prd[c];
+        iprd[c] = B->inv_prd[c];
+        single = single || (per[c] == 1 && B->g[c] == 1);
+    }
+    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += nwarps) {
+        const int i = (g << 5) + lane;
+        double gmin = 1e300;
+        if (i < n) {
+            const double xi[3] = {A.x0[i], A.x0[n + i], A.x0[2 * n + i]};
+            const double ri = A.xr[4 * (size_t)i + 3];
+            const int nn = L.nnb[i];
+            for (int k = 0; k < nn; ++k) {
+                const int j = L.nbr[(size_t)k * n + i] & kNbrIndexMask;
+                double d[3] = {xi[0] - A.x0[j], xi[1] - A.x0[n + j], xi[2] - A.x0[2 * n + j]};
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    if (per[c] == 1) d[c] -= rint(d[c] * iprd[c]) * prd[c];
+                const double r = sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+                const double gp = r - (ri + A.xr[4 * (size_t)j + 3]);
+                gmin = gp == gp ? fmin(gmin, gp) : -1e300;  // a NaN pair pins the group
+            }
+            if ((hist && L.touch[i] != 0ull) || single) gmin = -1e300;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) gmin = fmin(gmin, __shfl_down_sync(0xffffffffu, gmin, o));
+        if (lane == 0) {
+            gap[g] = __double2float_rd(gmin);
+            flags[g] = 0xffffffffu;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        float hmin = (float)B->hcell[0];
+        hmin = fminf(hmin, (float)B->hcell[1]);
+        hmin = fminf(hmin, (float)B->hcell[2]);
+        E->cull_tol = 1e-5f * hmin;
+        E->maxd2_bits = 0u;
+        E->shift_bound = 0.0f;
+        for (int c = 0; c < 3; ++c) E->prd_ref[c] = B->prd[c];
+        E->cull = (cull && !single) ? 1 : 0;
+    }
+}
+
 // C, second pass: the atoms the screen flagged (some neighbor within reach
-// of contact), with the full contact law.  Warps walk 32-atom groups in a
-// fixed order and skip groups whose flag word is zero, so the per-block
-// virial partials do not depend on scheduling.
+// of contact), with the full contact law.  A warp owns 32 groups strided
+// over the system (warp w: w, w + nwarps, ...), so flagged atoms -- which
+// cluster in space, and atoms are in Morton order -- spread over many warps
+// and SMs.  The warp takes the flagged atoms of all its groups in rounds of
+// up to 32 (one per lane, in group then atom order) and lays the (atom,
+// neighbor slot) entries of a round across the lanes, 32 entries per pass:
+// the latency of a round is that of one contact, not of its longest row or
+// of the number of groups.  Each atom's force, torque and virial are then
+// summed by the atom's own lane over its entries in slot order -- the order
+// of a one-thread-per-atom loop, so the sums are unchanged.  Per-block virial
+// partials depend only on the flag words, not on scheduling.
 template <int STYLE, bool MIXED>
 __global__ void __launch_bounds__(kBlockC)
     k_c(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
         tmps_engine* __restrict__ E, const uint32_t* __restrict__ flags, double* __restrict__ part) {
     using T = typename std::conditional<MIXED, float, double>::type;
     __shared__ double smem[6 * (kBlockC / 32)];
+    __shared__ uint8_t owner[kBlockC / 32][32];
+    __shared__ int32_t roster[kBlockC / 32][32];
     if (E->aborted) return;
     const int64_t s = E->step + 1;
     if (rebuild_due(E, s)) return;  // S marks the step aborted; the host rebuilds
@@ -363,292 +512,385 @@ __global__ void __launch_bounds__(kBlockC)
     T dt;
     if constexpr (MIXED) dt = E->dt_hi;
     else dt = E->dt;
+    // per-step constants
+    T hh[3] = {0, 0, 0}, prd[3], iprd[3];
+    float hlo[3] = {0, 0, 0}, prdlo[3] = {0, 0, 0};
+    int per[3], single[3], gdim[3];
+    T hrate[3] = {0, 0, 0}, hshear[3] = {0, 0, 0};
+    const bool vremap = B->vremap != 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        per[c] = B->per[c];
+        gdim[c] = B->g[c];
+        if constexpr (MIXED) {
+            hh[c] = E->h32[c];
+            hlo[c] = E->hlo32[c];
+            prd[c] = E->prd32[c];
+            prdlo[c] = E->prdlo32[c];
+            iprd[c] = E->iprd32[c];
+            single[c] = E->single_bin[c];
+        } else {
+            prd[c] = B->prd[c];
+            iprd[c] = B->inv_prd[c];
+            single[c] = 0;
+        }
+    }
+    if (vremap) {
+        // n . h_rate for the image count n = (n0, n1, n2) of the partner
+        hrate[0] = (T)B->h_rate[0]; hrate[1] = (T)B->h_rate[1]; hrate[2] = (T)B->h_rate[2];
+        hshear[0] = (T)B->h_rate[3]; hshear[1] = (T)B->h_rate[4]; hshear[2] = (T)B->h_rate[5];
+    }
     double Vd[6] = {0, 0, 0, 0, 0, 0};
     float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};  // mixed: per-thread double words
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int ngroups = (n + 31) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    // groups are dealt to warps round-robin (warp w owns w, w + nwarps, ...),
-    // so a run of flagged neighbouring groups -- contacts cluster in space,
-    // and atoms are in Morton order -- spreads over many warps and SMs; a
-    // lane reads one flag word, the warp visits only the nonzero ones
+    const size_t ss = (size_t)L.slots * n;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     for (int base = gw; base < ngroups; base += 32 * nwarps) {
-    const int mine = base + lane * nwarps;
-    const uint32_t myword = mine < ngroups ? flags[mine] : 0u;
-    uint32_t pending = __ballot_sync(0xffffffffu, myword != 0u);
-    while (pending) {
-        const int src = __ffs(pending) - 1;
-        pending &= pending - 1;
-        const uint32_t word = __shfl_sync(0xffffffffu, myword, src);
-        if (!((word >> lane) & 1u)) continue;
-        const int i = ((base + src * nwarps) << 5) + lane;
+    const int mygrp = base + lane * nwarps;
+    const uint32_t myword = mygrp < ngroups ? flags[mygrp] : 0u;
+    // flagged atoms of the 32 groups, numbered in lane (group) then bit order
+    const int cnt = __popc(myword);
+    int before = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, before, o);
+        if (lane >= o) before += t;
+    }
+    const int natoms = __shfl_sync(0xffffffffu, before, 31);
+    before -= cnt;
+    for (int r0 = 0; r0 < natoms; r0 += 32) {
+        if (before < r0 + 32 && before + cnt > r0) {
+            int idx = before;
+            for (uint32_t w = myword; w; w &= w - 1, ++idx)
+                if (idx >= r0 && idx < r0 + 32) roster[wib][idx - r0] = (mygrp << 5) + __ffs(w) - 1;
+        }
+        __syncwarp();
+        // this lane's atom and its row: entries [start, start + nn) of the round
+        const bool mine = lane < natoms - r0;
+        const int i = mine ? roster[wib][lane] : 0;
+        __syncwarp();
+        const int nn = mine ? L.nnb[i] : 0;
+        const uint64_t touch = (hist && mine) ? L.touch[i] : 0ull;
+        int incl = nn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int start = incl - nn;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
         T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
-        T xi[3], ri, mi, vi[3], wi[3];
-        T hh[3] = {0, 0, 0}, prd[3], iprd[3];
-        int per[3], single[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            per[c] = B->per[c];
-            if constexpr (MIXED) {
-                hh[c] = E->h32[c];
-                prd[c] = E->prd32[c];
-                iprd[c] = E->iprd32[c];
-                single[c] = E->single_bin[c];
-            } else {
-                prd[c] = B->prd[c];
-                iprd[c] = B->inv_prd[c];
-                single[c] = 0;
-            }
-        }
-        int32_t ci = 0;
-        if constexpr (MIXED) {
-            const float4 p = ld4f(A.pos32, i), v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
-            xi[0] = p.x; xi[1] = p.y; xi[2] = p.z; ri = p.w;
-            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-            if (B->vremap) ci = A.cell32[i];
-        } else {
-            const double4 p = ld4(A.xr, i), v = ld4(A.vm, i), w = ld4(A.om, i);
-            xi[0] = p.x; xi[1] = p.y; xi[2] = p.z; ri = p.w;
-            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-        }
-        const int nn = L.nnb[i];
-        const uint64_t touch = hist ? L.touch[i] : 0ull;
         uint64_t newtouch = 0ull;
-        const size_t ss = (size_t)L.slots * n;
-        for (int k = 0; k < nn; ++k) {
-            const int e = L.nbr[(size_t)k * n + i];
-            const int j = e & kNbrIndexMask;
-            const bool lo = i < j;
-            T xj[3], rj;
-            if constexpr (MIXED) {
-                const float4 p = ld4f(A.pos32, j);
-                xj[0] = p.x; xj[1] = p.y; xj[2] = p.z; rj = p.w;
-            } else {
-                const double4 p = ld4(A.xr, j);
-                xj[0] = p.x; xj[1] = p.y; xj[2] = p.z; rj = p.w;
+        for (int p0 = 0; p0 < total; p0 += 32) {
+            if (mine) {
+                const int k0 = max(start, p0), k1 = min(start + nn, p0 + 32);
+                for (int k = k0; k < k1; ++k) owner[wib][k - p0] = (uint8_t)lane;
             }
-            // separation x_i - x_j
-            T d[3];
-            T nimg[3] = {0, 0, 0};
-            if constexpr (MIXED) {
-                // offsets are relative to each atom's own cell: j's cell is the
-                // stencil offset (ox, oy, oz) away from i's, so
-                // x_i - x_j = (o_i - o_j) - offset * h
+            __syncwarp();
+            const bool live = p0 + lane < total;
+            const int ol = live ? owner[wib][lane] : 0;
+            const int ost = __shfl_sync(0xffffffffu, start, ol);
+            const int ia = __shfl_sync(0xffffffffu, i, ol);  // the entry's row atom
+            const uint32_t tlo = __shfl_sync(0xffffffffu, (uint32_t)touch, ol);
+            const uint32_t thi = __shfl_sync(0xffffffffu, (uint32_t)(touch >> 32), ol);
+            bool contact = false;
+            T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
+            if (live) {
+                const int k = p0 + lane - ost;      // the entry's slot in its row
+                const int e = L.nbr[(size_t)k * n + ia];
+                const int j = e & kNbrIndexMask;
+                const bool lo = ia < j;
+                T xi[3], xj[3], ri, rj;
+                int32_t ci = 0;
+                if constexpr (MIXED) {
+                    const float4 pi = ld4f(A.pos32, ia), pj = ld4f(A.pos32, j);
+                    xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+                    xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+                    if (vremap) ci = A.cell32[ia];
+                } else {
+                    const double4 pi = ld4(A.xr, ia), pj = ld4(A.xr, j);
+                    xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+                    xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+                }
+                // separation x_i - x_j
+                T d[3];
+                T nimg[3] = {0, 0, 0};
                 const int code = (unsigned)e >> kNbrIndexBits;
                 const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+                if constexpr (MIXED) {
+                    // offsets are relative to each atom's own cell: j's cell is
+                    // the stencil offset (ox, oy, oz) away from i's, so
+                    // x_i - x_j = (o_i - o_j) - offset * h
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    d[c] = (xi[c] - xj[c]) - (float)off[c] * hh[c];
-                    if (single[c]) {
-                        nimg[c] = rintf(d[c] * iprd[c]);
-                        d[c] -= nimg[c] * prd[c];
+                    for (int c = 0; c < 3; ++c) {
+                        d[c] = (xi[c] - xj[c]) - (float)off[c] * hh[c];
+                        if (single[c]) {
+                            nimg[c] = rintf(d[c] * iprd[c]);
+                            d[c] -= nimg[c] * prd[c];
+                        }
+                    }
+                    if (vremap) {  // image count for the partner velocity shift
+                        const int32_t cj = A.cell32[j];
+                        const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
+                                           cell_z(ci) + off[2] - cell_z(cj)};
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / gdim[c]);
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        d[c] = xi[c] - xj[c];
+                        if (per[c] == 1) {
+                            nimg[c] = rint(d[c] * iprd[c]);
+                            d[c] -= nimg[c] * prd[c];
+                        }
                     }
                 }
-                if (B->vremap) {  // image count for the partner velocity shift
-                    const int32_t cj = A.cell32[j];
-                    const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
-                                       cell_z(ci) + off[2] - cell_z(cj)};
+                PairIn<T> in;
+                const T sg = lo ? T(1) : T(-1);
+                in.ra = lo ? ri : rj;
+                in.rb = lo ? rj : ri;
+                bool near;
+                if constexpr (MIXED) {
+                    // FP32 screen, with room for the FP32 rounding of the words
+                    const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                    const float rs = (ri + rj) * 1.00001f;
+                    near = rq < rs * rs;
+                    if (near) {
+                        // separation, |d|^2, |d| and the overlap from the high and
+                        // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
+                        // FP32 difference of two unit-size numbers keeps 2^-24)
+                        const float4 il = ld4f(A.pos32lo, ia), jl = ld4f(A.pos32lo, j);
+                        const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
+                        float dh[3], dl[3];
 #pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / B->g[c]);
-                }
-            } else {
+                        for (int c = 0; c < 3; ++c) {
+                            float s1, e1, s2, e2;
+                            two_sum(xi[c], -xj[c], s1, e1);
+                            two_sum(s1, -(float)off[c] * hh[c], s2, e2);
+                            const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), (float)off[c] * hlo[c]),
+                                                        __fadd_rn(e1, e2));
+                            two_sum(s2, low, dh[c], dl[c]);
+                            if (single[c]) {
+                                const float ni = rintf(dh[c] * iprd[c]);
+                                float s3, e3;
+                                two_sum(dh[c], -ni * prd[c], s3, e3);
+                                two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * prdlo[c]), e3), dh[c], dl[c]);
+                            }
+                            dh[c] = sg * dh[c];
+                            dl[c] = sg * dl[c];
+                        }
+                        // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
+                        float pp[3], pe[3];
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    d[c] = xi[c] - xj[c];
-                    if (per[c] == 1) {
-                        nimg[c] = rint(d[c] * iprd[c]);
-                        d[c] -= nimg[c] * prd[c];
+                        for (int c = 0; c < 3; ++c) {
+                            pp[c] = __fmul_rn(dh[c], dh[c]);
+                            pe[c] = __fmaf_rn(dh[c], dh[c], -pp[c]);
+                        }
+                        float t1, te1, rh, re;
+                        two_sum(pp[0], pp[1], t1, te1);
+                        two_sum(t1, pp[2], rh, re);
+                        const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]),
+                                                                                __fmul_rn(dh[1], dl[1])),
+                                                                     __fmul_rn(dh[2], dl[2])));
+                        const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])),
+                                                    cross);
+                        float rsh, rsl;
+                        two_sum(rh, rl0, rsh, rsl);
+                        const float r_hi = __fsqrt_rn(rsh);
+                        const float res = __fmaf_rn(-r_hi, r_hi, rsh);  // exact
+                        const float r_lo = __fdiv_rn(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
+                        // ra + rb, both words
+                        const float4 al = lo ? il : jl, bl = lo ? jl : il;
+                        float sh_, se_;
+                        two_sum(in.ra, in.rb, sh_, se_);
+                        const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
+                        const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
+                        near = delta > 0.0f && rsh > 1e-28f;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
+                        in.rsq = rsh;
+                        in.r = r_hi;
+                        in.delta = delta;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
+                    in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
+                    const T radsum = in.ra + in.rb;
+                    near = in.rsq < radsum * radsum && in.rsq > T(1e-28);
+                    if (near) {
+                        in.r = sqrt(in.rsq);
+                        in.delta = radsum - in.r;
                     }
                 }
-            }
-            PairIn<T> in;
-            const T sg = lo ? T(1) : T(-1);
-            in.ra = lo ? ri : rj;
-            in.rb = lo ? rj : ri;
-            if constexpr (MIXED) {
-                // FP32 screen, with room for the FP32 rounding of the words
-                const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-                const float rs = (ri + rj) * 1.00001f;
-                if (!(rq < rs * rs)) continue;
-                // near contact: separation, |d|^2, |d| and the overlap from the
-                // high and low FP32 words, so the overlap keeps ~2^-48 of |d|
-                // (an FP32 difference of two unit-size numbers would keep 2^-24)
-                const int code = (unsigned)e >> kNbrIndexBits;
-                const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
-                const float4 il = ld4f(A.pos32lo, i), jl = ld4f(A.pos32lo, j);
-                const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
-                float dh[3], dl[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    float s1, e1, s2, e2;
-                    two_sum(xi[c], -xj[c], s1, e1);
-                    two_sum(s1, -(float)off[c] * hh[c], s2, e2);
-                    const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), (float)off[c] * E->hlo32[c]),
-                                                __fadd_rn(e1, e2));
-                    two_sum(s2, low, dh[c], dl[c]);
-                    if (single[c]) {
-                        const float ni = rintf(dh[c] * iprd[c]);
-                        float s3, e3;
-                        two_sum(dh[c], -ni * prd[c], s3, e3);
-                        two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * E->prdlo32[c]), e3), dh[c], dl[c]);
+                if (near) {
+                    contact = true;
+                    T vi[3], wi[3], mi, vj[3], wj[3], mj;
+                    if constexpr (MIXED) {
+                        const float4 v = ld4f(A.vel32, ia), w = ld4f(A.om32, ia);
+                        const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
+                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+                    } else {
+                        const double4 v = ld4(A.vm, ia), w = ld4(A.om, ia);
+                        const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
+                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
                     }
-                    dh[c] = sg * dh[c];
-                    dl[c] = sg * dl[c];
+                    T dv[3] = {0, 0, 0};
+                    if (vremap) {
+                        // image count of x_a - x_b, then n . h_rate for partner b
+                        T na[3];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
+                        dv[0] = (na[0] * hrate[0] + na[1] * hshear[2]) + na[2] * hshear[1];
+                        dv[1] = na[1] * hrate[1] + na[2] * hshear[0];
+                        dv[2] = na[2] * hrate[2];
+                    }
+                    in.ma = lo ? mi : mj;
+                    in.mb = lo ? mj : mi;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        in.va[c] = lo ? vi[c] : vj[c];
+                        in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
+                        in.wa[c] = lo ? wi[c] : wj[c];
+                        in.wb[c] = lo ? wj[c] : wi[c];
+                    }
+                    double sh[3] = {0, 0, 0};
+                    const size_t so = (size_t)k * n + ia;
+                    const bool was = k < 32 ? ((tlo >> k) & 1u) : ((thi >> (k - 32)) & 1u);
+                    if (hist && was) {
+                        const double sgd = lo ? 1.0 : -1.0;
+                        sh[0] = sgd * L.shear[so];
+                        sh[1] = sgd * L.shear[ss + so];
+                        sh[2] = sgd * L.shear[2 * ss + so];
+                    }
+                    PairOut<T> out;
+                    contact_law<T, STYLE>(P, dt, 1, in, sh, out);
+                    if (hist) {
+                        const double sgd = lo ? 1.0 : -1.0;
+                        L.shear[so] = sgd * sh[0];
+                        L.shear[ss + so] = sgd * sh[1];
+                        L.shear[2 * ss + so] = sgd * sh[2];
+                    }
+                    const T arm = lo ? out.arm_a : out.arm_b;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        fc[c] = sg * out.f[c];
+                        tc[c] = arm * out.tor[c];
+                    }
+                    vc[0] = T(0.5) * (in.d[0] * out.f[0]);
+                    vc[1] = T(0.5) * (in.d[1] * out.f[1]);
+                    vc[2] = T(0.5) * (in.d[2] * out.f[2]);
+                    vc[3] = T(0.5) * (in.d[0] * out.f[1]);
+                    vc[4] = T(0.5) * (in.d[0] * out.f[2]);
+                    vc[5] = T(0.5) * (in.d[1] * out.f[2]);
                 }
-                // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
-                float p[3], pe[3];
+            }
+            // each row atom's lane takes its contacts in slot order
+            uint32_t cm = __ballot_sync(0xffffffffu, contact);
+            while (cm) {
+                const int q = __ffs(cm) - 1;
+                cm &= cm - 1;
+                const int oq = owner[wib][q];
+                T gf[3], gt[3], gv[6];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    p[c] = __fmul_rn(dh[c], dh[c]);
-                    pe[c] = __fmaf_rn(dh[c], dh[c], -p[c]);
+                    gf[c] = __shfl_sync(0xffffffffu, fc[c], q);
+                    gt[c] = __shfl_sync(0xffffffffu, tc[c], q);
                 }
-                float t1, te1, rh, re;
-                two_sum(p[0], p[1], t1, te1);
-                two_sum(t1, p[2], rh, re);
-                const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]), __fmul_rn(dh[1], dl[1])),
-                                                             __fmul_rn(dh[2], dl[2])));
-                const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])), cross);
-                float rsh, rsl;
-                two_sum(rh, rl0, rsh, rsl);
-                const float r_hi = __fsqrt_rn(rsh);
-                const float res = __fmaf_rn(-r_hi, r_hi, rsh);  // exact
-                const float r_lo = __fdiv_rn(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
-                // ra + rb, both words
-                const float4 al = lo ? il : jl, bl = lo ? jl : il;
-                float sh_, se_;
-                two_sum(in.ra, in.rb, sh_, se_);
-                const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
-                const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
-                if (!(delta > 0.0f && rsh > 1e-28f)) continue;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
-                in.rsq = rsh;
-                in.r = r_hi;
-                in.delta = delta;
-            } else {
+                for (int c = 0; c < 6; ++c) gv[c] = __shfl_sync(0xffffffffu, vc[c], q);
+                if (lane == oq) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
-                in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
-                const T radsum = in.ra + in.rb;
-                if (!(in.rsq < radsum * radsum && in.rsq > T(1e-28))) continue;
-                in.r = sqrt(in.rsq);
-                in.delta = radsum - in.r;
+                    for (int c = 0; c < 3; ++c) {
+                        F[c] += gf[c];
+                        Tq[c] += gt[c];
+                    }
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) V[c] += gv[c];
+                    newtouch |= 1ull << (p0 + q - start);
+                }
             }
-            T vj[3], wj[3], mj;
+            __syncwarp();
+        }
+        if (mine) {
+            if (hist && newtouch != touch) L.touch[i] = newtouch;
+            T vi[3], wi[3], mi;
             if constexpr (MIXED) {
-                const float4 v = ld4f(A.vel32, j), w = ld4f(A.om32, j);
-                vj[0] = v.x; vj[1] = v.y; vj[2] = v.z; mj = v.w;
-                wj[0] = w.x; wj[1] = w.y; wj[2] = w.z;
+                const float4 v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
+                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
             } else {
-                const double4 v = ld4(A.vm, j), w = ld4(A.om, j);
-                vj[0] = v.x; vj[1] = v.y; vj[2] = v.z; mj = v.w;
-                wj[0] = w.x; wj[1] = w.y; wj[2] = w.z;
+                const double4 v = ld4(A.vm, i), w = ld4(A.om, i);
+                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
             }
-            T dv[3] = {0, 0, 0};
-            if (B->vremap) {
-                // image count of x_a - x_b, then n . h_rate for partner b
-                T na[3];
+            if (E->cundall) {  // FixDampingCundall.post_force_kernel
+                T gl, ga;
+                if constexpr (MIXED) {
+                    gl = E->gamma_lin32;
+                    ga = E->gamma_ang32;
+                } else {
+                    gl = E->gamma_lin;
+                    ga = E->gamma_ang;
+                }
 #pragma unroll
-                for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
-                const double* h = B->h_rate;
-                dv[0] = (T)((na[0] * (T)h[0] + na[1] * (T)h[5]) + na[2] * (T)h[4]);
-                dv[1] = (T)(na[1] * (T)h[1] + na[2] * (T)h[3]);
-                dv[2] = (T)(na[2] * (T)h[2]);
+                for (int c = 0; c < 3; ++c) {
+                    const T sf = F[c] * vi[c] >= T(0) ? T(1) : T(-1);
+                    F[c] *= T(1) - gl * sf;
+                    const T st = Tq[c] * wi[c] >= T(0) ? T(1) : T(-1);
+                    Tq[c] *= T(1) - ga * st;
+                }
             }
-            in.ma = lo ? mi : mj;
-            in.mb = lo ? mj : mi;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                in.va[c] = lo ? vi[c] : vj[c];
-                in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
-                in.wa[c] = lo ? wi[c] : wj[c];
-                in.wb[c] = lo ? wj[c] : wi[c];
-            }
-            double sh[3] = {0, 0, 0};
-            const size_t so = (size_t)k * n + i;
-            if (hist && ((touch >> k) & 1ull)) {
-                const double sgd = lo ? 1.0 : -1.0;
-                sh[0] = sgd * L.shear[so];
-                sh[1] = sgd * L.shear[ss + so];
-                sh[2] = sgd * L.shear[2 * ss + so];
-            }
-            PairOut<T> out;
-            contact_law<T, STYLE>(P, dt, 1, in, sh, out);
-            if (hist) {
-                const double sgd = lo ? 1.0 : -1.0;
-                L.shear[so] = sgd * sh[0];
-                L.shear[ss + so] = sgd * sh[1];
-                L.shear[2 * ss + so] = sgd * sh[2];
-                newtouch |= 1ull << k;
-            }
-            const T arm = lo ? out.arm_a : out.arm_b;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                F[c] += sg * out.f[c];
-                Tq[c] += arm * out.tor[c];
-            }
-            V[0] += T(0.5) * (in.d[0] * out.f[0]);
-            V[1] += T(0.5) * (in.d[1] * out.f[1]);
-            V[2] += T(0.5) * (in.d[2] * out.f[2]);
-            V[3] += T(0.5) * (in.d[0] * out.f[1]);
-            V[4] += T(0.5) * (in.d[0] * out.f[2]);
-            V[5] += T(0.5) * (in.d[1] * out.f[2]);
-        }
-        if (hist && newtouch != touch) L.touch[i] = newtouch;
-        if (E->cundall) {  // FixDampingCundall.post_force_kernel
-            T gl, ga;
             if constexpr (MIXED) {
-                gl = E->gamma_lin32;
-                ga = E->gamma_ang32;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    A.f32[c * n + i] = F[c];
+                    A.torque32[c * n + i] = Tq[c];
+                }
             } else {
-                gl = E->gamma_lin;
-                ga = E->gamma_ang;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    A.f[c * n + i] = F[c];
+                    A.torque[c * n + i] = Tq[c];
+                }
             }
+            // kinetic part of the virial with the end-of-step velocity
+            // v(t+dt) = v(t+dt/2) + dt/2 f/m (thermo.py:94-101): A counted
+            // m v(t+dt/2) v(t+dt/2) for every atom; the difference goes here
+            // (the same products from the same words, so a zero force adds an
+            // exact zero)
+            T im;
+            if constexpr (MIXED) im = 1.0f / mi;
+            else im = A.rinv[i];
+            const T hdt = T(0.5) * dt;
+            T vf[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const T sf = F[c] * vi[c] >= T(0) ? T(1) : T(-1);
-                F[c] *= T(1) - gl * sf;
-                const T st = Tq[c] * wi[c] >= T(0) ? T(1) : T(-1);
-                Tq[c] *= T(1) - ga * st;
+            for (int c = 0; c < 3; ++c) vf[c] = vi[c] + hdt * (F[c] * im);
+            const T kin[6] = {(mi * vf[0]) * vf[0], (mi * vf[1]) * vf[1], (mi * vf[2]) * vf[2],
+                              (mi * vf[0]) * vf[1], (mi * vf[0]) * vf[2], (mi * vf[1]) * vf[2]};
+            const T kh[6] = {(mi * vi[0]) * vi[0], (mi * vi[1]) * vi[1], (mi * vi[2]) * vi[2],
+                             (mi * vi[0]) * vi[1], (mi * vi[0]) * vi[2], (mi * vi[1]) * vi[2]};
+            if constexpr (MIXED) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    dw_add(Vh[c], Vl[c], V[c]);
+                    dw_add(Vh[c], Vl[c], kin[c]);
+                    dw_add(Vh[c], Vl[c], -kh[c]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) Vd[c] += (V[c] + kin[c]) - kh[c];
             }
-        }
-        if constexpr (MIXED) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                A.f32[c * n + i] = F[c];
-                A.torque32[c * n + i] = Tq[c];
-            }
-        } else {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                A.f[c * n + i] = F[c];
-                A.torque[c * n + i] = Tq[c];
-            }
-        }
-        // kinetic part of the virial with the end-of-step velocity
-        // v(t+dt) = v(t+dt/2) + dt/2 f/m (thermo.py:94-101)
-        T im;
-        if constexpr (MIXED) im = 1.0f / mi;
-        else im = A.rinv[i];
-        const T hdt = T(0.5) * dt;
-        T vf[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) vf[c] = vi[c] + hdt * (F[c] * im);
-        const T kin[6] = {(mi * vf[0]) * vf[0], (mi * vf[1]) * vf[1], (mi * vf[2]) * vf[2],
-                          (mi * vf[0]) * vf[1], (mi * vf[0]) * vf[2], (mi * vf[1]) * vf[2]};
-        if constexpr (MIXED) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                dw_add(Vh[c], Vl[c], V[c]);
-                dw_add(Vh[c], Vl[c], kin[c]);
-            }
-        } else {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) Vd[c] += V[c] + kin[c];
         }
     }
     }
@@ -784,6 +1026,12 @@ __device__ void servo_update_warp(tmps_box& b, tmps_servo& sv, tmps_engine& e, c
             e.remap_scale[d] = nprd / prd;
         }
     }
+    if (e.cull) {
+        // change of the periodic image shifts since the contact bounds' reference
+        const double dd = lane < 3 ? fabs(nprd - e.prd_ref[d]) : 0.0;
+        const double d1 = __shfl_sync(0xffffffffu, dd, 1), d2 = __shfl_sync(0xffffffffu, dd, 2);
+        if (lane == 0) e.shift_bound = fmaxf(e.shift_bound, __double2float_ru((dd + d1) + d2));
+    }
     if (lane == 0) {
         b.vremap = sv.remap == 2 ? 1 : 0;
         b.remap_pending = sv.remap == 1 ? 1 : 0;
@@ -804,7 +1052,7 @@ __device__ __forceinline__ void copy_words(S* dst, const S* src) {
 // always adds component t % 6), so every load is coalesced and independent.
 // The mixed form's partials are double words and are summed as such; only
 // the six totals become FP64.
-__global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps_engine* e, const double* part,
+__global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps_engine* e, const char* scratch,
                                                int32_t* status) {
     __shared__ double red[kBlockS];
     __shared__ float2 redf[kBlockS];
@@ -825,6 +1073,7 @@ __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps
     __syncthreads();
     const bool servo_now = se.servo && ((ssv.step_count + 1) % ssv.nevery == 0);
     if (servo_now) {
+        const double* part = reinterpret_cast<const double*>(scratch + se.part_off);
         const int total = se.nblocks * 6;
         int k = threadIdx.x;
         if (se.mixed) {
@@ -925,8 +1174,12 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
     st4f(a.om32lo, i, make_float4(wlo[0], wlo[1], wlo[2], (float)(1.0 / w.w)));
 }
 
-__global__ void k_prepare_engine(const tmps_box* __restrict__ b, tmps_engine* e) {
+__global__ void k_prepare_engine(const tmps_box* __restrict__ b, tmps_engine* e, int64_t part_off) {
     if (threadIdx.x || blockIdx.x) return;
+    e->part_off = part_off;
+    e->cull = 0;  // until tmps_fused_bounds sets the bounds
+    e->maxd2_bits = 0u;
+    e->shift_bound = 0.0f;
     for (int d = 0; d < 3; ++d) {
         e->lo0[d] = b->lo[d];
         e->h0[d] = b->hcell[d];
@@ -1079,25 +1332,36 @@ int contact_wave(int style, bool mixed) {
     return v;
 }
 int screen_blocks(int n, bool mixed) { const int b = grid_for(n, kBlockScreen); return b < screen_wave(mixed) ? b : screen_wave(mixed); }
+int a_wave(bool mixed) {
+    static int w[2] = {0, 0};
+    int& v = w[mixed ? 1 : 0];
+    if (!v) v = mixed ? wave_blocks(k_a32, kBlockA) : wave_blocks(k_a64, kBlockA);
+    return v;
+}
+int a_blocks(int n, bool mixed) { const int b = grid_for(n, kBlockA); return b < a_wave(mixed) ? b : a_wave(mixed); }
 int contact_blocks(int n, int style, bool mixed) {
     const int b = grid_for(n, kBlockC);
     return b < contact_wave(style, mixed) ? b : contact_wave(style, mixed);
 }
-size_t flags_offset(int n, int style, bool mixed) {
-    return ((size_t)(screen_blocks(n, mixed) + contact_blocks(n, style, mixed)) * 6 * sizeof(double) + 255) &
-           ~size_t(255);
-}
+// Scratch layout: [flag words, one per 32-atom group + 1][per-group gaps]
+// [virial partials, 6 per block of the two passes of C], each region on a
+// 256-byte boundary.  The first two depend on n alone, so A finds the flag
+// words at the base and S finds the partials through tmps_engine.part_off.
+size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+size_t gap_offset(int n) { return round256((size_t)((n + 31) / 32 + 1) * sizeof(uint32_t)); }
+size_t part_offset(int n) { return gap_offset(n) + round256((size_t)((n + 31) / 32) * sizeof(float)); }
 }  // namespace
 
 extern "C" {
 
 int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed) {
-    return screen_blocks(n, mixed != 0) + contact_blocks(n, style, mixed != 0);
+    return a_blocks(n, mixed != 0) + contact_blocks(n, style, mixed != 0);
 }
 
 int64_t tmps_fused_scratch_bytes(int32_t n, int32_t style, int32_t mixed) {
     if (n < 0) return -1;
-    return (int64_t)(flags_offset(n, style, mixed != 0) + (size_t)((n + 31) / 32 + 1) * sizeof(uint32_t));
+    return (int64_t)(part_offset(n) +
+                     (size_t)(a_blocks(n, mixed != 0) + contact_blocks(n, style, mixed != 0)) * 6 * sizeof(double));
 }
 
 int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* d_eng, const int32_t* cell_of,
@@ -1108,7 +1372,7 @@ int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* 
         k_prepare<<<grid_for(a->n, kBlockA), kBlockA, 0, s>>>(*a, d_box, d_eng, cell_of);
         note_launches(1);
     }
-    k_prepare_engine<<<1, 32, 0, s>>>(d_box, d_eng);
+    k_prepare_engine<<<1, 32, 0, s>>>(d_box, d_eng, (int64_t)part_offset(a->n));
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
@@ -1121,17 +1385,20 @@ int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream) 
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
-int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* stream) {
-    if (!a || !d_box || !d_eng || a->n < 0) return TMPS_ERR_BAD_ARG;
+int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* scratch, void* stream) {
+    if (!a || !d_box || !d_eng || !scratch || a->n < 0) return TMPS_ERR_BAD_ARG;
     if (!a->pos32 && (!a->rinv || !a->x0)) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
-    const int g = grid_for(a->n, kBlockA);
+    const int n = a->n;
+    const bool mixed = a->pos32 != nullptr;
     cudaStream_t s = (cudaStream_t)stream;
-    if (a->pos32) {
+    const uint32_t* flags = (const uint32_t*)scratch;
+    double* part = (double*)((char*)scratch + part_offset(n));  // A's partials come first
+    if (mixed) {
         if (!mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-        k_a32<<<g, kBlockA, 0, s>>>(*a, d_box, d_eng);
+        k_a32<<<a_blocks(n, true), kBlockA, 0, s>>>(*a, d_box, d_eng, flags, part);
     } else {
-        k_a64<<<g, kBlockA, 0, s>>>(*a, d_box, d_eng);
+        k_a64<<<a_blocks(n, false), kBlockA, 0, s>>>(*a, d_box, d_eng, flags, part);
     }
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
@@ -1145,14 +1412,15 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
     const int n = a->n;
     const bool mixed = a->pos32 != nullptr;
     const int g1 = screen_blocks(n, mixed), g2 = contact_blocks(n, p->style, mixed);
-    double* part1 = (double*)scratch;
-    double* part2 = part1 + (size_t)g1 * 6;
-    uint32_t* flags = (uint32_t*)((char*)scratch + flags_offset(n, p->style, mixed));
+    uint32_t* flags = (uint32_t*)scratch;
+    const float* gap = (const float*)((char*)scratch + gap_offset(n));
+    // the contact pass's partials follow A's
+    double* part2 = (double*)((char*)scratch + part_offset(n)) + (size_t)a_blocks(n, mixed) * 6;
     cudaStream_t s = (cudaStream_t)stream;
     if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
     const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
-    if (mixed) k_screen<true><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, part1);
-    else k_screen<false><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, part1);
+    if (mixed) k_screen<true><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, gap);
+    else k_screen<false><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, gap);
 #define TMPS_LAUNCH_C(ST)                                                                          \
     if (mixed) k_c<ST, true><<<g2, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, flags, part2);       \
     else k_c<ST, false><<<g2, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, flags, part2);
@@ -1171,7 +1439,23 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
 int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const void* scratch,
                      int32_t* d_status, void* stream) {
     if (!d_box || !d_servo || !d_eng || !scratch || !d_status) return TMPS_ERR_BAD_ARG;
-    k_s<<<1, kBlockS, 0, (cudaStream_t)stream>>>(d_box, d_servo, d_eng, (const double*)scratch, d_status);
+    k_s<<<1, kBlockS, 0, (cudaStream_t)stream>>>(d_box, d_servo, d_eng, (const char*)scratch, d_status);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
+                      const tmps_pair_params* p, int32_t cull, void* scratch, void* stream) {
+    if (!a || !nl || !d_box || !d_eng || !p || !scratch || a->n < 0 || nl->n != a->n || !a->x0 || !a->xr)
+        return TMPS_ERR_BAD_ARG;
+    if (nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
+    const int n = a->n;
+    const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
+    uint32_t* flags = (uint32_t*)scratch;
+    float* gap = (float*)((char*)scratch + gap_offset(n));
+    const int g = n > 0 ? grid_for(n, kBlockA) : 1;
+    k_bounds<<<g, kBlockA, 0, (cudaStream_t)stream>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, cull ? 1 : 0, flags,
+                                                       gap);
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }

@@ -2,20 +2,22 @@
 The fused step engine behind ``Simulation.run``.
 
 One step of Simulation._sub_step_inner (simulation.py:205-247) with fix
-nve/sphere, optionally damping/cundall and deform/pressure, becomes three
-launches (tmps_fused_a, tmps_fused_c, tmps_fused_servo) that decide on the
-device whether the step needs a neighbor rebuild.  Steps are queued in chunks
-with one host synchronisation per chunk.  When a step finds it needs a
-rebuild, every later launch of the chunk does nothing; the host then rebuilds
-exactly as the reference does at that step (save history, wrap, build,
-restore history), finishes the step, and carries on.
+nve/sphere, optionally damping/cundall and deform/pressure, becomes four
+kernels (tmps_fused_a; tmps_fused_c's screen and contact passes;
+tmps_fused_servo) that decide on the device whether the step needs a neighbor
+rebuild.  Steps are queued in chunks (replayed as CUDA graphs) with one host
+synchronisation per chunk.  When a step finds it needs a rebuild, every later
+launch of the chunk does nothing; the host then rebuilds exactly as the
+reference does at that step (save history, wrap, build, restore history),
+finishes the step, and carries on.
 
 Two precisions:
   "fp64"  every operation FP64 (the plain FP64 form);
-  "mixed" FP32 contact arithmetic and per-atom force accumulation, FP64
-          for the velocity/position updates (split positions: FP64 offsets
-          from each atom's cell origin), the shear history and the virial
-          reduction that drives the servo.
+  "mixed" FP32 contact arithmetic and per-atom force accumulation;
+          positions (offsets from each atom's cell origin), velocities and
+          angular velocities as double-word FP32 (hi + lo, ~48 bits) updated
+          with error-free transforms; FP64 shear history; virial partials as
+          double words, their totals -- what the servo reads -- in FP64.
 """
 
 from __future__ import annotations
@@ -49,7 +51,8 @@ class FusedEngine:
     # kernels per step: A, the two passes of C, S
     LAUNCHES_PER_STEP = 4
 
-    def __init__(self, sim, precision: str = "fp64", chunk: int = 64, graphs: bool = True) -> None:
+    def __init__(self, sim, precision: str = "fp64", chunk: int = 64, graphs: bool = True,
+                 cull: bool = True) -> None:
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.sim = sim
@@ -67,6 +70,9 @@ class FusedEngine:
         # A chunk of `chunk` steps is captured once as a CUDA graph and replayed;
         # a rebuild swaps buffers, so the graph is captured again after one.
         self.graphs = bool(graphs)
+        # C skips 32-atom groups whose gap bound rules out any contact (exact;
+        # off screens every group, with bit-identical results)
+        self.cull = bool(cull)
         self._graph = None
         self._graph_key = None
         self.graph_replays = 0
@@ -151,15 +157,22 @@ class FusedEngine:
         self.status.zero_()
 
     def _prepare(self) -> None:
-        nl = self.sim.neighbor
-        rc = _device.lib().tmps_fused_prepare(self.atoms(), self.sim.domain.dbox, self._eng.data_ptr(),
-                                              nl.cell_of.data_ptr(), _device.stream())
+        """Split state and per-step constants for the current list, then the per-group
+        contact bounds C uses to skip groups that cannot touch."""
+        sim = self.sim
+        nl = sim.neighbor
+        L, st = _device.lib(), _device.stream()
+        atoms = self.atoms()
+        rc = L.tmps_fused_prepare(atoms, sim.domain.dbox, self._eng.data_ptr(), nl.cell_of.data_ptr(), st)
         _lib.check(rc, "tmps_fused_prepare")
+        rc = L.tmps_fused_bounds(atoms, sim.history.cstruct(nl), sim.domain.dbox, self._eng.data_ptr(),
+                                 sim.pair_style.params, 1 if self.cull else 0, self.part.data_ptr(), st)
+        _lib.check(rc, "tmps_fused_bounds")
 
     def _launch_step(self, L, st, atoms, nl_struct, params) -> None:
         dbox, eng = self.sim.domain.dbox, self._eng.data_ptr()
         with _device.timed("fused_a"):
-            rc = L.tmps_fused_a(atoms, dbox, eng, st)
+            rc = L.tmps_fused_a(atoms, dbox, eng, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_a")
         with _device.timed("fused_c"):
             rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.part.data_ptr(), st)
@@ -218,6 +231,22 @@ class FusedEngine:
         self._graph.replay()
         self.graph_replays += 1
         self.graph_kernel_launches += self.chunk * self.LAUNCHES_PER_STEP
+
+    def cull_stats(self) -> tuple[int, int]:
+        """(32-atom groups, groups the contact bound rules out right now), from the
+        device state.  No reference counterpart; for reports and tests."""
+        n = self._n
+        ng = (n + 31) // 32
+        e = self._engine_state()
+        if not e.cull or ng == 0:
+            return ng, 0
+        # scratch layout: flag words (ng + 1, 256-byte aligned), then the gaps
+        off = ((ng + 1) * 4 + 255) // 256 * 256
+        gap = self.part[off:off + 4 * ng].view(torch.float32).cpu().numpy()
+        f32 = np.float32
+        md = np.sqrt(np.array([e.maxd2_bits], dtype=np.uint32).view(np.float32)[0])
+        thr = (f32(2.0) * md) * f32(1.0001) + f32(e.shift_bound) + f32(e.cull_tol)
+        return ng, int(np.count_nonzero(gap > thr))
 
     def _check_status(self) -> None:
         st = int(self.status.item())

@@ -137,3 +137,48 @@ def test_graph_replay_matches_eager_launches(gpu, oracle, precision):
         states.append(gpu_state(sim))
     for k in ("x", "v", "omega", "f", "torque"):
         np.testing.assert_array_equal(states[0][k], states[1][k])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_contact_bound_culling_is_exact(gpu, oracle, precision):
+    """Skipping 32-atom groups that the gap bound rules out changes no bit of the
+    result, and the culled run still matches the oracle.  A loose packing with
+    moving spheres and a compressing servo (remap x): groups are culled early,
+    contacts form later."""
+    from taichimps_gb300.engine import FusedEngine
+    from taichimps_gb300.packing import make_packing
+    p = make_packing(2000, 0.9, 1.1, 0.40, seed=3, jitter=0.05, vel_sigma=0.1)
+    L = p["L"]
+    deform = dict(axes={d: {"style": "pressure", "ptarget": 1.0, "pgain": 1e-3} for d in "xyz"}, couple="xyz",
+                  max_rate=1e-1, remap="x")
+    steps = 300
+    states, culled = [], []
+    for cull in (True, False):
+        sim, osim = make_twin(oracle, p["x"], p["radius"], 2.5, [0.0] * 3, [L] * 3, v=p["v"], pair="hertz/history",
+                              dt=5e-5, cundall=(0.7, 0.7), deform=deform)
+        sim.setup_run(steps)
+        sim.init_simulation()
+        eng = FusedEngine(sim, precision, chunk=32, cull=cull)
+        eng.begin()
+        eng.run(steps // 2)
+        culled.append(eng.cull_stats())
+        eng.run(steps - steps // 2)
+        eng.finish()
+        sim.domain.pull()
+        states.append(gpu_state(sim))
+        if cull:
+            osim.run(steps)
+            o = oracle_state(osim)
+            assert np.abs(o["f"]).max() > 0
+            g = states[0]
+            if precision == "fp64":
+                for k in ("x", "v", "f", "torque"):
+                    assert rel_err(g[k], o[k]) < 1e-10, (k, rel_err(g[k], o[k]))
+            else:
+                assert np.abs(g["x"] - o["x"]).max() / L < MIXED_X
+                assert rel_err(g["v"], o["v"]) < MIXED_V
+                assert rel_err(g["f"], o["f"]) < MIXED_F
+    assert culled[0][1] > 0, culled       # the bound did rule groups out
+    assert culled[1][1] == 0
+    for k in ("x", "v", "omega", "f", "torque"):
+        np.testing.assert_array_equal(states[0][k], states[1][k])
