@@ -105,6 +105,17 @@ __device__ __forceinline__ void block_sum_dw(float (&h)[NV], float (&l)[NV], flo
     }
 }
 
+// Programmatic dependent launch.  The four kernels of a step are launched
+// with programmatic stream serialization, so each may be scheduled while its
+// predecessor drains.  Each one first waits for its predecessor grid to
+// complete and its writes to be visible (griddepcontrol.wait: a hardware
+// wait, no spin), and only then touches memory and lets its own successor be
+// scheduled.  Waits chain, so every earlier kernel has completed too.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ bool rebuild_due(const tmps_engine* __restrict__ e, int64_t s) {
     const int64_t since = s - e->last_build_step;
     if (since <= 0) return false;  // built in this very step already
@@ -138,6 +149,7 @@ __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* _
                                                   tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
                                                   double* __restrict__ part) {
     __shared__ double smem[6 * (kBlockA / 32)];
+    pdl_enter();
     if (e->aborted) return;
     const int n = a.n;
     const int lane = threadIdx.x & 31;
@@ -206,6 +218,7 @@ __global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box
     // a double<->float conversion costs as much as a DFMA, so this kernel
     // issues no FP64 instruction at all.
     __shared__ float2 smem[6 * (kBlockA / 32)];
+    pdl_enter();
     if (e->aborted) return;
     const int n = a.n;
     const int lane = threadIdx.x & 31;
@@ -309,11 +322,14 @@ __device__ __forceinline__ void zero_force(const tmps_atoms& A, int i) {
 //    to skip loading them.
 // This pass writes no sums, so which warp handles which group is free: a
 // warp takes 32 groups strided over the system (one per lane) and checks
-// their bounds at once, then screens the live ones.
+// their bounds at once, then screens the live ones; inside a live group an
+// atom whose own gap bound rules contact out reads no row, and the rest read
+// their rows four entries (and partners) at a time.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlockScreen)
     k_screen(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B, tmps_engine* __restrict__ E, int hist,
-             uint32_t* __restrict__ flags, const float* __restrict__ gap) {
+             uint32_t* __restrict__ flags, const float* __restrict__ gap, const float* __restrict__ agap) {
+    pdl_enter();
     if (E->aborted) return;
     const int64_t s = E->step + 1;
     if (rebuild_due(E, s)) return;
@@ -343,8 +359,34 @@ __global__ void __launch_bounds__(kBlockScreen)
             iprd64[c] = B->inv_prd[c];
         }
     }
-    const bool two = L.slots > 1;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // one neighbor entry within reach of contact?
+    auto reach32 = [&](const float4& pi, const float4& pj, int e) {
+        const int code = (unsigned)e >> kNbrIndexBits;
+        const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1), (float)(code / 9 - 1)};
+        const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj.x, pj.y, pj.z};
+        float d[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
+            if (single[c]) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
+        }
+        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+        const float rs = (pi.w + pj.w) * 1.00001f;
+        return rq < rs * rs;
+    };
+    auto reach64 = [&](const double4& pi, const double4& pj) {
+        double d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if (per[c] == 1) d[c] -= rint(d[c] * iprd64[c]) * prd64[c];
+        const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+        const double radsum = pi.w + pj.w;
+        return rsq < radsum * radsum && rsq > 1e-28;
+    };
+    constexpr int kChunk = 4;  // row entries (and their partners) loaded at once
+    const int kfirst = L.slots < kChunk ? L.slots : kChunk;
+    // consecutive groups (neighbours in space) go to consecutive blocks
+    const int gw = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
     for (int base = gw; base < ngroups; base += 32 * nwarps) {
         const int mygrp = base + lane * nwarps;
         uint32_t myold = 0u;
@@ -368,49 +410,47 @@ __global__ void __launch_bounds__(kBlockScreen)
             const bool valid = i < n;
             bool cand = false;
             if (valid) {
-                // every load that does not depend on another is issued at once:
-                // row length, own position, the first two neighbor entries (read
-                // whatever the row length; used only below it)
+                // issued together: the atom's own bound, row length, position
+                // and first row entries (read whatever the row length)
+                const float ag = agap[i];
                 const int nn = L.nnb[i];
-                const int e0 = L.nbr[i];
-                const int e1 = two ? L.nbr[(size_t)n + i] : 0;
-                if constexpr (MIXED) {
-                    const float4 pi = ld4f(A.pos32, i);
-                    auto reach = [&](int e) {
-                        const float4 pj = ld4f(A.pos32, e & kNbrIndexMask);
-                        const int code = (unsigned)e >> kNbrIndexBits;
-                        const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1), (float)(code / 9 - 1)};
-                        const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj.x, pj.y, pj.z};
-                        float d[3];
+                int e[kChunk];
 #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
-                            if (single[c]) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
+                for (int u = 0; u < kChunk; ++u) e[u] = u < kfirst ? L.nbr[(size_t)u * n + i] : 0;
+                if (!(cull && ag > thr)) {
+                    if constexpr (MIXED) {
+                        const float4 pi = ld4f(A.pos32, i);
+                        for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
+                            if (k0 > 0) {
+#pragma unroll
+                                for (int u = 0; u < kChunk; ++u)
+                                    if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
+                            }
+                            float4 pj[kChunk];
+#pragma unroll
+                            for (int u = 0; u < kChunk; ++u)
+                                if (k0 + u < nn) pj[u] = ld4f(A.pos32, e[u] & kNbrIndexMask);
+#pragma unroll
+                            for (int u = 0; u < kChunk; ++u)
+                                if (k0 + u < nn) cand = reach32(pi, pj[u], e[u]) || cand;
                         }
-                        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-                        const float rs = (pi.w + pj.w) * 1.00001f;
-                        return rq < rs * rs;
-                    };
-                    const bool c0 = nn > 0 && reach(e0);
-                    const bool c1 = nn > 1 && reach(e1);
-                    cand = c0 || c1;
-                    for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
-                } else {
-                    const double4 pi = ld4(A.xr, i);
-                    auto reach = [&](int e) {
-                        const double4 pj = ld4(A.xr, e & kNbrIndexMask);
-                        double d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+                    } else {
+                        const double4 pi = ld4(A.xr, i);
+                        for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
+                            if (k0 > 0) {
 #pragma unroll
-                        for (int c = 0; c < 3; ++c)
-                            if (per[c] == 1) d[c] -= rint(d[c] * iprd64[c]) * prd64[c];
-                        const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-                        const double radsum = pi.w + pj.w;
-                        return rsq < radsum * radsum && rsq > 1e-28;
-                    };
-                    const bool c0 = nn > 0 && reach(e0);
-                    const bool c1 = nn > 1 && reach(e1);
-                    cand = c0 || c1;
-                    for (int k = 2; k < nn && !cand; ++k) cand = reach(L.nbr[(size_t)k * n + i]);
+                                for (int u = 0; u < kChunk; ++u)
+                                    if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
+                            }
+                            double4 pj[kChunk];
+#pragma unroll
+                            for (int u = 0; u < kChunk; ++u)
+                                if (k0 + u < nn) pj[u] = ld4(A.xr, e[u] & kNbrIndexMask);
+#pragma unroll
+                            for (int u = 0; u < kChunk; ++u)
+                                if (k0 + u < nn) cand = reach64(pi, pj[u]) || cand;
+                        }
+                    }
                 }
             }
             const uint32_t word = __ballot_sync(0xffffffffu, cand);
@@ -423,14 +463,15 @@ __global__ void __launch_bounds__(kBlockScreen)
     }
 }
 
-// Per-group contact bounds at the reference positions x0 (the positions of
-// the last build): the smallest gap |d| - (ri + rj) over the group's rows,
-// rounded down to FP32; -inf for a group holding a live contact or when a
-// periodic dimension has a single bin (the image is then not fixed by the
-// stencil).  Every flag word is set: each atom's force may be nonzero.
+// Contact bounds at the reference positions x0 (the positions of the last
+// build): per atom and per 32-atom group, the smallest gap |d| - (ri + rj)
+// over the rows, rounded down to FP32; -inf for an atom holding a live
+// contact (and its group) or when a periodic dimension has a single bin (the
+// image is then not fixed by the stencil).  Every flag word is set: each
+// atom's force may be nonzero.
 __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B,
                                                      tmps_engine* __restrict__ E, int hist, int cull, uint32_t* flags,
-                                                     float* gap) {
+                                                     float* gap, float* agap) {
     const int n = A.n;
     const int lane = threadIdx.x & 31;
     const int ngroups = (n + 31) >> 5;
@@ -463,6 +504,7 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
                 gmin = gp == gp ? fmin(gmin, gp) : -1e300;  // a NaN pair pins the group
             }
             if ((hist && L.touch[i] != 0ull) || single) gmin = -1e300;
+            agap[i] = __double2float_rd(gmin);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gmin = fmin(gmin, __shfl_down_sync(0xffffffffu, gmin, o));
@@ -485,9 +527,9 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
 
 // C, second pass: the atoms the screen flagged (some neighbor within reach
 // of contact), with the full contact law.  A warp owns 32 groups strided
-// over the system (warp w: w, w + nwarps, ...), so flagged atoms -- which
-// cluster in space, and atoms are in Morton order -- spread over many warps
-// and SMs.  The warp takes the flagged atoms of all its groups in rounds of
+// over the system (warp w: w, w + nwarps, ...; warps numbered across blocks
+// first), so flagged atoms -- which cluster in space, and atoms are in
+// Morton order -- spread over many warps and SMs.  The warp takes the flagged atoms of all its groups in rounds of
 // up to 32 (one per lane, in group then atom order) and lays the (atom,
 // neighbor slot) entries of a round across the lanes, 32 entries per pass:
 // the latency of a round is that of one contact, not of its longest row or
@@ -503,6 +545,7 @@ __global__ void __launch_bounds__(kBlockC)
     __shared__ double smem[6 * (kBlockC / 32)];
     __shared__ uint8_t owner[kBlockC / 32][32];
     __shared__ int32_t roster[kBlockC / 32][32];
+    pdl_enter();
     if (E->aborted) return;
     const int64_t s = E->step + 1;
     if (rebuild_due(E, s)) return;  // S marks the step aborted; the host rebuilds
@@ -546,7 +589,8 @@ __global__ void __launch_bounds__(kBlockC)
     const int ngroups = (n + 31) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const size_t ss = (size_t)L.slots * n;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // consecutive groups (neighbours in space) go to consecutive blocks
+    const int gw = blockIdx.x + gridDim.x * wib;
     for (int base = gw; base < ngroups; base += 32 * nwarps) {
     const int mygrp = base + lane * nwarps;
     const uint32_t myword = mygrp < ngroups ? flags[mygrp] : 0u;
@@ -1060,6 +1104,7 @@ __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps
     __shared__ tmps_box sb;
     __shared__ tmps_servo ssv;
     __shared__ tmps_engine se;
+    pdl_enter();
     copy_words(&se, e);
     __syncthreads();
     if (se.aborted) return;
@@ -1284,6 +1329,22 @@ __global__ void k_settle_flags(tmps_box* b, tmps_engine* e) {
 
 bool launch_ok() { return cudaPeekAtLastError() == cudaSuccess; }
 
+// Launch with programmatic stream serialization (see pdl_enter).
+template <typename... P, typename... A>
+void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, A&&... args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
 bool mixed_ok(const tmps_atoms* a) {
     return a->pos32 && a->pos32lo && a->vel32 && a->vel32lo && a->om32 && a->om32lo && a->cell32 && a->f32 &&
            a->torque32 && a->o0_32;
@@ -1344,12 +1405,14 @@ int contact_blocks(int n, int style, bool mixed) {
     return b < contact_wave(style, mixed) ? b : contact_wave(style, mixed);
 }
 // Scratch layout: [flag words, one per 32-atom group + 1][per-group gaps]
-// [virial partials, 6 per block of the two passes of C], each region on a
-// 256-byte boundary.  The first two depend on n alone, so A finds the flag
-// words at the base and S finds the partials through tmps_engine.part_off.
+// [per-atom gaps][virial partials, 6 per block of A and of C's contact
+// pass], each region on a 256-byte boundary.  The first three depend on n
+// alone, so A finds the flag words at the base and S finds the partials
+// through tmps_engine.part_off.
 size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
 size_t gap_offset(int n) { return round256((size_t)((n + 31) / 32 + 1) * sizeof(uint32_t)); }
-size_t part_offset(int n) { return gap_offset(n) + round256((size_t)((n + 31) / 32) * sizeof(float)); }
+size_t atom_gap_offset(int n) { return gap_offset(n) + round256((size_t)((n + 31) / 32) * sizeof(float)); }
+size_t part_offset(int n) { return atom_gap_offset(n) + round256((size_t)n * sizeof(float)); }
 }  // namespace
 
 extern "C" {
@@ -1396,9 +1459,9 @@ int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void*
     double* part = (double*)((char*)scratch + part_offset(n));  // A's partials come first
     if (mixed) {
         if (!mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-        k_a32<<<a_blocks(n, true), kBlockA, 0, s>>>(*a, d_box, d_eng, flags, part);
+        launch_pdl(k_a32, a_blocks(n, true), kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     } else {
-        k_a64<<<a_blocks(n, false), kBlockA, 0, s>>>(*a, d_box, d_eng, flags, part);
+        launch_pdl(k_a64, a_blocks(n, false), kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     }
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
@@ -1414,16 +1477,19 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
     const int g1 = screen_blocks(n, mixed), g2 = contact_blocks(n, p->style, mixed);
     uint32_t* flags = (uint32_t*)scratch;
     const float* gap = (const float*)((char*)scratch + gap_offset(n));
+    const float* agap = (const float*)((char*)scratch + atom_gap_offset(n));
     // the contact pass's partials follow A's
     double* part2 = (double*)((char*)scratch + part_offset(n)) + (size_t)a_blocks(n, mixed) * 6;
     cudaStream_t s = (cudaStream_t)stream;
     if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
     const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
-    if (mixed) k_screen<true><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, gap);
-    else k_screen<false><<<g1, kBlockScreen, 0, s>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, flags, gap);
+    const int hi = has_hist ? 1 : 0;
+    if (mixed) launch_pdl(k_screen<true>, g1, kBlockScreen, s, *a, *nl, d_box, d_eng, hi, flags, gap, agap);
+    else launch_pdl(k_screen<false>, g1, kBlockScreen, s, *a, *nl, d_box, d_eng, hi, flags, gap, agap);
+    const uint32_t* cflags = flags;
 #define TMPS_LAUNCH_C(ST)                                                                          \
-    if (mixed) k_c<ST, true><<<g2, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, flags, part2);       \
-    else k_c<ST, false><<<g2, kBlockC, 0, s>>>(*a, *nl, *p, d_box, d_eng, flags, part2);
+    if (mixed) launch_pdl(k_c<ST, true>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, cflags, part2); \
+    else launch_pdl(k_c<ST, false>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, cflags, part2);
     switch (p->style) {
         case 0: TMPS_LAUNCH_C(0) break;
         case 1: TMPS_LAUNCH_C(1) break;
@@ -1439,7 +1505,7 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
 int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const void* scratch,
                      int32_t* d_status, void* stream) {
     if (!d_box || !d_servo || !d_eng || !scratch || !d_status) return TMPS_ERR_BAD_ARG;
-    k_s<<<1, kBlockS, 0, (cudaStream_t)stream>>>(d_box, d_servo, d_eng, (const char*)scratch, d_status);
+    launch_pdl(k_s, 1, kBlockS, (cudaStream_t)stream, d_box, d_servo, d_eng, (const char*)scratch, d_status);
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
@@ -1453,9 +1519,10 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
     const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
     uint32_t* flags = (uint32_t*)scratch;
     float* gap = (float*)((char*)scratch + gap_offset(n));
+    float* agap = (float*)((char*)scratch + atom_gap_offset(n));
     const int g = n > 0 ? grid_for(n, kBlockA) : 1;
     k_bounds<<<g, kBlockA, 0, (cudaStream_t)stream>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, cull ? 1 : 0, flags,
-                                                       gap);
+                                                       gap, agap);
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
