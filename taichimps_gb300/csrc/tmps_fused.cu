@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* _
     pdl_enter();
     if (e->aborted) return;
     const int n = a.n;
+    const int nb = e->nblocks;  // partials are component-major, [6][nb]
     const int lane = threadIdx.x & 31;
     const int32_t s = (int32_t)(e->step + 1);
     const double dt = e->dt, dtf = 0.5 * dt;
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* _
     block_sum<6, kBlockA>(K, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = K[c];
+        for (int c = 0; c < 6; ++c) part[(size_t)c * nb + blockIdx.x] = K[c];
     }
 }
 
@@ -221,6 +222,7 @@ __global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box
     pdl_enter();
     if (e->aborted) return;
     const int n = a.n;
+    const int nb = e->nblocks;  // partials are component-major, [6][nb]
     const int lane = threadIdx.x & 31;
     const int32_t s = (int32_t)(e->step + 1);
     const float dth = e->dt_hi, dtl = e->dt_lo;
@@ -281,7 +283,7 @@ __global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box
     block_sum_dw<6, kBlockA>(Kh, Kl, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < 6; ++k) reinterpret_cast<float2*>(part)[(size_t)blockIdx.x * 6 + k] = make_float2(Kh[k], Kl[k]);
+        for (int k = 0; k < 6; ++k) reinterpret_cast<float2*>(part)[(size_t)k * nb + blockIdx.x] = make_float2(Kh[k], Kl[k]);
     }
 }
 
@@ -549,6 +551,7 @@ __global__ void __launch_bounds__(kBlockC)
     if (E->aborted) return;
     const int64_t s = E->step + 1;
     if (rebuild_due(E, s)) return;  // S marks the step aborted; the host rebuilds
+    const int nb = E->nblocks;      // partials are component-major, [6][nb]
     constexpr bool kHist = STYLE == STYLE_HOOKE_HISTORY || STYLE == STYLE_HERTZ_HISTORY || STYLE == STYLE_GRANULAR;
     const bool hist = kHist && (STYLE != STYLE_GRANULAR || P.tangential_id >= 2);
     const int n = A.n;
@@ -942,13 +945,13 @@ __global__ void __launch_bounds__(kBlockC)
         block_sum_dw<6, kBlockC>(Vh, Vl, reinterpret_cast<float2*>(smem));
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) reinterpret_cast<float2*>(part)[(size_t)blockIdx.x * 6 + c] = make_float2(Vh[c], Vl[c]);
+            for (int c = 0; c < 6; ++c) reinterpret_cast<float2*>(part)[(size_t)c * nb + blockIdx.x] = make_float2(Vh[c], Vl[c]);
         }
     } else {
         block_sum<6, kBlockC>(Vd, smem);
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) part[(size_t)blockIdx.x * 6 + c] = Vd[c];
+            for (int c = 0; c < 6; ++c) part[(size_t)c * nb + blockIdx.x] = Vd[c];
         }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) E->final_pending = 1;
@@ -969,13 +972,23 @@ __device__ double limit_rate_f(double rate, double ptarget, int normalize, doubl
     return out;
 }
 
-constexpr int kBlockS = 192;  // a multiple of 6 and of 32
+constexpr int kBlockS = 768;  // four warps per virial component
 
-// The servo's arithmetic on staged copies of the three structs, run by one
-// warp: lane k < 6 forms pressure component k, lane d < 3 updates dimension
-// d.  Each value is the same FP64 expression as in the one-thread form; the
-// lanes only put the independent divisions into one warp instruction each.
-__device__ void servo_update_warp(tmps_box& b, tmps_servo& sv, tmps_engine& e, const double* acc, int32_t* status) {
+// The servo's arithmetic on staged copies of the three structs.  On this
+// part an FP64 instruction costs ~64 cycles of latency and a division ~670,
+// however few lanes are active, so the work is laid out for the SM's four
+// FP64 units: warp 0 runs the serial chain (pressure -> rate -> new box,
+// lane k < 6 one pressure component, lane d < 3 one dimension), then the
+// independent derived quantities are spread over the block's warps.  Each
+// value is the same FP64 expression as a one-thread form would compute.
+struct ServoNew {
+    double lo[3], hi[3], prd[3];   // new box
+    double olo[3], oprd[3];        // old box
+    int bad;
+};
+
+__device__ void servo_chain_warp(const tmps_box& b, tmps_servo& sv, const tmps_engine& e, const double* acc,
+                                 ServoNew& o) {
     const int lane = threadIdx.x & 31;
     const double dt = e.dt;
     const double vol = b.prd[0] * b.prd[1] * b.prd[2];
@@ -987,12 +1000,10 @@ __device__ void servo_update_warp(tmps_box& b, tmps_servo& sv, tmps_engine& e, c
     const double t0 = __shfl_sync(0xffffffffu, t, 0), t1 = __shfl_sync(0xffffffffu, t, 1),
                  t2 = __shfl_sync(0xffffffffu, t, 2);
     const int d = lane;
-    double lo = 0.0, prd = 0.0, nlo = 0.0, nhi = 0.0, nprd = 1.0;
+    double nprd = 1.0;
     if (lane < 3) {
-        lo = b.lo[d];
-        prd = b.prd[d];
-        nlo = lo;
-        nhi = b.hi[d];
+        const double lo = b.lo[d], prd = b.prd[d];
+        double nlo = lo, nhi = b.hi[d];
         const int st = sv.style[d];
         const double ls = sv.lo_start[d], hs = sv.hi_start[d];
         if (st >= 1 && st <= 4) {
@@ -1043,42 +1054,71 @@ __device__ void servo_update_warp(tmps_box& b, tmps_servo& sv, tmps_engine& e, c
             nhi = hs + 0.5 * sv.cum[d];
         }
         nprd = nhi - nlo;
+        o.lo[d] = nlo;
+        o.hi[d] = nhi;
+        o.prd[d] = nprd;
+        o.olo[d] = lo;
+        o.oprd[d] = prd;
     }
-    if (__any_sync(0xffffffffu, !(nprd > 0.0))) {
-        if (lane == 0) atomicOr(status, TMPS_STATUS_BOX_NONPOSITIVE);
-        return;
-    }
-    if (lane < 3) {
-        b.old_lo[d] = lo;
-        b.old_prd[d] = prd;
-        b.lo[d] = nlo;
-        b.hi[d] = nhi;
-        b.prd[d] = nprd;
-        b.inv_prd[d] = 1.0 / nprd;
-        const double hc = nprd / (double)b.g[d];
-        b.hcell[d] = hc;
-        b.h_rate[d] = (nprd - prd) / dt;
-        b.h_rate[3 + d] = 0.0;
-        if (e.mixed) {
-            split((nprd - prd) / prd, e.eps_hi[d], e.eps_lo[d]);
-            split(hc, e.h32[d], e.hlo32[d]);
-            split(nprd, e.prd32[d], e.prdlo32[d]);
-            e.iprd32[d] = (float)b.inv_prd[d];
-            e.dlo32[d] = (float)(nlo - e.lo0[d]);
-            e.dh32[d] = (float)(hc - e.h0[d]);
-        } else {
-            e.remap_scale[d] = nprd / prd;
+    const bool bad = __any_sync(0xffffffffu, !(nprd > 0.0));
+    if (lane == 0) o.bad = bad ? 1 : 0;
+}
+
+// The quantities derived from the new box, one kind per warp (lanes 0..2 =
+// dimensions); nothing is written when the new box is not positive.
+__device__ void servo_derive(tmps_box& b, const tmps_servo& sv, tmps_engine& e, const ServoNew& o) {
+    if (o.bad) return;
+    const int warp = threadIdx.x >> 5, d = threadIdx.x & 31;
+    if (d >= 3) return;
+    const double nprd = o.prd[d], prd = o.oprd[d];
+    switch (warp) {
+        case 0:
+            b.inv_prd[d] = 1.0 / nprd;
+            if (e.mixed) e.iprd32[d] = (float)b.inv_prd[d];
+            break;
+        case 1: {
+            const double hc = nprd / (double)b.g[d];
+            b.hcell[d] = hc;
+            if (e.mixed) {
+                split(hc, e.h32[d], e.hlo32[d]);
+                e.dh32[d] = (float)(hc - e.h0[d]);
+            }
+            break;
         }
-    }
-    if (e.cull) {
-        // change of the periodic image shifts since the contact bounds' reference
-        const double dd = lane < 3 ? fabs(nprd - e.prd_ref[d]) : 0.0;
-        const double d1 = __shfl_sync(0xffffffffu, dd, 1), d2 = __shfl_sync(0xffffffffu, dd, 2);
-        if (lane == 0) e.shift_bound = fmaxf(e.shift_bound, __double2float_ru((dd + d1) + d2));
-    }
-    if (lane == 0) {
-        b.vremap = sv.remap == 2 ? 1 : 0;
-        b.remap_pending = sv.remap == 1 ? 1 : 0;
+        case 2:
+            b.h_rate[d] = (nprd - prd) / e.dt;
+            b.h_rate[3 + d] = 0.0;
+            break;
+        case 3:
+            if (e.mixed) split((nprd - prd) / prd, e.eps_hi[d], e.eps_lo[d]);
+            else e.remap_scale[d] = nprd / prd;
+            break;
+        case 4:
+            if (e.mixed) {
+                split(nprd, e.prd32[d], e.prdlo32[d]);
+                e.dlo32[d] = (float)(o.lo[d] - e.lo0[d]);
+            }
+            break;
+        case 5: {
+            b.old_lo[d] = o.olo[d];
+            b.old_prd[d] = prd;
+            b.lo[d] = o.lo[d];
+            b.hi[d] = o.hi[d];
+            b.prd[d] = nprd;
+            if (e.cull) {
+                // change of the periodic image shifts since the contact bounds' reference
+                const double dd = fabs(nprd - e.prd_ref[d]);
+                const double d1 = __shfl_sync(0x7u, dd, 1), d2 = __shfl_sync(0x7u, dd, 2);
+                if (d == 0) e.shift_bound = fmaxf(e.shift_bound, __double2float_ru((dd + d1) + d2));
+            }
+            if (d == 0) {
+                b.vremap = sv.remap == 2 ? 1 : 0;
+                b.remap_pending = sv.remap == 1 ? 1 : 0;
+            }
+            break;
+        }
+        default:
+            break;
     }
 }
 
@@ -1090,20 +1130,46 @@ __device__ __forceinline__ void copy_words(S* dst, const S* src) {
     for (int k = threadIdx.x; k < (int)(sizeof(S) / 4); k += blockDim.x) o[k] = a[k];
 }
 
-// S: finish the step.  Decide the rebuild, sum the virial partials of C in a
-// fixed order, run the servo.  The three structs are staged through shared
-// memory; the partial sums are read component-major by 192 threads (thread t
-// always adds component t % 6), so every load is coalesced and independent.
-// The mixed form's partials are double words and are summed as such; only
-// the six totals become FP64.
+// S: finish the step.  Decide the rebuild, sum the virial partials of A and
+// C in a fixed order, run the servo.  The box and servo structs are written
+// by S alone, and the previous step's S has completed before this one can
+// start, so they are staged before the dependency wait; the engine struct
+// (A and C write parts of it) after.  The partials are component-major,
+// [6][nblocks]: four warps per component each take every fourth run of 32
+// blocks (coalesced, all loads of a lane in flight at once), then a shuffle
+// tree and the four warp sums in order.  The mixed form's partials are
+// double words and are summed as such; only the six totals become FP64.
+constexpr int kWarpsS = kBlockS / 32;
+static_assert(kWarpsS == 24, "four warps per virial component");
+constexpr int kPartLoads = 10;  // per lane: up to 32 * 4 * 10 = 1280 partial blocks in one round
+
+template <typename V, typename Add>
+__device__ __forceinline__ V sum_component(const V* row, int nb, int q, int lane, V zero, Add add) {
+    V acc = zero;
+    for (int k0 = q * 32 + lane; k0 < nb; k0 += 128 * kPartLoads) {
+        V v[kPartLoads];
+#pragma unroll
+        for (int u = 0; u < kPartLoads; ++u) {
+            const int k = k0 + 128 * u;
+            v[u] = k < nb ? row[k] : zero;
+        }
+#pragma unroll
+        for (int u = 0; u < kPartLoads; ++u) acc = add(acc, v[u]);
+    }
+    return acc;
+}
+
 __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps_engine* e, const char* scratch,
                                                int32_t* status) {
-    __shared__ double red[kBlockS];
-    __shared__ float2 redf[kBlockS];
     __shared__ double tot[6];
+    __shared__ double wsum[kWarpsS];
+    __shared__ float2 wsumf[kWarpsS];
     __shared__ tmps_box sb;
     __shared__ tmps_servo ssv;
     __shared__ tmps_engine se;
+    __shared__ ServoNew snew;
+    copy_words(&sb, b);
+    copy_words(&ssv, sv);
     pdl_enter();
     copy_words(&se, e);
     __syncthreads();
@@ -1113,56 +1179,45 @@ __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps
         if (threadIdx.x == 0) e->aborted = 1;
         return;
     }
-    copy_words(&sb, b);
-    copy_words(&ssv, sv);
-    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool servo_now = se.servo && ((ssv.step_count + 1) % ssv.nevery == 0);
     if (servo_now) {
         const double* part = reinterpret_cast<const double*>(scratch + se.part_off);
-        const int total = se.nblocks * 6;
-        int k = threadIdx.x;
+        const int nb = se.nblocks, c = warp >> 2, q = warp & 3;
         if (se.mixed) {
-            // double-word partials, summed in double words (two chains per thread)
-            const float2* pf = reinterpret_cast<const float2*>(part);
-            float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
-            for (; k + kBlockS < total; k += 2 * kBlockS) {
-                const float2 q0 = pf[k], q1 = pf[k + kBlockS];
-                dw_add2(h0, l0, q0.x, q0.y);
-                dw_add2(h1, l1, q1.x, q1.y);
+            const float2* row = reinterpret_cast<const float2*>(part) + (size_t)c * nb;
+            float2 acc = sum_component(row, nb, q, lane, make_float2(0.0f, 0.0f), [](float2 x, float2 y) {
+                dw_add2(x.x, x.y, y.x, y.y);
+                return x;
+            });
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float bh = __shfl_down_sync(0xffffffffu, acc.x, o), bl = __shfl_down_sync(0xffffffffu, acc.y, o);
+                dw_add2(acc.x, acc.y, bh, bl);
             }
-            if (k < total) {
-                const float2 q0 = pf[k];
-                dw_add2(h0, l0, q0.x, q0.y);
-            }
-            dw_add2(h0, l0, h1, l1);
-            redf[threadIdx.x] = make_float2(h0, l0);
+            if (lane == 0) wsumf[warp] = acc;
             __syncthreads();
             if (threadIdx.x < 6) {
                 float h = 0.0f, l = 0.0f;
-                for (int q = threadIdx.x; q < kBlockS; q += 6) dw_add2(h, l, redf[q].x, redf[q].y);
+#pragma unroll
+                for (int w = 0; w < 4; ++w) dw_add2(h, l, wsumf[4 * threadIdx.x + w].x, wsumf[4 * threadIdx.x + w].y);
                 tot[threadIdx.x] = (double)h + (double)l;
             }
         } else {
-            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-            for (; k + 3 * kBlockS < total; k += 4 * kBlockS) {
-                a0 += part[k];
-                a1 += part[k + kBlockS];
-                a2 += part[k + 2 * kBlockS];
-                a3 += part[k + 3 * kBlockS];
-            }
-            for (; k < total; k += kBlockS) a0 += part[k];
-            red[threadIdx.x] = (a0 + a1) + (a2 + a3);
+            const double* row = part + (size_t)c * nb;
+            double t = sum_component(row, nb, q, lane, 0.0, [](double x, double y) { return x + y; });
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            if (lane == 0) wsum[warp] = t;
             __syncthreads();
-            if (threadIdx.x < 6) {
-                double t = 0.0;
-                for (int q = threadIdx.x; q < kBlockS; q += 6) t += red[q];
-                tot[threadIdx.x] = t;
-            }
+            if (threadIdx.x < 6)
+                tot[threadIdx.x] = ((wsum[4 * threadIdx.x] + wsum[4 * threadIdx.x + 1]) + wsum[4 * threadIdx.x + 2]) +
+                                   wsum[4 * threadIdx.x + 3];
         }
         __syncthreads();
     }
-    if (threadIdx.x < 32) {
-        if (threadIdx.x == 0) {
+    if (warp == 0) {
+        if (lane == 0) {
             se.step = s;
             sb.remap_pending = 0;
             if (se.servo) {
@@ -1171,9 +1226,16 @@ __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps
             }
         }
         __syncwarp();
-        if (servo_now) servo_update_warp(sb, ssv, se, tot, status);
+        if (servo_now) {
+            servo_chain_warp(sb, ssv, se, tot, snew);
+            if (lane == 0 && snew.bad) atomicOr(status, TMPS_STATUS_BOX_NONPOSITIVE);
+        }
     }
     __syncthreads();
+    if (servo_now) {
+        servo_derive(sb, ssv, se, snew);
+        __syncthreads();
+    }
     copy_words(e, &se);
     copy_words(b, &sb);
     copy_words(sv, &ssv);
@@ -1478,8 +1540,8 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
     uint32_t* flags = (uint32_t*)scratch;
     const float* gap = (const float*)((char*)scratch + gap_offset(n));
     const float* agap = (const float*)((char*)scratch + atom_gap_offset(n));
-    // the contact pass's partials follow A's
-    double* part2 = (double*)((char*)scratch + part_offset(n)) + (size_t)a_blocks(n, mixed) * 6;
+    // partials are component-major, [6][nblocks]; the contact pass's blocks follow A's
+    double* part2 = (double*)((char*)scratch + part_offset(n)) + (size_t)a_blocks(n, mixed);
     cudaStream_t s = (cudaStream_t)stream;
     if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
     const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
