@@ -339,10 +339,11 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
  * sum m v v of every atom at mid-step velocity. */
 int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* scratch, void* stream);
 
-/* Launch C, two kernels: a screen over all atoms (finishes contact-free ones,
- * flags the rest) and the contact law over the flagged ones.  `scratch`
- * (tmps_fused_scratch_bytes(n), caller memory: flag words, per-group gaps,
- * then the d_eng->nblocks = tmps_fused_blocks(n) virial partial sums). */
+/* Launch C: per 32-atom group a bound check (tmps_fused_bounds), a screen of
+ * the atoms the bounds leave (finishes contact-free ones, flags the rest) and
+ * the contact law over the flagged ones.  `scratch` (tmps_fused_scratch_bytes(n),
+ * caller memory: flag words, per-group and per-atom gaps, then the
+ * d_eng->nblocks = tmps_fused_blocks(n) virial partial sums). */
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
                  const tmps_pair_params* p, void* scratch, void* stream);
 
@@ -352,7 +353,7 @@ int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, c
 
 /* Number of virial partial sums A and C write for n atoms with this pair
  * style (tmps_pair_params.style) in this form (mixed 0/1): one per block of
- * one resident wave of A and of C's contact pass. */
+ * one resident wave of A and of C. */
 int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed);
 
 /* Scratch bytes tmps_fused_c / tmps_fused_servo need (same arguments). */

@@ -28,7 +28,6 @@ namespace {
 
 constexpr int kBlockA = 256;
 constexpr int kBlockC = 128;
-constexpr int kBlockScreen = 256;
 
 // Error-free transformations in FP32 (Knuth's two-sum; FMA for products):
 // s + e == a + b exactly.  Used to form the separation and the overlap of a
@@ -289,6 +288,23 @@ __global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box
 
 // ---------------------------------------------------------------------- C
 
+constexpr int kLive = 4;  // live groups a warp screens together
+
+// Position of the k-th (from 0) set bit of m (k < popc(m)).
+__device__ __forceinline__ int nth_bit(uint32_t m, int k) {
+    int pos = 0;
+#pragma unroll
+    for (int sh = 16; sh > 0; sh >>= 1) {
+        const int c = __popc(m & ((1u << sh) - 1u));
+        if (k >= c) {
+            k -= c;
+            m >>= sh;
+            pos += sh;
+        }
+    }
+    return pos;
+}
+
 template <bool MIXED>
 __device__ __forceinline__ void zero_force(const tmps_atoms& A, int i) {
     const int n = A.n;
@@ -300,167 +316,6 @@ __device__ __forceinline__ void zero_force(const tmps_atoms& A, int i) {
         } else {
             A.f[c * n + i] = 0.0;
             A.torque[c * n + i] = 0.0;
-        }
-    }
-}
-
-// C, first pass: is any neighbor of an atom within reach of contact?  The
-// test is the contact test itself in the FP64 form and a conservative FP32
-// version of it in the mixed form (the second pass decides exactly).  Atoms
-// with no such neighbor are finished here -- zero force and torque, their
-// contact history cleared; their kinetic virial term is A's -- and the rest
-// are flagged, one ballot word per 32-atom group, for the second pass.
-//
-// Two economies, neither of which changes a result:
-//  * a whole group is finished without reading its rows when its smallest
-//    gap |d| - (ri + rj) at the reference positions (tmps_fused_bounds)
-//    exceeds 2 max|x - x0| + the change of the periodic image shifts + a
-//    rounding slack: by the triangle inequality none of its pairs can touch.
-//    Both running maxima only grow, so such a group has had no contact since
-//    the reference either, and its contact history is already clear.
-//  * the flag words double as "force may be nonzero": an atom's force and
-//    torque are written (as zeros) only when it was flagged the step
-//    before, so every unflagged atom holds an exact zero, which A relies on
-//    to skip loading them.
-// This pass writes no sums, so which warp handles which group is free: a
-// warp takes 32 groups strided over the system (one per lane) and checks
-// their bounds at once, then screens the live ones; inside a live group an
-// atom whose own gap bound rules contact out reads no row, and the rest read
-// their rows four entries (and partners) at a time.
-template <bool MIXED>
-__global__ void __launch_bounds__(kBlockScreen)
-    k_screen(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B, tmps_engine* __restrict__ E, int hist,
-             uint32_t* __restrict__ flags, const float* __restrict__ gap, const float* __restrict__ agap) {
-    pdl_enter();
-    if (E->aborted) return;
-    const int64_t s = E->step + 1;
-    if (rebuild_due(E, s)) return;
-    const int n = A.n;
-    const int lane = threadIdx.x & 31;
-    const int ngroups = (n + 31) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const bool cull = E->cull != 0;
-    float thr = 0.0f;
-    if (cull) {
-        const float md = sqrtf(__uint_as_float(E->maxd2_bits));
-        thr = ((2.0f * md) * 1.0001f + E->shift_bound) + E->cull_tol;
-    }
-    float hh[3], prd32[3], iprd32[3];
-    double prd64[3], iprd64[3];
-    int per[3], single[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        per[c] = B->per[c];
-        if constexpr (MIXED) {
-            hh[c] = E->h32[c];
-            prd32[c] = E->prd32[c];
-            iprd32[c] = E->iprd32[c];
-            single[c] = E->single_bin[c];
-        } else {
-            prd64[c] = B->prd[c];
-            iprd64[c] = B->inv_prd[c];
-        }
-    }
-    // one neighbor entry within reach of contact?
-    auto reach32 = [&](const float4& pi, const float4& pj, int e) {
-        const int code = (unsigned)e >> kNbrIndexBits;
-        const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1), (float)(code / 9 - 1)};
-        const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj.x, pj.y, pj.z};
-        float d[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
-            if (single[c]) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
-        }
-        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-        const float rs = (pi.w + pj.w) * 1.00001f;
-        return rq < rs * rs;
-    };
-    auto reach64 = [&](const double4& pi, const double4& pj) {
-        double d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-            if (per[c] == 1) d[c] -= rint(d[c] * iprd64[c]) * prd64[c];
-        const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-        const double radsum = pi.w + pj.w;
-        return rsq < radsum * radsum && rsq > 1e-28;
-    };
-    constexpr int kChunk = 4;  // row entries (and their partners) loaded at once
-    const int kfirst = L.slots < kChunk ? L.slots : kChunk;
-    // consecutive groups (neighbours in space) go to consecutive blocks
-    const int gw = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
-    for (int base = gw; base < ngroups; base += 32 * nwarps) {
-        const int mygrp = base + lane * nwarps;
-        uint32_t myold = 0u;
-        bool live = false;
-        if (mygrp < ngroups) {
-            myold = flags[mygrp];
-            live = !(cull && gap[mygrp] > thr);
-            if (!live && myold != 0u) {
-                // culled now, flagged last step: clear the stale forces
-                for (uint32_t w = myold; w; w &= w - 1) zero_force<MIXED>(A, (mygrp << 5) + __ffs(w) - 1);
-                flags[mygrp] = 0u;
-            }
-        }
-        uint32_t pending = __ballot_sync(0xffffffffu, live);
-        while (pending) {
-            const int src = __ffs(pending) - 1;
-            pending &= pending - 1;
-            const int g = base + src * nwarps;
-            const uint32_t old = __shfl_sync(0xffffffffu, myold, src);
-            const int i = (g << 5) + lane;
-            const bool valid = i < n;
-            bool cand = false;
-            if (valid) {
-                // issued together: the atom's own bound, row length, position
-                // and first row entries (read whatever the row length)
-                const float ag = agap[i];
-                const int nn = L.nnb[i];
-                int e[kChunk];
-#pragma unroll
-                for (int u = 0; u < kChunk; ++u) e[u] = u < kfirst ? L.nbr[(size_t)u * n + i] : 0;
-                if (!(cull && ag > thr)) {
-                    if constexpr (MIXED) {
-                        const float4 pi = ld4f(A.pos32, i);
-                        for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
-                            if (k0 > 0) {
-#pragma unroll
-                                for (int u = 0; u < kChunk; ++u)
-                                    if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
-                            }
-                            float4 pj[kChunk];
-#pragma unroll
-                            for (int u = 0; u < kChunk; ++u)
-                                if (k0 + u < nn) pj[u] = ld4f(A.pos32, e[u] & kNbrIndexMask);
-#pragma unroll
-                            for (int u = 0; u < kChunk; ++u)
-                                if (k0 + u < nn) cand = reach32(pi, pj[u], e[u]) || cand;
-                        }
-                    } else {
-                        const double4 pi = ld4(A.xr, i);
-                        for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
-                            if (k0 > 0) {
-#pragma unroll
-                                for (int u = 0; u < kChunk; ++u)
-                                    if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
-                            }
-                            double4 pj[kChunk];
-#pragma unroll
-                            for (int u = 0; u < kChunk; ++u)
-                                if (k0 + u < nn) pj[u] = ld4(A.xr, e[u] & kNbrIndexMask);
-#pragma unroll
-                            for (int u = 0; u < kChunk; ++u)
-                                if (k0 + u < nn) cand = reach64(pi, pj[u]) || cand;
-                        }
-                    }
-                }
-            }
-            const uint32_t word = __ballot_sync(0xffffffffu, cand);
-            if (lane == 0 && word != old) flags[g] = word;
-            if (valid && !cand) {
-                if (hist && L.touch[i] != 0ull) L.touch[i] = 0ull;
-                if ((old >> lane) & 1u) zero_force<MIXED>(A, i);
-            }
         }
     }
 }
@@ -527,26 +382,44 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
     }
 }
 
-// C, second pass: the atoms the screen flagged (some neighbor within reach
-// of contact), with the full contact law.  A warp owns 32 groups strided
-// over the system (warp w: w, w + nwarps, ...; warps numbered across blocks
-// first), so flagged atoms -- which cluster in space, and atoms are in
-// Morton order -- spread over many warps and SMs.  The warp takes the flagged atoms of all its groups in rounds of
-// up to 32 (one per lane, in group then atom order) and lays the (atom,
-// neighbor slot) entries of a round across the lanes, 32 entries per pass:
-// the latency of a round is that of one contact, not of its longest row or
-// of the number of groups.  Each atom's force, torque and virial are then
-// summed by the atom's own lane over its entries in slot order -- the order
-// of a one-thread-per-atom loop, so the sums are unchanged.  Per-block virial
-// partials depend only on the flag words, not on scheduling.
+// C: the contact forces of one step.  Per warp, 32 groups strided over the
+// system (warp w owns groups w, w + nwarps, ...; warps numbered across blocks
+// first, so neighbouring groups -- atoms are in Morton order -- go to
+// different SMs):
+//  1. bound check, one group per lane: a group whose smallest gap at the
+//     reference positions (tmps_fused_bounds) exceeds 2 max|x - x0| + the
+//     change of the periodic image shifts + a rounding slack cannot touch
+//     (triangle inequality; both running maxima only grow, so it has had no
+//     contact since the reference and its history is clear): its atoms are
+//     finished with no row read;
+//  2. screen: the atoms of up to kLive live groups whose own gap bound does
+//     not rule contact out are screened together, one per lane -- is any
+//     neighbor within reach of contact? (the contact test itself in FP64; a
+//     conservative FP32 version in the mixed form) -- reading their rows
+//     four entries (and partners) at a time.  Their ballot words are the
+//     group's new flag words; an atom not flagged gets its history cleared;
+//  3. contact: the flagged atoms, in group then atom order, in rounds of up
+//     to 32: the (atom, neighbor slot) entries of a round are laid across the
+//     lanes, 32 per pass, so a round costs the latency of one contact, not of
+//     its longest row.  Each atom's force, torque and virial are summed by the
+//     atom's own lane over its entries in slot order -- the order of a
+//     one-thread-per-atom loop.
+// The flag words double as "force may be nonzero": an atom's force and
+// torque are written as zeros only when it was flagged the step before, so
+// every unflagged atom holds an exact zero, which A relies on to skip
+// loading them.  None of the skipping changes a result.  The per-block
+// virial partials depend only on the flag words and the grid, not on
+// scheduling; the kinetic term of an unflagged atom is A's.
 template <int STYLE, bool MIXED>
 __global__ void __launch_bounds__(kBlockC)
-    k_c(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
-        tmps_engine* __restrict__ E, const uint32_t* __restrict__ flags, double* __restrict__ part) {
+    k_cf(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
+         tmps_engine* __restrict__ E, uint32_t* __restrict__ flags, const float* __restrict__ gap,
+         const float* __restrict__ agap, double* __restrict__ part) {
     using T = typename std::conditional<MIXED, float, double>::type;
     __shared__ double smem[6 * (kBlockC / 32)];
     __shared__ uint8_t owner[kBlockC / 32][32];
-    __shared__ int32_t roster[kBlockC / 32][32];
+    __shared__ int32_t croster[kBlockC / 32][32];
+    __shared__ uint32_t cwords[kBlockC / 32][kLive];
     pdl_enter();
     if (E->aborted) return;
     const int64_t s = E->step + 1;
@@ -594,353 +467,505 @@ __global__ void __launch_bounds__(kBlockC)
     const size_t ss = (size_t)L.slots * n;
     // consecutive groups (neighbours in space) go to consecutive blocks
     const int gw = blockIdx.x + gridDim.x * wib;
-    for (int base = gw; base < ngroups; base += 32 * nwarps) {
-    const int mygrp = base + lane * nwarps;
-    const uint32_t myword = mygrp < ngroups ? flags[mygrp] : 0u;
-    // flagged atoms of the 32 groups, numbered in lane (group) then bit order
-    const int cnt = __popc(myword);
-    int before = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, before, o);
-        if (lane >= o) before += t;
+    const bool cull = E->cull != 0;
+    float thr = 0.0f;
+    if (cull) {
+        // a NaN displacement makes thr NaN and culls nothing
+        const float md = sqrtf(__uint_as_float(E->maxd2_bits));
+        thr = ((2.0f * md) * 1.0001f + E->shift_bound) + E->cull_tol;
     }
-    const int natoms = __shfl_sync(0xffffffffu, before, 31);
-    before -= cnt;
-    for (int r0 = 0; r0 < natoms; r0 += 32) {
-        if (before < r0 + 32 && before + cnt > r0) {
-            int idx = before;
-            for (uint32_t w = myword; w; w &= w - 1, ++idx)
-                if (idx >= r0 && idx < r0 + 32) roster[wib][idx - r0] = (mygrp << 5) + __ffs(w) - 1;
-        }
-        __syncwarp();
-        // this lane's atom and its row: entries [start, start + nn) of the round
-        const bool mine = lane < natoms - r0;
-        const int i = mine ? roster[wib][lane] : 0;
-        __syncwarp();
-        const int nn = mine ? L.nnb[i] : 0;
-        const uint64_t touch = (hist && mine) ? L.touch[i] : 0ull;
-        int incl = nn;
+    constexpr int kChunk = 4;  // row entries (and their partners) loaded at once
+    const int kfirst = L.slots < kChunk ? L.slots : kChunk;
+    // screen one atom: is any neighbor within reach of contact?
+    auto screen_atom = [&](int i) -> bool {
+        const int nn = L.nnb[i];
+        int e[kChunk];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        const int start = incl - nn;
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
-        uint64_t newtouch = 0ull;
-        for (int p0 = 0; p0 < total; p0 += 32) {
-            if (mine) {
-                const int k0 = max(start, p0), k1 = min(start + nn, p0 + 32);
-                for (int k = k0; k < k1; ++k) owner[wib][k - p0] = (uint8_t)lane;
-            }
-            __syncwarp();
-            const bool live = p0 + lane < total;
-            const int ol = live ? owner[wib][lane] : 0;
-            const int ost = __shfl_sync(0xffffffffu, start, ol);
-            const int ia = __shfl_sync(0xffffffffu, i, ol);  // the entry's row atom
-            const uint32_t tlo = __shfl_sync(0xffffffffu, (uint32_t)touch, ol);
-            const uint32_t thi = __shfl_sync(0xffffffffu, (uint32_t)(touch >> 32), ol);
-            bool contact = false;
-            T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
-            if (live) {
-                const int k = p0 + lane - ost;      // the entry's slot in its row
-                const int e = L.nbr[(size_t)k * n + ia];
-                const int j = e & kNbrIndexMask;
-                const bool lo = ia < j;
-                T xi[3], xj[3], ri, rj;
-                int32_t ci = 0;
-                if constexpr (MIXED) {
-                    const float4 pi = ld4f(A.pos32, ia), pj = ld4f(A.pos32, j);
-                    xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
-                    xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
-                    if (vremap) ci = A.cell32[ia];
-                } else {
-                    const double4 pi = ld4(A.xr, ia), pj = ld4(A.xr, j);
-                    xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
-                    xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+        for (int u = 0; u < kChunk; ++u) e[u] = u < kfirst ? L.nbr[(size_t)u * n + i] : 0;
+        bool cand = false;
+        if constexpr (MIXED) {
+            const float4 pi = ld4f(A.pos32, i);
+            for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
+                if (k0 > 0) {
+#pragma unroll
+                    for (int u = 0; u < kChunk; ++u)
+                        if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
                 }
-                // separation x_i - x_j
-                T d[3];
-                T nimg[3] = {0, 0, 0};
-                const int code = (unsigned)e >> kNbrIndexBits;
-                const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
-                if constexpr (MIXED) {
-                    // offsets are relative to each atom's own cell: j's cell is
-                    // the stencil offset (ox, oy, oz) away from i's, so
-                    // x_i - x_j = (o_i - o_j) - offset * h
+                float4 pj[kChunk];
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        d[c] = (xi[c] - xj[c]) - (float)off[c] * hh[c];
-                        if (single[c]) {
-                            nimg[c] = rintf(d[c] * iprd[c]);
-                            d[c] -= nimg[c] * prd[c];
+                for (int u = 0; u < kChunk; ++u)
+                    if (k0 + u < nn) pj[u] = ld4f(A.pos32, e[u] & kNbrIndexMask);
+#pragma unroll
+                for (int u = 0; u < kChunk; ++u) {
+                    if (k0 + u < nn) {
+                        const int code = (unsigned)e[u] >> kNbrIndexBits;
+                        const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1),
+                                              (float)(code / 9 - 1)};
+                        const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj[u].x, pj[u].y, pj[u].z};
+                        float d[3];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
+                            if (single[c]) d[c] -= rintf(d[c] * iprd[c]) * prd[c];
                         }
+                        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                        const float rs = (pi.w + pj[u].w) * 1.00001f;
+                        cand = cand || rq < rs * rs;
                     }
-                    if (vremap) {  // image count for the partner velocity shift
-                        const int32_t cj = A.cell32[j];
-                        const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
-                                           cell_z(ci) + off[2] - cell_z(cj)};
+                }
+            }
+        } else {
+            const double4 pi = ld4(A.xr, i);
+            for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
+                if (k0 > 0) {
+#pragma unroll
+                    for (int u = 0; u < kChunk; ++u)
+                        if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
+                }
+                double4 pj[kChunk];
+#pragma unroll
+                for (int u = 0; u < kChunk; ++u)
+                    if (k0 + u < nn) pj[u] = ld4(A.xr, e[u] & kNbrIndexMask);
+#pragma unroll
+                for (int u = 0; u < kChunk; ++u) {
+                    if (k0 + u < nn) {
+                        double d[3] = {pi.x - pj[u].x, pi.y - pj[u].y, pi.z - pj[u].z};
 #pragma unroll
                         for (int c = 0; c < 3; ++c)
-                            if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / gdim[c]);
+                            if (per[c] == 1) d[c] -= rint(d[c] * iprd[c]) * prd[c];
+                        const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                        const double radsum = pi.w + pj[u].w;
+                        cand = cand || (rsq < radsum * radsum && rsq > 1e-28);
                     }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        d[c] = xi[c] - xj[c];
-                        if (per[c] == 1) {
-                            nimg[c] = rint(d[c] * iprd[c]);
-                            d[c] -= nimg[c] * prd[c];
-                        }
-                    }
-                }
-                PairIn<T> in;
-                const T sg = lo ? T(1) : T(-1);
-                in.ra = lo ? ri : rj;
-                in.rb = lo ? rj : ri;
-                bool near;
-                if constexpr (MIXED) {
-                    // FP32 screen, with room for the FP32 rounding of the words
-                    const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-                    const float rs = (ri + rj) * 1.00001f;
-                    near = rq < rs * rs;
-                    if (near) {
-                        // separation, |d|^2, |d| and the overlap from the high and
-                        // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
-                        // FP32 difference of two unit-size numbers keeps 2^-24)
-                        const float4 il = ld4f(A.pos32lo, ia), jl = ld4f(A.pos32lo, j);
-                        const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
-                        float dh[3], dl[3];
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            float s1, e1, s2, e2;
-                            two_sum(xi[c], -xj[c], s1, e1);
-                            two_sum(s1, -(float)off[c] * hh[c], s2, e2);
-                            const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), (float)off[c] * hlo[c]),
-                                                        __fadd_rn(e1, e2));
-                            two_sum(s2, low, dh[c], dl[c]);
-                            if (single[c]) {
-                                const float ni = rintf(dh[c] * iprd[c]);
-                                float s3, e3;
-                                two_sum(dh[c], -ni * prd[c], s3, e3);
-                                two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * prdlo[c]), e3), dh[c], dl[c]);
-                            }
-                            dh[c] = sg * dh[c];
-                            dl[c] = sg * dl[c];
-                        }
-                        // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
-                        float pp[3], pe[3];
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            pp[c] = __fmul_rn(dh[c], dh[c]);
-                            pe[c] = __fmaf_rn(dh[c], dh[c], -pp[c]);
-                        }
-                        float t1, te1, rh, re;
-                        two_sum(pp[0], pp[1], t1, te1);
-                        two_sum(t1, pp[2], rh, re);
-                        const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]),
-                                                                                __fmul_rn(dh[1], dl[1])),
-                                                                     __fmul_rn(dh[2], dl[2])));
-                        const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])),
-                                                    cross);
-                        float rsh, rsl;
-                        two_sum(rh, rl0, rsh, rsl);
-                        const float r_hi = __fsqrt_rn(rsh);
-                        const float res = __fmaf_rn(-r_hi, r_hi, rsh);  // exact
-                        const float r_lo = __fdiv_rn(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
-                        // ra + rb, both words
-                        const float4 al = lo ? il : jl, bl = lo ? jl : il;
-                        float sh_, se_;
-                        two_sum(in.ra, in.rb, sh_, se_);
-                        const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
-                        const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
-                        near = delta > 0.0f && rsh > 1e-28f;
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
-                        in.rsq = rsh;
-                        in.r = r_hi;
-                        in.delta = delta;
-                    }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
-                    in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
-                    const T radsum = in.ra + in.rb;
-                    near = in.rsq < radsum * radsum && in.rsq > T(1e-28);
-                    if (near) {
-                        in.r = sqrt(in.rsq);
-                        in.delta = radsum - in.r;
-                    }
-                }
-                if (near) {
-                    contact = true;
-                    T vi[3], wi[3], mi, vj[3], wj[3], mj;
-                    if constexpr (MIXED) {
-                        const float4 v = ld4f(A.vel32, ia), w = ld4f(A.om32, ia);
-                        const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
-                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-                    } else {
-                        const double4 v = ld4(A.vm, ia), w = ld4(A.om, ia);
-                        const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
-                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-                    }
-                    T dv[3] = {0, 0, 0};
-                    if (vremap) {
-                        // image count of x_a - x_b, then n . h_rate for partner b
-                        T na[3];
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
-                        dv[0] = (na[0] * hrate[0] + na[1] * hshear[2]) + na[2] * hshear[1];
-                        dv[1] = na[1] * hrate[1] + na[2] * hshear[0];
-                        dv[2] = na[2] * hrate[2];
-                    }
-                    in.ma = lo ? mi : mj;
-                    in.mb = lo ? mj : mi;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        in.va[c] = lo ? vi[c] : vj[c];
-                        in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
-                        in.wa[c] = lo ? wi[c] : wj[c];
-                        in.wb[c] = lo ? wj[c] : wi[c];
-                    }
-                    double sh[3] = {0, 0, 0};
-                    const size_t so = (size_t)k * n + ia;
-                    const bool was = k < 32 ? ((tlo >> k) & 1u) : ((thi >> (k - 32)) & 1u);
-                    if (hist && was) {
-                        const double sgd = lo ? 1.0 : -1.0;
-                        sh[0] = sgd * L.shear[so];
-                        sh[1] = sgd * L.shear[ss + so];
-                        sh[2] = sgd * L.shear[2 * ss + so];
-                    }
-                    PairOut<T> out;
-                    contact_law<T, STYLE>(P, dt, 1, in, sh, out);
-                    if (hist) {
-                        const double sgd = lo ? 1.0 : -1.0;
-                        L.shear[so] = sgd * sh[0];
-                        L.shear[ss + so] = sgd * sh[1];
-                        L.shear[2 * ss + so] = sgd * sh[2];
-                    }
-                    const T arm = lo ? out.arm_a : out.arm_b;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        fc[c] = sg * out.f[c];
-                        tc[c] = arm * out.tor[c];
-                    }
-                    vc[0] = T(0.5) * (in.d[0] * out.f[0]);
-                    vc[1] = T(0.5) * (in.d[1] * out.f[1]);
-                    vc[2] = T(0.5) * (in.d[2] * out.f[2]);
-                    vc[3] = T(0.5) * (in.d[0] * out.f[1]);
-                    vc[4] = T(0.5) * (in.d[0] * out.f[2]);
-                    vc[5] = T(0.5) * (in.d[1] * out.f[2]);
                 }
             }
-            // each row atom's lane takes its contacts in slot order
-            uint32_t cm = __ballot_sync(0xffffffffu, contact);
-            while (cm) {
-                const int q = __ffs(cm) - 1;
-                cm &= cm - 1;
-                const int oq = owner[wib][q];
-                T gf[3], gt[3], gv[6];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    gf[c] = __shfl_sync(0xffffffffu, fc[c], q);
-                    gt[c] = __shfl_sync(0xffffffffu, tc[c], q);
+        }
+        return cand;
+    };
+    // contact forces of the `count` atoms in croster[wib]
+    auto contact_round = [&](int count) {
+        const bool mine = lane < count;
+        const int i = mine ? croster[wib][lane] : 0;
+        __syncwarp();
+            const int nn = mine ? L.nnb[i] : 0;
+            const uint64_t touch = (hist && mine) ? L.touch[i] : 0ull;
+            int incl = nn;
+    #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int start = incl - nn;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
+            uint64_t newtouch = 0ull;
+            for (int p0 = 0; p0 < total; p0 += 32) {
+                if (mine) {
+                    const int k0 = max(start, p0), k1 = min(start + nn, p0 + 32);
+                    for (int k = k0; k < k1; ++k) owner[wib][k - p0] = (uint8_t)lane;
                 }
-#pragma unroll
-                for (int c = 0; c < 6; ++c) gv[c] = __shfl_sync(0xffffffffu, vc[c], q);
-                if (lane == oq) {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        F[c] += gf[c];
-                        Tq[c] += gt[c];
+                __syncwarp();
+                const bool live = p0 + lane < total;
+                const int ol = live ? owner[wib][lane] : 0;
+                const int ost = __shfl_sync(0xffffffffu, start, ol);
+                const int ia = __shfl_sync(0xffffffffu, i, ol);  // the entry's row atom
+                const uint32_t tlo = __shfl_sync(0xffffffffu, (uint32_t)touch, ol);
+                const uint32_t thi = __shfl_sync(0xffffffffu, (uint32_t)(touch >> 32), ol);
+                bool contact = false;
+                T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
+                if (live) {
+                    const int k = p0 + lane - ost;      // the entry's slot in its row
+                    const int e = L.nbr[(size_t)k * n + ia];
+                    const int j = e & kNbrIndexMask;
+                    const bool lo = ia < j;
+                    T xi[3], xj[3], ri, rj;
+                    int32_t ci = 0;
+                    if constexpr (MIXED) {
+                        const float4 pi = ld4f(A.pos32, ia), pj = ld4f(A.pos32, j);
+                        xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+                        xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+                        if (vremap) ci = A.cell32[ia];
+                    } else {
+                        const double4 pi = ld4(A.xr, ia), pj = ld4(A.xr, j);
+                        xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+                        xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
                     }
+                    // separation x_i - x_j
+                    T d[3];
+                    T nimg[3] = {0, 0, 0};
+                    const int code = (unsigned)e >> kNbrIndexBits;
+                    const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+                    if constexpr (MIXED) {
+                        // offsets are relative to each atom's own cell: j's cell is
+                        // the stencil offset (ox, oy, oz) away from i's, so
+                        // x_i - x_j = (o_i - o_j) - offset * h
+    #pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            d[c] = (xi[c] - xj[c]) - (float)off[c] * hh[c];
+                            if (single[c]) {
+                                nimg[c] = rintf(d[c] * iprd[c]);
+                                d[c] -= nimg[c] * prd[c];
+                            }
+                        }
+                        if (vremap) {  // image count for the partner velocity shift
+                            const int32_t cj = A.cell32[j];
+                            const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
+                                               cell_z(ci) + off[2] - cell_z(cj)};
+    #pragma unroll
+                            for (int c = 0; c < 3; ++c)
+                                if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / gdim[c]);
+                        }
+                    } else {
+    #pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            d[c] = xi[c] - xj[c];
+                            if (per[c] == 1) {
+                                nimg[c] = rint(d[c] * iprd[c]);
+                                d[c] -= nimg[c] * prd[c];
+                            }
+                        }
+                    }
+                    PairIn<T> in;
+                    const T sg = lo ? T(1) : T(-1);
+                    in.ra = lo ? ri : rj;
+                    in.rb = lo ? rj : ri;
+                    bool near;
+                    if constexpr (MIXED) {
+                        // FP32 screen, with room for the FP32 rounding of the words
+                        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                        const float rs = (ri + rj) * 1.00001f;
+                        near = rq < rs * rs;
+                        if (near) {
+                            // separation, |d|^2, |d| and the overlap from the high and
+                            // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
+                            // FP32 difference of two unit-size numbers keeps 2^-24)
+                            const float4 il = ld4f(A.pos32lo, ia), jl = ld4f(A.pos32lo, j);
+                            const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
+                            float dh[3], dl[3];
+    #pragma unroll
+                            for (int c = 0; c < 3; ++c) {
+                                float s1, e1, s2, e2;
+                                two_sum(xi[c], -xj[c], s1, e1);
+                                two_sum(s1, -(float)off[c] * hh[c], s2, e2);
+                                const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), (float)off[c] * hlo[c]),
+                                                            __fadd_rn(e1, e2));
+                                two_sum(s2, low, dh[c], dl[c]);
+                                if (single[c]) {
+                                    const float ni = rintf(dh[c] * iprd[c]);
+                                    float s3, e3;
+                                    two_sum(dh[c], -ni * prd[c], s3, e3);
+                                    two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * prdlo[c]), e3), dh[c], dl[c]);
+                                }
+                                dh[c] = sg * dh[c];
+                                dl[c] = sg * dl[c];
+                            }
+                            // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
+                            float pp[3], pe[3];
+    #pragma unroll
+                            for (int c = 0; c < 3; ++c) {
+                                pp[c] = __fmul_rn(dh[c], dh[c]);
+                                pe[c] = __fmaf_rn(dh[c], dh[c], -pp[c]);
+                            }
+                            float t1, te1, rh, re;
+                            two_sum(pp[0], pp[1], t1, te1);
+                            two_sum(t1, pp[2], rh, re);
+                            const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]),
+                                                                                    __fmul_rn(dh[1], dl[1])),
+                                                                         __fmul_rn(dh[2], dl[2])));
+                            const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])),
+                                                        cross);
+                            float rsh, rsl;
+                            two_sum(rh, rl0, rsh, rsl);
+                            const float r_hi = __fsqrt_rn(rsh);
+                            const float res = __fmaf_rn(-r_hi, r_hi, rsh);  // exact
+                            const float r_lo = __fdiv_rn(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
+                            // ra + rb, both words
+                            const float4 al = lo ? il : jl, bl = lo ? jl : il;
+                            float sh_, se_;
+                            two_sum(in.ra, in.rb, sh_, se_);
+                            const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
+                            const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
+                            near = delta > 0.0f && rsh > 1e-28f;
+    #pragma unroll
+                            for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
+                            in.rsq = rsh;
+                            in.r = r_hi;
+                            in.delta = delta;
+                        }
+                    } else {
+    #pragma unroll
+                        for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
+                        in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
+                        const T radsum = in.ra + in.rb;
+                        near = in.rsq < radsum * radsum && in.rsq > T(1e-28);
+                        if (near) {
+                            in.r = sqrt(in.rsq);
+                            in.delta = radsum - in.r;
+                        }
+                    }
+                    if (near) {
+                        contact = true;
+                        T vi[3], wi[3], mi, vj[3], wj[3], mj;
+                        if constexpr (MIXED) {
+                            const float4 v = ld4f(A.vel32, ia), w = ld4f(A.om32, ia);
+                            const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
+                            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                            vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                            wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+                        } else {
+                            const double4 v = ld4(A.vm, ia), w = ld4(A.om, ia);
+                            const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
+                            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                            vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                            wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+                        }
+                        T dv[3] = {0, 0, 0};
+                        if (vremap) {
+                            // image count of x_a - x_b, then n . h_rate for partner b
+                            T na[3];
+    #pragma unroll
+                            for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
+                            dv[0] = (na[0] * hrate[0] + na[1] * hshear[2]) + na[2] * hshear[1];
+                            dv[1] = na[1] * hrate[1] + na[2] * hshear[0];
+                            dv[2] = na[2] * hrate[2];
+                        }
+                        in.ma = lo ? mi : mj;
+                        in.mb = lo ? mj : mi;
+    #pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            in.va[c] = lo ? vi[c] : vj[c];
+                            in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
+                            in.wa[c] = lo ? wi[c] : wj[c];
+                            in.wb[c] = lo ? wj[c] : wi[c];
+                        }
+                        double sh[3] = {0, 0, 0};
+                        const size_t so = (size_t)k * n + ia;
+                        const bool was = k < 32 ? ((tlo >> k) & 1u) : ((thi >> (k - 32)) & 1u);
+                        if (hist && was) {
+                            const double sgd = lo ? 1.0 : -1.0;
+                            sh[0] = sgd * L.shear[so];
+                            sh[1] = sgd * L.shear[ss + so];
+                            sh[2] = sgd * L.shear[2 * ss + so];
+                        }
+                        PairOut<T> out;
+                        contact_law<T, STYLE>(P, dt, 1, in, sh, out);
+                        if (hist) {
+                            const double sgd = lo ? 1.0 : -1.0;
+                            L.shear[so] = sgd * sh[0];
+                            L.shear[ss + so] = sgd * sh[1];
+                            L.shear[2 * ss + so] = sgd * sh[2];
+                        }
+                        const T arm = lo ? out.arm_a : out.arm_b;
+    #pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            fc[c] = sg * out.f[c];
+                            tc[c] = arm * out.tor[c];
+                        }
+                        vc[0] = T(0.5) * (in.d[0] * out.f[0]);
+                        vc[1] = T(0.5) * (in.d[1] * out.f[1]);
+                        vc[2] = T(0.5) * (in.d[2] * out.f[2]);
+                        vc[3] = T(0.5) * (in.d[0] * out.f[1]);
+                        vc[4] = T(0.5) * (in.d[0] * out.f[2]);
+                        vc[5] = T(0.5) * (in.d[1] * out.f[2]);
+                    }
+                }
+                // each row atom's lane takes its contacts in slot order
+                uint32_t cm = __ballot_sync(0xffffffffu, contact);
+                while (cm) {
+                    const int q = __ffs(cm) - 1;
+                    cm &= cm - 1;
+                    const int oq = owner[wib][q];
+                    T gf[3], gt[3], gv[6];
+    #pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        gf[c] = __shfl_sync(0xffffffffu, fc[c], q);
+                        gt[c] = __shfl_sync(0xffffffffu, tc[c], q);
+                    }
+    #pragma unroll
+                    for (int c = 0; c < 6; ++c) gv[c] = __shfl_sync(0xffffffffu, vc[c], q);
+                    if (lane == oq) {
+    #pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            F[c] += gf[c];
+                            Tq[c] += gt[c];
+                        }
+    #pragma unroll
+                        for (int c = 0; c < 6; ++c) V[c] += gv[c];
+                        newtouch |= 1ull << (p0 + q - start);
+                    }
+                }
+                __syncwarp();
+            }
+            if (mine) {
+                if (hist && newtouch != touch) L.touch[i] = newtouch;
+                T vi[3], wi[3], mi;
+                if constexpr (MIXED) {
+                    const float4 v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
+                    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                    wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                } else {
+                    const double4 v = ld4(A.vm, i), w = ld4(A.om, i);
+                    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                    wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                }
+                if (E->cundall) {  // FixDampingCundall.post_force_kernel
+                    T gl, ga;
+                    if constexpr (MIXED) {
+                        gl = E->gamma_lin32;
+                        ga = E->gamma_ang32;
+                    } else {
+                        gl = E->gamma_lin;
+                        ga = E->gamma_ang;
+                    }
+    #pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const T sf = F[c] * vi[c] >= T(0) ? T(1) : T(-1);
+                        F[c] *= T(1) - gl * sf;
+                        const T st = Tq[c] * wi[c] >= T(0) ? T(1) : T(-1);
+                        Tq[c] *= T(1) - ga * st;
+                    }
+                }
+                if constexpr (MIXED) {
+    #pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        A.f32[c * n + i] = F[c];
+                        A.torque32[c * n + i] = Tq[c];
+                    }
+                } else {
+    #pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        A.f[c * n + i] = F[c];
+                        A.torque[c * n + i] = Tq[c];
+                    }
+                }
+                // kinetic part of the virial with the end-of-step velocity
+                // v(t+dt) = v(t+dt/2) + dt/2 f/m (thermo.py:94-101): A counted
+                // m v(t+dt/2) v(t+dt/2) for every atom; the difference goes here
+                // (the same products from the same words, so a zero force adds an
+                // exact zero)
+                T im;
+                if constexpr (MIXED) im = 1.0f / mi;
+                else im = A.rinv[i];
+                const T hdt = T(0.5) * dt;
+                T vf[3];
+    #pragma unroll
+                for (int c = 0; c < 3; ++c) vf[c] = vi[c] + hdt * (F[c] * im);
+                const T kin[6] = {(mi * vf[0]) * vf[0], (mi * vf[1]) * vf[1], (mi * vf[2]) * vf[2],
+                                  (mi * vf[0]) * vf[1], (mi * vf[0]) * vf[2], (mi * vf[1]) * vf[2]};
+                const T kh[6] = {(mi * vi[0]) * vi[0], (mi * vi[1]) * vi[1], (mi * vi[2]) * vi[2],
+                                 (mi * vi[0]) * vi[1], (mi * vi[0]) * vi[2], (mi * vi[1]) * vi[2]};
+                if constexpr (MIXED) {
+    #pragma unroll
+                    for (int c = 0; c < 6; ++c) {
+                        dw_add(Vh[c], Vl[c], V[c]);
+                        dw_add(Vh[c], Vl[c], kin[c]);
+                        dw_add(Vh[c], Vl[c], -kh[c]);
+                    }
+                } else {
+    #pragma unroll
+                    for (int c = 0; c < 6; ++c) Vd[c] += (V[c] + kin[c]) - kh[c];
+                }
+            }
+    };
+    if (lane < kLive) cwords[wib][lane] = 0u;
+    __syncwarp();
+    int ncand = 0;  // atoms waiting in croster (warp-uniform)
+    for (int base = gw; base < ngroups; base += 32 * nwarps) {
+        const int mygrp = base + lane * nwarps;
+        uint32_t myold = 0u;
+        bool live = false;
+        if (mygrp < ngroups) {
+            myold = flags[mygrp];
+            live = !(cull && gap[mygrp] > thr);
+            if (!live && myold != 0u) {
+                // ruled out now, flagged last step: clear the stale forces
+                for (uint32_t w = myold; w; w &= w - 1) zero_force<MIXED>(A, (mygrp << 5) + __ffs(w) - 1);
+                flags[mygrp] = 0u;
+            }
+        }
+        uint32_t pending = __ballot_sync(0xffffffffu, live);
+        while (pending) {
+            // up to kLive live groups at once
+            int gq[kLive];
+            uint32_t oq[kLive], nw[kLive];
+            int nq = 0;
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) V[c] += gv[c];
-                    newtouch |= 1ull << (p0 + q - start);
+            for (int u = 0; u < kLive; ++u) {
+                gq[u] = 0;
+                oq[u] = 0u;
+                if (pending) {
+                    const int src = __ffs(pending) - 1;
+                    pending &= pending - 1;
+                    gq[u] = base + src * nwarps;
+                    oq[u] = __shfl_sync(0xffffffffu, myold, src);
+                    nq = u + 1;
+                }
+            }
+            // the atoms' own bounds, all issued at once
+            float ag[kLive];
+#pragma unroll
+            for (int u = 0; u < kLive; ++u) {
+                const int i = (gq[u] << 5) + lane;
+                ag[u] = (u < nq && i < n) ? agap[i] : 0.0f;
+            }
+            int near_total = 0;
+#pragma unroll
+            for (int u = 0; u < kLive; ++u) {
+                const int i = (gq[u] << 5) + lane;
+                nw[u] = __ballot_sync(0xffffffffu, u < nq && i < n && !(cull && ag[u] > thr));
+                near_total += __popc(nw[u]);
+            }
+            // screen the near atoms, 32 at a time, in group then atom order
+            for (int r0 = 0; r0 < near_total; r0 += 32) {
+                const int idx = r0 + lane;
+                int uq = -1, bit = 0, acc = 0, g = 0;
+#pragma unroll
+                for (int u = 0; u < kLive; ++u) {
+                    const int c = __popc(nw[u]);
+                    if (uq < 0 && idx < acc + c) {
+                        uq = u;
+                        bit = nth_bit(nw[u], idx - acc);
+                        g = gq[u];
+                    }
+                    acc += c;
+                }
+                bool cand = false;
+                int i = 0;
+                if (uq >= 0) {
+                    i = (g << 5) + bit;
+                    cand = screen_atom(i);
+                    if (cand) atomicOr(&cwords[wib][uq], 1u << bit);
+                    else if (hist && L.touch[i] != 0ull) L.touch[i] = 0ull;
+                }
+                // flagged atoms join the contact roster
+                const uint32_t cm = __ballot_sync(0xffffffffu, cand);
+                if (ncand + __popc(cm) > 32) {
+                    contact_round(ncand);
+                    ncand = 0;
+                }
+                if (cand) croster[wib][ncand + __popc(cm & ((1u << lane) - 1u))] = i;
+                ncand += __popc(cm);
+                __syncwarp();
+            }
+            __syncwarp();
+            // new flag words; stale forces of atoms no longer flagged
+#pragma unroll
+            for (int u = 0; u < kLive; ++u) {
+                if (u < nq) {
+                    const uint32_t w = cwords[wib][u];
+                    const int i = (gq[u] << 5) + lane;
+                    if (lane == 0 && w != oq[u]) flags[gq[u]] = w;
+                    if (i < n && ((oq[u] >> lane) & 1u) && !((w >> lane) & 1u)) zero_force<MIXED>(A, i);
                 }
             }
             __syncwarp();
-        }
-        if (mine) {
-            if (hist && newtouch != touch) L.touch[i] = newtouch;
-            T vi[3], wi[3], mi;
-            if constexpr (MIXED) {
-                const float4 v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
-                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-            } else {
-                const double4 v = ld4(A.vm, i), w = ld4(A.om, i);
-                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-            }
-            if (E->cundall) {  // FixDampingCundall.post_force_kernel
-                T gl, ga;
-                if constexpr (MIXED) {
-                    gl = E->gamma_lin32;
-                    ga = E->gamma_ang32;
-                } else {
-                    gl = E->gamma_lin;
-                    ga = E->gamma_ang;
-                }
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const T sf = F[c] * vi[c] >= T(0) ? T(1) : T(-1);
-                    F[c] *= T(1) - gl * sf;
-                    const T st = Tq[c] * wi[c] >= T(0) ? T(1) : T(-1);
-                    Tq[c] *= T(1) - ga * st;
-                }
-            }
-            if constexpr (MIXED) {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    A.f32[c * n + i] = F[c];
-                    A.torque32[c * n + i] = Tq[c];
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    A.f[c * n + i] = F[c];
-                    A.torque[c * n + i] = Tq[c];
-                }
-            }
-            // kinetic part of the virial with the end-of-step velocity
-            // v(t+dt) = v(t+dt/2) + dt/2 f/m (thermo.py:94-101): A counted
-            // m v(t+dt/2) v(t+dt/2) for every atom; the difference goes here
-            // (the same products from the same words, so a zero force adds an
-            // exact zero)
-            T im;
-            if constexpr (MIXED) im = 1.0f / mi;
-            else im = A.rinv[i];
-            const T hdt = T(0.5) * dt;
-            T vf[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) vf[c] = vi[c] + hdt * (F[c] * im);
-            const T kin[6] = {(mi * vf[0]) * vf[0], (mi * vf[1]) * vf[1], (mi * vf[2]) * vf[2],
-                              (mi * vf[0]) * vf[1], (mi * vf[0]) * vf[2], (mi * vf[1]) * vf[2]};
-            const T kh[6] = {(mi * vi[0]) * vi[0], (mi * vi[1]) * vi[1], (mi * vi[2]) * vi[2],
-                             (mi * vi[0]) * vi[1], (mi * vi[0]) * vi[2], (mi * vi[1]) * vi[2]};
-            if constexpr (MIXED) {
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    dw_add(Vh[c], Vl[c], V[c]);
-                    dw_add(Vh[c], Vl[c], kin[c]);
-                    dw_add(Vh[c], Vl[c], -kh[c]);
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 6; ++c) Vd[c] += (V[c] + kin[c]) - kh[c];
-            }
+            if (lane < kLive) cwords[wib][lane] = 0u;
+            __syncwarp();
         }
     }
-    }
+    if (ncand > 0) contact_round(ncand);
     if constexpr (MIXED) {
         block_sum_dw<6, kBlockC>(Vh, Vl, reinterpret_cast<float2*>(smem));
         if (threadIdx.x == 0) {
@@ -1433,28 +1458,21 @@ int wave_blocks(K kernel, int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, block, 0) != cudaSuccess || occ < 1) occ = 1;
     return occ * sm_count();
 }
-int screen_wave(bool mixed) {
-    static int w[2] = {0, 0};
-    int& v = w[mixed ? 1 : 0];
-    if (!v) v = mixed ? wave_blocks(k_screen<true>, kBlockScreen) : wave_blocks(k_screen<false>, kBlockScreen);
-    return v;
-}
 int contact_wave(int style, bool mixed) {
     static int w[5][2] = {};
     if (style < 0 || style > 4) style = 4;
     int& v = w[style][mixed ? 1 : 0];
     if (!v) {
         switch (style) {
-            case 0: v = mixed ? wave_blocks(k_c<0, true>, kBlockC) : wave_blocks(k_c<0, false>, kBlockC); break;
-            case 1: v = mixed ? wave_blocks(k_c<1, true>, kBlockC) : wave_blocks(k_c<1, false>, kBlockC); break;
-            case 2: v = mixed ? wave_blocks(k_c<2, true>, kBlockC) : wave_blocks(k_c<2, false>, kBlockC); break;
-            case 3: v = mixed ? wave_blocks(k_c<3, true>, kBlockC) : wave_blocks(k_c<3, false>, kBlockC); break;
-            default: v = mixed ? wave_blocks(k_c<4, true>, kBlockC) : wave_blocks(k_c<4, false>, kBlockC); break;
+            case 0: v = mixed ? wave_blocks(k_cf<0, true>, kBlockC) : wave_blocks(k_cf<0, false>, kBlockC); break;
+            case 1: v = mixed ? wave_blocks(k_cf<1, true>, kBlockC) : wave_blocks(k_cf<1, false>, kBlockC); break;
+            case 2: v = mixed ? wave_blocks(k_cf<2, true>, kBlockC) : wave_blocks(k_cf<2, false>, kBlockC); break;
+            case 3: v = mixed ? wave_blocks(k_cf<3, true>, kBlockC) : wave_blocks(k_cf<3, false>, kBlockC); break;
+            default: v = mixed ? wave_blocks(k_cf<4, true>, kBlockC) : wave_blocks(k_cf<4, false>, kBlockC); break;
         }
     }
     return v;
 }
-int screen_blocks(int n, bool mixed) { const int b = grid_for(n, kBlockScreen); return b < screen_wave(mixed) ? b : screen_wave(mixed); }
 int a_wave(bool mixed) {
     static int w[2] = {0, 0};
     int& v = w[mixed ? 1 : 0];
@@ -1536,22 +1554,17 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
     if (p->style < 0 || p->style > 4 || nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
     const int n = a->n;
     const bool mixed = a->pos32 != nullptr;
-    const int g1 = screen_blocks(n, mixed), g2 = contact_blocks(n, p->style, mixed);
+    const int g2 = contact_blocks(n, p->style, mixed);
     uint32_t* flags = (uint32_t*)scratch;
     const float* gap = (const float*)((char*)scratch + gap_offset(n));
     const float* agap = (const float*)((char*)scratch + atom_gap_offset(n));
-    // partials are component-major, [6][nblocks]; the contact pass's blocks follow A's
+    // partials are component-major, [6][nblocks]; C's blocks follow A's
     double* part2 = (double*)((char*)scratch + part_offset(n)) + (size_t)a_blocks(n, mixed);
     cudaStream_t s = (cudaStream_t)stream;
     if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-    const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
-    const int hi = has_hist ? 1 : 0;
-    if (mixed) launch_pdl(k_screen<true>, g1, kBlockScreen, s, *a, *nl, d_box, d_eng, hi, flags, gap, agap);
-    else launch_pdl(k_screen<false>, g1, kBlockScreen, s, *a, *nl, d_box, d_eng, hi, flags, gap, agap);
-    const uint32_t* cflags = flags;
-#define TMPS_LAUNCH_C(ST)                                                                          \
-    if (mixed) launch_pdl(k_c<ST, true>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, cflags, part2); \
-    else launch_pdl(k_c<ST, false>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, cflags, part2);
+#define TMPS_LAUNCH_C(ST)                                                                                    \
+    if (mixed) launch_pdl(k_cf<ST, true>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, flags, gap, agap, part2); \
+    else launch_pdl(k_cf<ST, false>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, flags, gap, agap, part2);
     switch (p->style) {
         case 0: TMPS_LAUNCH_C(0) break;
         case 1: TMPS_LAUNCH_C(1) break;
@@ -1560,7 +1573,7 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
         default: TMPS_LAUNCH_C(4) break;
     }
 #undef TMPS_LAUNCH_C
-    note_launches(2);
+    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 

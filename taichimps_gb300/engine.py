@@ -2,10 +2,9 @@
 The fused step engine behind ``Simulation.run``.
 
 One step of Simulation._sub_step_inner (simulation.py:205-247) with fix
-nve/sphere, optionally damping/cundall and deform/pressure, becomes four
-kernels (tmps_fused_a; tmps_fused_c's screen and contact passes;
-tmps_fused_servo) that decide on the device whether the step needs a neighbor
-rebuild.  Steps are queued in chunks (replayed as CUDA graphs) with one host
+nve/sphere, optionally damping/cundall and deform/pressure, becomes three
+kernels (tmps_fused_a, tmps_fused_c, tmps_fused_servo) that decide on the
+device whether the step needs a neighbor rebuild.  Steps are queued in chunks (replayed as CUDA graphs) with one host
 synchronisation per chunk.  When a step finds it needs a rebuild, every later
 launch of the chunk does nothing; the host then rebuilds exactly as the
 reference does at that step (save history, wrap, build, restore history),
@@ -48,8 +47,8 @@ def fusable(sim) -> bool:
 
 
 class FusedEngine:
-    # kernels per step: A, the two passes of C, S
-    LAUNCHES_PER_STEP = 4
+    # kernels per step: A, C, S
+    LAUNCHES_PER_STEP = 3
 
     def __init__(self, sim, precision: str = "fp64", chunk: int = 64, graphs: bool = True,
                  cull: bool = True) -> None:
