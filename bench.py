@@ -134,22 +134,41 @@ def list_stats(sim):
     return nnb, bits / max(sim.atom.nlocal, 1)
 
 
-def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float) -> float:
-    """HBM bytes per atom a launch must move (reads + writes of per-atom and per-slot arrays; gathers of
-    neighbor state are L2 reuse after the cell re-sort and are not counted).
+def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float, flagged: float) -> float:
+    """Bytes per atom a launch must move through HBM.
 
-    fused_a  FP64: x/v/omega records 96 r + 96 w, f/torque 48 r, 1/m 1/I 16 r, x0 24 r
-             mixed: records 96 r + 96 w, FP32 force/torque 24 r, 1/m 1/I 16 r, FP32 offset-at-build 12 r,
-                    cell 4 r, FP32 copies (pos, vel, omega) 48 w
-    fused_c  FP64: own records 96 r, 1/m 8 r, row length 4 + touch 8 r, f/torque 48 w
-             mixed: own FP32 copies 48 r, 1/m 8 r, row length 4 + touch 8 r, FP32 force/torque 24 w
-             both: 4 per neighbor index, 48 per touching slot (FP64 shear read + write)"""
+    fused_a (A), every atom:
+      mixed: reads the six FP32 state words (position, velocity, angular velocity, high and low) 96,
+             offset at the last build 12, packed cell 4; writes the six state words 96          = 208
+      FP64:  reads x, v, omega records 96, 1/m and 1/I 16, x at the last build 24; writes the records 96
+                                                                                                 = 232
+      plus, per flagged atom (`flagged` = fraction), the force and torque: 24 (mixed) / 48 (FP64).
+    fused_c (C): the contact kernel's nominal per-atom bytes, S + 4 n_nb + 52 n_c (own state read once
+      and force written once, S = 84 mixed / 140 FP64; 4 per neighbor index; 4 partner + 48 shear per
+      touching slot).  C's bound check skips most of these bytes (groups that cannot touch read 4 bytes
+      per 32 atoms), so this figure is nominal: it says what a kernel without the check would move."""
     if kernel == "fused_a":
-        return 280.0 if precision == "fp64" else 296.0
+        return (208.0 + 24.0 * flagged) if precision == "mixed" else (232.0 + 48.0 * flagged)
     if kernel == "fused_c":
-        base = 164.0 if precision == "fp64" else 92.0
-        return base + 4.0 * n_nb + 48.0 * n_c
+        return (84.0 if precision == "mixed" else 140.0) + 4.0 * n_nb + 52.0 * n_c
     return 0.0
+
+
+KERNEL_NAMES = {("fused_a", "mixed"): "k_a32", ("fused_a", "fp64"): "k_a64", ("fused_c", "mixed"): "k_cf",
+                ("fused_c", "fp64"): "k_cf", ("fused_s", "mixed"): "k_s", ("fused_s", "fp64"): "k_s"}
+TRAFFIC_FILE = ROOT / "profiles" / "ncu_traffic_config2_1M.json"
+
+
+def ncu_traffic(kernel: str, precision: str):
+    """DRAM bytes (read + write) per launch of a kernel of this workload, from the committed ncu capture
+    (profiles/ncu_traffic_config2_1M.json, which names its command); None when absent."""
+    if not TRAFFIC_FILE.exists():
+        return None
+    d = json.loads(TRAFFIC_FILE.read_text())
+    k = d.get("kernels", {}).get(f"{KERNEL_NAMES[(kernel, precision)]}/{precision}")
+    if not k:
+        return None
+    return {"bytes": k["dram_bytes_read"] + k["dram_bytes_write"], "source": f"ncu: {d.get('command', '')}"}
 
 
 def run_gpu_arm(args, p, precision, rank, world):
@@ -186,6 +205,7 @@ def run_gpu_arm(args, p, precision, rank, world):
     # graph replays do not pass through the host entry points, so count the launches the graph holds
     launches = (L.tmps_launch_count() - l0) + (eng.graph_kernel_launches - g0)
     cull = eng.cull_stats()
+    flagged = eng.flagged_count() / max(sim.atom.nlocal, 1)
     # per-kernel CUDA-event timings: the next K steps launched one by one (same run, same state)
     _device.TIMED = {k: [] for k in names}
     eng.run(K)
@@ -205,7 +225,7 @@ def run_gpu_arm(args, p, precision, rank, world):
     kern = {k: (sum(v) / len(v) if v else None) for k, v in timed.items()}
     return dict(sim=sim, n=n, ms=ms, launches=launches, clocks=clk, kern_ms=kern, n_nb=n_nb, n_c=n_c,
                 pressure=pressure, builds=sim.neighbor.build_count, rebuilds_timed=eng.rebuilds,
-                steps_run=sim.timestep, cull=cull)
+                steps_run=sim.timestep, cull=cull, flagged=flagged)
 
 
 def run_e2e(args, p, precision):
@@ -360,8 +380,9 @@ def main():
     peak = peaks.get("hbm_gbs", 6806.5)
     kern = r["kern_ms"]
     dom_name = max(("fused_a", "fused_c"), key=lambda k: kern.get(k) or 0.0)
-    bytes_atom = algorithmic_bytes(dom_name, head, r["n_nb"], r["n_c"])
+    bytes_atom = algorithmic_bytes(dom_name, head, r["n_nb"], r["n_c"], r["flagged"])
     achieved = bytes_atom * n / (kern[dom_name] * 1e-3) / 1e9 if kern.get(dom_name) else None
+    traffic = ncu_traffic(dom_name, head)
     e2e = None if args.no_e2e else run_e2e(args, p, head)
     cpu = None
     p_oracle = None
@@ -375,7 +396,7 @@ def main():
     scal = lambda t: (t[0] + t[1] + t[2]) / 3.0
     forms_out = {}
     for k, v in runs.items():
-        kb = {kk: algorithmic_bytes(kk, k, v["n_nb"], v["n_c"]) for kk in ("fused_a", "fused_c")}
+        kb = {kk: algorithmic_bytes(kk, k, v["n_nb"], v["n_c"], v["flagged"]) for kk in ("fused_a", "fused_c")}
         forms_out[k] = {
             "value": values[k], "ms_per_step": v["ms"] / K, "kernel_ms": v["kern_ms"],
             "kernel_gbs": {kk: (kb[kk] * n / (v["kern_ms"][kk] * 1e-3) / 1e9 if v["kern_ms"].get(kk) else None)
@@ -383,7 +404,9 @@ def main():
             "mean_pressure": scal(v["pressure"]), "pressure": list(map(float, v["pressure"])),
             "mean_pressure_rel_err_vs_oracle": None if p_oracle is None else rel(scal(v["pressure"]), scal(p_oracle)),
             "gpu_launches": v["launches"], "rebuilds_in_timed_steps": v["rebuilds_timed"],
-            "groups_culled": {"groups": v["cull"][0], "culled_after_timed_steps": v["cull"][1]}}
+            "groups_culled": {"groups": v["cull"][0], "culled_after_timed_steps": v["cull"][1]},
+            "flagged_atoms_frac": v["flagged"],
+            "kernel_bytes_per_atom": kb, "kernel_bytes_note": "fused_c: nominal (see algorithmic_bytes)"}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": r["ms"] / K, "higher_is_better": True, "scaling": "weak",
@@ -393,9 +416,12 @@ def main():
         "config": {"workload": WORKLOAD, "n_atoms": n, "precision": head, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2: ~0.4 GB of per-atom and neighbor state per replica",
                    "neighbors_per_atom": r["n_nb"], "contacts_per_atom": r["n_c"], "neighbor_builds": r["builds"]},
-        "roofline": {"kernel": dom_name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "bytes_per_atom": bytes_atom, "kernel_ms": kern[dom_name], "peak_source": "measured"},
+        "roofline": {"kernel": KERNEL_NAMES[(dom_name, head)], "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": traffic["bytes"] if traffic else None,
+                     "traffic_source": traffic["source"] if traffic else None,
+                     "algorithmic_bytes_per_launch": bytes_atom * n, "bytes_per_atom": bytes_atom,
+                     "kernel_ms": kern[dom_name], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
         "speedup_mixed_vs_fp64": (values["mixed"] / values["fp64"]) if len(values) == 2 else None,
         "oracle_mean_pressure": None if p_oracle is None else scal(p_oracle),
         "pressure_compared_after_steps": r["steps_run"],

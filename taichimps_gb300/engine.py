@@ -247,6 +247,15 @@ class FusedEngine:
         thr = (f32(2.0) * md) * f32(1.0001) + f32(e.shift_bound) + f32(e.cull_tol)
         return ng, int(np.count_nonzero(gap > thr))
 
+    def flagged_count(self) -> int:
+        """Atoms C flagged (some neighbor within reach of contact) in the last step, from the flag
+        words.  No reference counterpart; for reports and tests."""
+        ng = (self._n + 31) // 32
+        if ng == 0:
+            return 0
+        w = self.part[:4 * ng].view(torch.int32).cpu().numpy().view(np.uint32)
+        return int(np.unpackbits(w.view(np.uint8)).sum())
+
     def _check_status(self) -> None:
         st = int(self.status.item())
         if st & _lib.STATUS_BOX_NONPOSITIVE and self.deform is not None:
