@@ -111,11 +111,15 @@ class ClockSampler:
 # ----------------------------------------------------------------- GPU arm
 
 
-def make_sim(G, p, n, precision):
+def make_sim(G, p, n, precision, host=None):
+    """The config-2 system; `host` (optional) holds x, v as pinned float64 tensors to upload from."""
     L = p["L"]
     dom = G.Domain(boxlo=[0.0] * 3, boxhi=[L] * 3, boundary=("p", "p", "p"))
     atom = G.AtomSystem(max_atoms=n)
-    atom.add_particles(x=p["x"], radius=p["radius"], density=p["density"], v=p["v"])
+    if host is not None:
+        atom.add_particles(x=host["x"], radius=host["radius"], density=p["density"], v=host["v"])
+    else:
+        atom.add_particles(x=p["x"], radius=p["radius"], density=p["density"], v=p["v"])
     nl = G.NeighborList(domain=dom, skin=SKIN, max_atoms=n, max_neighbors_per_atom=32)
     hist = G.ContactHistory(max_atoms=n, max_neighbors=32)
     pair = G.GranHertzHistory(domain=dom, **PAIR)
@@ -229,39 +233,41 @@ def run_gpu_arm(args, p, precision, rank, world):
 
 
 def run_e2e(args, p, precision):
-    """The same metric through the public API, from host arrays (pinned): upload, setup, K steps with a
-    read-back of the servo's pressure tensor after every step (what the reference's host servo path reads
-    each step), download of positions and velocities.  Steps are queued one at a time, so every step
-    pays a host round trip as the reference's does."""
+    """The same metric through the public API, from pinned host arrays: upload and setup
+    (Simulation.run builds the list and evaluates the setup forces), K steps whose servo pressure tensor
+    lands in pinned host memory every step (the per-step read-back of the reference's host servo path,
+    FixDeformPressure.record_pressure), then the download of positions and velocities.  The whole job
+    runs once untimed first (allocator and graph warm-up), then once timed."""
     import torch
     import taichimps_gb300 as G
-    from taichimps_gb300.engine import FusedEngine
 
     n = len(p["x"])
     K = args.steps
     host = {k: torch.from_numpy(np.ascontiguousarray(p[k])).pin_memory() for k in ("x", "radius", "v")}
+
+    def job():
+        sim = make_sim(G, p, n, precision, host=host)
+        fix = sim.fixes[-1]
+        fix.record_pressure(K + 1)
+        sim.run(K)
+        pressures = fix.pressure_history(range(1, K + 1))
+        x = sim.atom.x.to_numpy()
+        v = sim.atom.v.to_numpy()
+        return x, v, pressures
+
+    job()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sim = make_sim(G, {"x": host["x"].numpy(), "radius": host["radius"].numpy(), "v": host["v"].numpy(),
-                       "density": p["density"], "L": p["L"]}, n, precision)
-    fix = sim.fixes[-1]
-    sim.setup_run(K)
-    sim.init_simulation()
-    eng = FusedEngine(sim, precision, chunk=1)
-    eng.begin()
-    for _ in range(K):
-        eng.run(1)
-        fix.last_pressure()
-    eng.finish()
-    x = sim.atom.x.to_numpy()
-    v = sim.atom.v.to_numpy()
+    x, v, pressures = job()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    assert np.isfinite(x).all() and np.isfinite(v).all()
-    up = n * (3 * 8 + 8 + 8 + 3 * 8)           # positions, radius, density-derived mass, velocities
-    down = n * 2 * 3 * 8 + K * (48 + 4 + 160)   # final x, v; per step pressure, status, engine state
+    assert np.isfinite(x).all() and np.isfinite(v).all() and np.isfinite(pressures).all()
+    up = n * (3 * 8 + 8 + 3 * 8 + 2 * 8)        # positions, radius, velocities; mass and inertia
+    down = n * 2 * 3 * 8 + K * 48               # final x, v; per step the pressure tensor
     return {"value": n * K / dt, "unit": UNIT, "h2d_bytes_per_step": up / K, "d2h_bytes_per_step": down / K,
-            "seconds": dt, "precision": precision}
+            "seconds": dt, "precision": precision,
+            "includes": "upload, neighbor build + setup forces, K steps, per-step pressure to host, download "
+                        "(second of two identical jobs)"}
 
 
 # ----------------------------------------------------------------- CPU (oracle)

@@ -193,6 +193,11 @@ typedef struct tmps_engine {
     uint32_t maxd2_bits;     /* running max of |x - x0|^2 over atoms and steps, FP32 bits */
     int32_t cull;            /* 1: the per-group gaps in the scratch are valid */
     float cull_tol;          /* absolute slack for the FP32 rounding of the test */
+    /* Optional per-step record of the servo's pressure tensor in host memory
+     * (tmps_fused_pressure_log): step s writes plog[(s % plog_len) * 6 + k]. */
+    double* plog;            /* device address of a pinned host array, or NULL */
+    int32_t plog_len;
+    int32_t pad5_;
 } tmps_engine;
 
 /* ---- library ---------------------------------------------------------- */
@@ -358,6 +363,14 @@ int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed);
 
 /* Scratch bytes tmps_fused_c / tmps_fused_servo need (same arguments). */
 int64_t tmps_fused_scratch_bytes(int32_t n, int32_t style, int32_t mixed);
+
+/* Records the servo's pressure tensor of every fused step into h_log, pinned
+ * (page-locked, device-mapped) host memory of len x 6 doubles: step s writes
+ * row s % len, from the device, with no host synchronisation.  h_log = NULL
+ * stops recording.  The reference's host servo path reads this tensor back
+ * every step (deform_pressure.py:1113-1219); this is that read without the
+ * round trip. */
+int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void* stream);
 
 /* Applies what the fused step leaves pending -- the second half-kick of the
  * last step and a remap x the servo asked for -- so the state is that of the

@@ -105,6 +105,8 @@ class FixDeformPressure(Fix):
         self._started = False
         self.on_device = True
         self.device_reason = ""
+        # optional per-step record of the pressure tensor in pinned host memory (record_pressure)
+        self.pressure_log: torch.Tensor | None = None
 
     def _configure(self, axes: dict) -> None:
         for name, spec in axes.items():
@@ -262,3 +264,19 @@ class FixDeformPressure(Fix):
     def last_pressure(self) -> np.ndarray:
         """The pressure tensor the servo used on its last update (synchronises)."""
         return np.array(_device.pull_struct(self._dservo, _lib.Servo).pressure[:])
+
+    def record_pressure(self, capacity: int) -> None:
+        """Have every fused step write its pressure tensor to pinned host memory (a ring of
+        `capacity` rows, row = timestep % capacity), with no host synchronisation: the
+        per-step read-back of the reference's host servo path (deform_pressure.py:1113-1219)
+        without the round trip.  capacity 0 stops recording."""
+        self.pressure_log = (torch.zeros((int(capacity), 6), dtype=torch.float64).pin_memory()
+                             if capacity > 0 else None)
+
+    def pressure_history(self, steps) -> np.ndarray:
+        """Recorded pressure tensors of the given timesteps (rows of 6), after the run returned."""
+        if self.pressure_log is None:
+            raise RuntimeError("record_pressure() was not called")
+        torch.cuda.synchronize()
+        log = self.pressure_log.numpy()
+        return np.stack([log[int(s) % len(log)] for s in steps])

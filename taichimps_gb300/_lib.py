@@ -98,6 +98,7 @@ class Engine(ctypes.Structure):
         ("prd_ref", c_f64 * 3), ("part_off", ctypes.c_int64),
         ("shift_bound", ctypes.c_float), ("maxd2_bits", ctypes.c_uint32), ("cull", c_i32),
         ("cull_tol", ctypes.c_float),
+        ("plog", ctypes.c_void_p), ("plog_len", c_i32), ("pad5_", c_i32),
     ]
 
 
@@ -140,6 +141,7 @@ _SIGS = {
     "tmps_fused_blocks": (c_i32, [c_i32, c_i32, c_i32]),
     "tmps_fused_scratch_bytes": (ctypes.c_int64, [c_i32, c_i32, c_i32]),
     "tmps_fused_settle": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp]),
+    "tmps_fused_pressure_log": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
 }
 
 _lib: ctypes.CDLL | None = None

@@ -52,11 +52,17 @@ class FieldView:
     def to_numpy(self) -> np.ndarray:
         a = self._atom
         shape = (a.max_atoms,) if self._w == 1 else (a.max_atoms, self._w)
+        if not a.nlocal:
+            return np.zeros(shape, dtype=self._dtype)
+        # back to insertion order on the device, then one contiguous copy
+        vals = self._internal().detach()
+        ordered = torch.empty(vals.shape, dtype=vals.dtype, device=vals.device)
+        ordered[a.buffers.uid.long()] = vals
+        host = ordered.cpu().numpy().astype(self._dtype, copy=False)
+        if a.nlocal == a.max_atoms:
+            return host
         out = np.zeros(shape, dtype=self._dtype)
-        if a.nlocal:
-            vals = self._internal().detach().cpu().numpy()
-            uid = a.uid_host()
-            out[uid] = vals
+        out[:a.nlocal] = host
         return out
 
     def from_numpy(self, arr) -> None:
@@ -162,7 +168,18 @@ class AtomSystem:
     # ---------------------------------------------------------- particles
 
     def add_particles(self, x, radius, density, v=None, omega=None, tag=None, atom_type=1) -> None:
-        """Append particles; rmass = 4/3 pi r^3 density (atom.py:55-145)."""
+        """Append particles; rmass = 4/3 pi r^3 density (atom.py:55-145).  Arrays may be numpy or
+        torch tensors; a pinned host tensor or a CUDA tensor is uploaded without a host copy."""
+        tens = {k: a for k, a in (("x", x), ("v", v), ("omega", omega)) if isinstance(a, torch.Tensor)}
+        if isinstance(radius, torch.Tensor):
+            radius = radius.detach().cpu().numpy()
+        if tens and self.nlocal == 0 and all(t.dtype == torch.float64 and t.dim() == 2 and t.shape[1] == 3
+                                              for t in tens.values()):
+            self._add_first_tensors(tens, radius, density, tag, atom_type)
+            return
+        x = x.detach().cpu().numpy() if isinstance(x, torch.Tensor) else x
+        v = v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
+        omega = omega.detach().cpu().numpy() if isinstance(omega, torch.Tensor) else omega
         x_np = np.asarray(x, dtype=np.float64)
         if x_np.ndim == 1:
             x_np = x_np.reshape(1, 3)
@@ -184,8 +201,35 @@ class AtomSystem:
         tags = (np.arange(start + 1, start + n_new + 1, dtype=np.int32) if tag is None
                 else np.asarray(tag, dtype=np.int32))
 
-        old = self._gather_all() if self.nlocal else None
         n = start + n_new
+        if start == 0:
+            # first particles: upload the inputs, assemble the packed records on the device
+            nb = _Buffers(n, self.device)
+            dev = self.device
+
+            def up(arr):
+                return torch.from_numpy(np.ascontiguousarray(arr)).to(dev)
+
+            nb.xr[:, :3] = up(x_np)
+            nb.xr[:, 3] = up(rad)
+            nb.vm[:, :3] = up(v_np)
+            nb.vm[:, 3] = up(mass)
+            if omega is not None:
+                nb.om[:, :3] = up(o_np)
+            nb.om[:, 3] = up(inertia)
+            nb.tag.copy_(up(tags))
+            nb.uid.copy_(torch.arange(n, dtype=torch.int32, device=dev))
+            self._buf = nb
+            self._alt = _Buffers(n, dev)
+            self.atom_type_host = np.concatenate([self.atom_type_host, types])
+            self.mask_host = np.concatenate([self.mask_host, np.ones(n_new, dtype=np.int32)])
+            self.nlocal = n
+            self._uid_cache = None
+            self.max_radius = float(rad.max()) if n else 0.0
+            for cb in self._listeners:
+                cb()
+            return
+        old = self._gather_all()
         nb = _Buffers(n, self.device)
         host = {
             "xr": np.zeros((n, 4)), "vm": np.zeros((n, 4)), "om": np.zeros((n, 4)),
@@ -193,11 +237,10 @@ class AtomSystem:
             "tag": np.zeros(n, dtype=np.int32), "uid": np.arange(n, dtype=np.int32),
             "x0": np.zeros((3, n)),
         }
-        if old is not None:
-            for k in ("xr", "vm", "om", "tag"):
-                host[k][:start] = old[k]
-            for k in ("f", "torque", "virial", "x0"):
-                host[k][:, :start] = old[k]
+        for k in ("xr", "vm", "om", "tag"):
+            host[k][:start] = old[k]
+        for k in ("f", "torque", "virial", "x0"):
+            host[k][:, :start] = old[k]
         host["xr"][start:, :3] = x_np
         host["xr"][start:, 3] = rad
         host["vm"][start:, :3] = v_np
@@ -214,6 +257,46 @@ class AtomSystem:
         self.nlocal = n
         self._uid_cache = None
         self.max_radius = float(host["xr"][:, 3].max()) if n else 0.0
+        for cb in self._listeners:
+            cb()
+
+    def _add_first_tensors(self, tens, radius, density, tag, atom_type) -> None:
+        """add_particles into an empty system from float64 [n, 3] tensors (x; v and omega optional):
+        records assembled on the device; mass and inertia computed on the host as in add_particles."""
+        dev = self.device
+        xt = tens["x"]
+        n = int(xt.shape[0])
+        if n > self.max_atoms:
+            raise ValueError(f"Exceeded max_atoms capacity: {n} > {self.max_atoms}")
+        rad = np.asarray(radius, dtype=np.float64)
+        if rad.ndim == 0:
+            rad = np.full(n, float(rad))
+        dens = np.full(n, float(density)) if np.isscalar(density) else np.asarray(density, dtype=np.float64)
+        types = (np.full(n, int(atom_type), dtype=np.int32) if np.isscalar(atom_type)
+                 else np.asarray(atom_type, dtype=np.int32))
+        vol = (4.0 / 3.0) * np.pi * (rad ** 3)
+        mass = vol * dens
+        inertia = ((0.4 * mass) * rad) * rad
+        tags = np.arange(1, n + 1, dtype=np.int32) if tag is None else np.asarray(tag, dtype=np.int32)
+        nb = _Buffers(n, dev)
+        nb.xr[:, :3] = xt.to(dev, non_blocking=True)
+        if "v" in tens:
+            nb.vm[:, :3] = tens["v"].to(dev, non_blocking=True)
+        if "omega" in tens:
+            nb.om[:, :3] = tens["omega"].to(dev, non_blocking=True)
+        up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        nb.xr[:, 3] = up(rad)
+        nb.vm[:, 3] = up(mass)
+        nb.om[:, 3] = up(inertia)
+        nb.tag.copy_(up(tags))
+        nb.uid.copy_(torch.arange(n, dtype=torch.int32, device=dev))
+        self._buf = nb
+        self._alt = _Buffers(n, dev)
+        self.atom_type_host = types
+        self.mask_host = np.ones(n, dtype=np.int32)
+        self.nlocal = n
+        self._uid_cache = None
+        self.max_radius = float(rad.max()) if n else 0.0
         for cb in self._listeners:
             cb()
 

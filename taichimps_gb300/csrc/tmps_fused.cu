@@ -1261,6 +1261,8 @@ __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps
         if (servo_now) {
             servo_chain_warp(sb, ssv, se, tot, snew);
             if (lane == 0 && snew.bad) atomicOr(status, TMPS_STATUS_BOX_NONPOSITIVE);
+            if (se.plog != nullptr && se.plog_len > 0 && lane < 6)
+                se.plog[(size_t)(s % se.plog_len) * 6 + lane] = ssv.pressure[lane];
         }
     }
     __syncthreads();
@@ -1413,6 +1415,12 @@ __global__ void __launch_bounds__(kBlockA) k_settle(tmps_atoms a, const tmps_box
     st4(a.xr, i, x);
     st4(a.vm, i, v);
     st4(a.om, i, w);
+}
+
+__global__ void k_set_log(tmps_engine* e, double* log, int32_t len) {
+    if (threadIdx.x || blockIdx.x) return;
+    e->plog = log;
+    e->plog_len = log ? len : 0;
 }
 
 __global__ void k_settle_flags(tmps_box* b, tmps_engine* e) {
@@ -1605,6 +1613,24 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
     const int g = n > 0 ? grid_for(n, kBlockA) : 1;
     k_bounds<<<g, kBlockA, 0, (cudaStream_t)stream>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, cull ? 1 : 0, flags,
                                                        gap, agap);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void* stream) {
+    if (!d_eng || (h_log && len < 1)) return TMPS_ERR_BAD_ARG;
+    double* dptr = nullptr;
+    if (h_log) {
+        // only page-locked host memory the device can address
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, h_log) != cudaSuccess || at.type != cudaMemoryTypeHost ||
+            at.devicePointer == nullptr) {
+            (void)cudaGetLastError();
+            return TMPS_ERR_BAD_ARG;
+        }
+        dptr = (double*)at.devicePointer;
+    }
+    k_set_log<<<1, 1, 0, (cudaStream_t)stream>>>(d_eng, dptr, len);
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }

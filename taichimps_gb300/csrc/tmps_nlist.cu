@@ -106,16 +106,34 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(int m, const int32_t* __re
     }
 }
 
-// Gather every per-atom array into the new order; store x0 for the skin check.
+// Gather every per-atom array into the new order; store x0 for the skin check
+// and, when `off32` is given, each position as an FP32 offset from the origin
+// lo + c h of its own cell (h = prd / g), radius in .w, for the build's
+// prefilter.
 __global__ void __launch_bounds__(kBlock) k_permute(tmps_atoms src, tmps_atoms dst,
+                                                    const tmps_box* __restrict__ b,
                                                     const int32_t* __restrict__ order,
                                                     const int32_t* __restrict__ old_cell,
-                                                    int32_t* cell_of) {
+                                                    int32_t* cell_of, float4* __restrict__ off32) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = src.n;
     if (p >= n) return;
     int i = order[p];
     double4 x = ld4(src.xr, i);
+    if (off32) {
+        const int gx = b->g[0], gxy = b->g[0] * b->g[1];
+        const int lin = old_cell[i];
+        const int cz = lin / gxy, cy = (lin - cz * gxy) / gx, cx = lin - cz * gxy - cy * gx;
+        const int cc[3] = {cx, cy, cz};
+        const double xx[3] = {x.x, x.y, x.z};
+        float o[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double h = b->prd[k] / (double)b->g[k];
+            o[k] = (float)(xx[k] - (b->lo[k] + (double)cc[k] * h));
+        }
+        off32[p] = make_float4(o[0], o[1], o[2], (float)x.w);
+    }
     st4(dst.xr, p, x);
     st4(dst.vm, p, ld4(src.vm, i));
     st4(dst.om, p, ld4(src.om, i));
@@ -139,11 +157,21 @@ __global__ void __launch_bounds__(kBlock) k_permute(tmps_atoms src, tmps_atoms d
 // The full list.  Stencil order and wrap/skip rules of neighbor.py:329-351;
 // the cut test is done with explicit round-to-nearest operations so no
 // multiply-add contraction can move a pair across the cut.
+//
+// With `off32` (and every periodic dimension at least 3 cells wide) each
+// candidate first meets an FP32 prefilter on cell-local offsets: a pair
+// within the cut lies in adjacent cells, so its separation is exactly
+// (o_i - o_j) - offset * h, which FP32 carries to ~1e-6 of (h + |o|).  A
+// candidate is dropped only when its FP32 distance exceeds the cut by more
+// than ten times that error bound; every other candidate gets the exact FP64
+// test, so the list is the same pair set the FP64 test alone gives, at a
+// fraction of the FP64 work (this part's FP64 pipe is ~70x narrower than its
+// FP32 pipe, and the exact test divides).
 __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* __restrict__ b,
                                                   double skin, const int32_t* __restrict__ cell_of,
                                                   const int32_t* __restrict__ rank,
                                                   const int32_t* __restrict__ start, tmps_nlist nl,
-                                                  int32_t* status) {
+                                                  const float4* __restrict__ off32, int32_t* status) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = a.n;
     if (p >= n) return;
@@ -153,6 +181,19 @@ __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* 
     const int cz = lin / gxy, cy = (lin - cz * gxy) / gx, cx = lin - cz * gxy - cy * gx;
     const double4 xi = ld4(a.xr, p);
     const double prd[3] = {b->prd[0], b->prd[1], b->prd[2]};
+    const bool pre = off32 != nullptr && !(px == 1 && gx < 3) && !(py == 1 && gy < 3) && !(pz == 1 && gz < 3);
+    float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+    float h32[3] = {0.f, 0.f, 0.f}, hsum = 0.f, mi = 0.f;
+    const float skin32 = (float)skin;
+    if (pre) {
+        oi = off32[p];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            h32[k] = (float)(prd[k] / (double)b->g[k]);
+            hsum += h32[k];
+        }
+        mi = fmaxf(fmaxf(fabsf(oi.x), fabsf(oi.y)), fabsf(oi.z));
+    }
     int count = 0;
     bool overflow = false;
     for (int ox = -1; ox <= 1; ++ox)
@@ -168,8 +209,18 @@ __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* 
                 const int r = rank[nx + ny * gx + nz * gxy];
                 const int code = (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1);
                 const int beg = start[r], end = start[r + 1];
+                const float fx = (float)ox * h32[0], fy = (float)oy * h32[1], fz = (float)oz * h32[2];
                 for (int q = beg; q < end; ++q) {
                     if (q == p) continue;
+                    if (pre) {
+                        const float4 oj = off32[q];
+                        const float dx = (oi.x - oj.x) - fx, dy = (oi.y - oj.y) - fy, dz = (oi.z - oj.z) - fz;
+                        const float rq = (dx * dx + dy * dy) + dz * dz;
+                        const float mj = fmaxf(fmaxf(fabsf(oj.x), fabsf(oj.y)), fabsf(oj.z));
+                        const float cut = (oi.w + oj.w) + skin32;
+                        const float lim = cut + 1e-5f * (((hsum + mi) + mj) + cut);
+                        if (!(rq < lim * lim) && rq == rq) continue;  // out of reach (a NaN goes on to the exact test)
+                    }
                     const double4 xj = ld4(a.xr, q);
                     double d[3] = {__dsub_rn(xi.x, xj.x), __dsub_rn(xi.y, xj.y), __dsub_rn(xi.z, xj.z)};
 #pragma unroll
@@ -239,9 +290,9 @@ extern "C" {
 
 int64_t tmps_nlist_workspace_bytes(int32_t n, int32_t ncell) {
     if (n < 0 || ncell < 0) return -1;
-    // count[ncell], start[ncell+1], fill[ncell], old_cell[n]
+    // count[ncell], start[ncell+1], fill[ncell], old_cell[n], off32[n]
     return (int64_t)(align256((size_t)ncell * 4) + align256((size_t)(ncell + 1) * 4) +
-                     align256((size_t)ncell * 4) + align256((size_t)n * 4));
+                     align256((size_t)ncell * 4) + align256((size_t)n * 4) + align256((size_t)n * 16));
 }
 
 int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_box* d_box,
@@ -266,6 +317,8 @@ int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_bo
     int32_t* fill = (int32_t*)w;
     w += align256((size_t)m * 4);
     int32_t* old_cell = (int32_t*)w;
+    w += align256((size_t)n * 4);
+    float4* off32 = (float4*)w;
 
     if (cudaMemsetAsync(count, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
     if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
@@ -274,8 +327,8 @@ int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_bo
     k_scan<<<1, kScanBlock, 0, s>>>(count, start, m);
     k_scatter<<<gb, kBlock, 0, s>>>(n, cell_rank, old_cell, start, fill, order);
     k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
-    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, order, old_cell, cell_of);
-    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, d_status);
+    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, d_box, order, old_cell, cell_of, off32);
+    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, off32, d_status);
     note_launches(6);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
@@ -360,8 +413,8 @@ extern "C" int tmps_nlist_build_noalloc(const tmps_atoms* src, const tmps_atoms*
     k_scan<<<1, kScanBlock, 0, s>>>(count, start, m);
     k_scatter<<<gb, kBlock, 0, s>>>(n, cell_rank, old_cell, start, fill, order);
     k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
-    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, order, old_cell, cell_of);
-    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, d_status);
+    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, d_box, order, old_cell, cell_of, nullptr);
+    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, nullptr, d_status);
     note_launches(6);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }

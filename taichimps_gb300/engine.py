@@ -148,6 +148,10 @@ class FusedEngine:
             sv.nsteps, sv.nsteps_total, sv.step_count, sv.nevery = fx.nsteps, fx.nsteps_total, fx.step_count, fx.nevery
             _device.push_struct(fx._dservo, sv)
         self._prepare()
+        log = self.deform.pressure_log if self.deform is not None else None
+        rc = _device.lib().tmps_fused_pressure_log(self._eng.data_ptr(), None if log is None else log.data_ptr(),
+                                                   0 if log is None else len(log), _device.stream())
+        _lib.check(rc, "tmps_fused_pressure_log")
         if self.mixed:
             # the setup forces (FP64) seed the first half-kick
             b = atom.buffers

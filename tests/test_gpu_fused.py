@@ -182,3 +182,28 @@ def test_contact_bound_culling_is_exact(gpu, oracle, precision):
     assert culled[1][1] == 0
     for k in ("x", "v", "omega", "f", "torque"):
         np.testing.assert_array_equal(states[0][k], states[1][k])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pressure_record_each_step(gpu, oracle, precision):
+    """record_pressure: every fused step writes the servo's pressure tensor to pinned host memory; the
+    ring holds the last steps, the final row is the servo's own, and each row matches the oracle's
+    pressure after that many steps."""
+    rng = np.random.default_rng(4)
+    x, r = dense_packing(rng, 343, 7.6, 0.48, 0.56)
+    deform = dict(axes={d: {"style": "pressure", "ptarget": 1.0, "pgain": 1e-3} for d in "xyz"}, couple="xyz",
+                  max_rate=1e-1, remap="x")
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [7.6] * 3, pair="hertz/history", dt=5e-5,
+                          cundall=(0.7, 0.7), deform=deform)
+    sim.precision = precision
+    fix = sim.fixes[-1]
+    fix.record_pressure(8)
+    sim.run(70)
+    rows = fix.pressure_history(range(63, 71))
+    np.testing.assert_array_equal(rows[-1], fix.last_pressure())
+    assert np.isfinite(rows).all() and np.abs(rows).max() > 0
+    tol = 1e-10 if precision == "fp64" else MIXED_P
+    osim.run(62)
+    for k, s in enumerate(range(63, 71)):
+        osim.step()
+        assert rel_err(rows[k], osim.last_pressure) < tol, (s, rel_err(rows[k], osim.last_pressure))
