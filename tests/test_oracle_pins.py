@@ -6,17 +6,23 @@ with the reference's inputs and tolerances, so that the oracle the GPU path is
 checked against is itself checked before it is trusted.
 """
 
+import json
 import math
+from pathlib import Path
 
 import numpy as np
 import pytest
 
+# literal inputs and expected values of the reference's tests (tests/golden/make_known_answers.py)
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "known_answers.json").read_text())["cases"]
+
 
 def _two_sphere_hooke(O):
-    dom = O.OracleDomain.make([-10.0] * 3, [10.0] * 3, ("f", "f", "f"))
-    atoms = O.OracleAtoms(x=[[0.0, 0.0, 0.0], [1.9, 0.0, 0.0]], v=[[0.1, 0, 0], [-0.1, 0, 0]],
-                          radius=[1.0, 1.0], density=[1000.0, 1000.0], tag=[1, 2])
-    nl = O.OracleNeighbor(dom, skin=0.2, max_neighbors=10)
+    c = GOLDEN["hooke_normal_contact"]
+    d, p = c["domain"], c["particles"]
+    dom = O.OracleDomain.make(d["boxlo"], d["boxhi"], tuple(d["boundary"]))
+    atoms = O.OracleAtoms(x=p["x"], v=p["v"], radius=p["radius"], density=p["density"], tag=p["tag"])
+    nl = O.OracleNeighbor(dom, skin=c["skin"], max_neighbors=10)
     nl.build(atoms)
     hist = O.OracleHistory(10)
     hist.restore_state(atoms, nl)
@@ -26,12 +32,13 @@ def _two_sphere_hooke(O):
 def test_hooke_known_answer(oracle):
     """tests/test_hooke.py:16-55: F = 4288.790204786391 (LAMMPS-verified), rtol 1e-12."""
     O = oracle
+    c = GOLDEN["hooke_normal_contact"]
     dom, atoms, nl, hist = _two_sphere_hooke(O)
-    pair = O.OraclePair("hooke", kn=1000.0, gamman=10.0, kt=0.0, gammat=0.0, xmu=0.0, dampflag=0)
-    pair.compute(atoms, nl, hist, dom, dt=0.001)
-    expected = 4288.790204786391
-    np.testing.assert_allclose(atoms.f[0], [-expected, 0.0, 0.0], rtol=1e-12)
-    np.testing.assert_allclose(atoms.f[1], [expected, 0.0, 0.0], rtol=1e-12)
+    pair = O.OraclePair("hooke", **c["pair"])
+    pair.compute(atoms, nl, hist, dom, dt=c["dt"])
+    fx0, fx1 = c["expected_fx"]
+    np.testing.assert_allclose(atoms.f[0], [fx0, 0.0, 0.0], rtol=c["rtol"])
+    np.testing.assert_allclose(atoms.f[1], [fx1, 0.0, 0.0], rtol=c["rtol"])
 
 
 def _random_packing(rng, n=60, box=6.0):
@@ -123,12 +130,15 @@ def test_pbc_wrap(oracle):
     """tests/test_domain_neighbor.py:15-31: 10.5 -> 0.5, -0.2 -> 9.8."""
     import ctypes
     O = oracle
-    dom = O.OracleDomain.make([0.0] * 3, [10.0] * 3)
-    x = np.array([[10.5, -0.2, 5.0]])
+    c = GOLDEN["pbc_wrap"]
+    d = c["domain"]
+    dom = O.OracleDomain.make(d["boxlo"], d["boxhi"], tuple(d["boundary"]))
+    x = np.array(c["particles"]["x"], dtype=np.float64)
     v = np.zeros((1, 3))
     O.lib().or_pbc(ctypes.byref(dom.cbox()), 1, O._p(x), O._p(v))
     assert 0.0 <= x[0, 0] < 10.0 and 0.0 <= x[0, 1] < 10.0
-    assert np.isclose(x[0, 0], 0.5) and np.isclose(x[0, 1], 9.8)
+    for k, val in c["expected"].items():
+        assert np.isclose(x[0, int(k)], val)
 
 
 def test_neighbor_list_and_skin_trigger(oracle):
