@@ -293,6 +293,13 @@ int tmps_contact(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
                  const tmps_pair_params* p, double dt, int32_t shearupdate, int32_t accumulate,
                  void* stream);
 
+/* ComputeContactAtom.compute (src/taichimps/computes/contact_atom.py:21-63):
+ * per atom (internal order) into d_count (device int32[n]) the number of
+ * neighbors with rsq < (ri + rj)^2 and rsq > 1e-18, each contact counted for
+ * both partners (the coordination number). */
+int tmps_contact_count(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, int32_t* d_count,
+                       void* stream);
+
 /* ---- virial, pressure servo, remap ------------------------------------- */
 
 /* Computes.compute_virial_kernel (src/taichimps/computes/thermo.py:62-109):

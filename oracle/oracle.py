@@ -252,6 +252,15 @@ class OracleNeighbor:
         return bool(lib().or_skin_check(atoms.n, _p(atoms.x), _p(self.x0),
                                         ctypes.c_double(0.25 * self.skin * self.skin)))
 
+    def contact_count(self, atoms: OracleAtoms) -> np.ndarray:
+        """ComputeContactAtom.compute (computes/contact_atom.py:21-63): per-atom contact counts."""
+        out = np.zeros(atoms.n, dtype=np.int32)
+        if atoms.n:
+            lib().or_contact_count(ctypes.byref(self.domain.cbox()), atoms.n, _p(atoms.x), _p(atoms.radius),
+                                   self.max_nb, _p(self.num_neighbors, _i32p), _p(self.neighbors, _i32p),
+                                   _p(out, _i32p))
+        return out
+
     def pair_set(self, tags: np.ndarray) -> set[tuple[int, int]]:
         """The built half list as a set of (tag_i, tag_j) with tag_i < tag_j."""
         out = set()

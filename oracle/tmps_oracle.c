@@ -275,6 +275,27 @@ int or_build_pair_list(int n, int max_nb, const int32_t* num_neighbors, const in
 
 /* NeighborList.check_displacement (neighbor.py:214-245): 1 when any atom
  * moved more than half the skin since x0 was stored. */
+/* ComputeContactAtom.compute_kernel (computes/contact_atom.py:21-52): over the
+ * half list, every pair with rsq < (ri + rj)^2 and rsq > 1e-18 counts for both
+ * of its atoms. */
+void or_contact_count(const or_box_t* b, int n, const double* x, const double* radius, int max_nb,
+                      const int32_t* num_neighbors, const int32_t* neighbors, int32_t* count) {
+    for (int i = 0; i < n; ++i) count[i] = 0;
+    for (int i = 0; i < n; ++i) {
+        for (int k = 0; k < num_neighbors[i]; ++k) {
+            const int j = neighbors[(size_t)i * max_nb + k];
+            double d[3] = {x[3 * i] - x[3 * j], x[3 * i + 1] - x[3 * j + 1], x[3 * i + 2] - x[3 * j + 2]};
+            min_image(b, d);
+            const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+            const double radsum = radius[i] + radius[j];
+            if (rsq < radsum * radsum && rsq > 1e-18) {
+                count[i] += 1;
+                count[j] += 1;
+            }
+        }
+    }
+}
+
 int or_skin_check(int n, const double* x, const double* x0, double trigger_sq) {
     int hit = 0;
 #pragma omp parallel for if (g_nthreads > 1) reduction(| : hit)

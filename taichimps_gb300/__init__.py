@@ -5,7 +5,7 @@ API (pair / fix / neighbor / history / compute classes driven by Simulation).
 """
 
 from .atom import AtomSystem
-from .computes import Computes
+from .computes import ComputeContactAtom, Computes
 from .contact_history import ContactHistory
 from .domain import Domain
 from .EXTRA_FIX import Fix, FixDampingCundall, FixDeformPressure, FixNVESphere
@@ -13,6 +13,6 @@ from .GRANULAR import GranHertz, GranHertzHistory, GranHooke, GranHookeHistory, 
 from .neighbor import NeighborList
 from .simulation import Simulation
 
-__all__ = ["AtomSystem", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
+__all__ = ["AtomSystem", "ComputeContactAtom", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
            "FixDeformPressure", "FixNVESphere", "GranHertz", "GranHertzHistory", "GranHooke",
            "GranHookeHistory", "GranularPair", "PairGranular", "NeighborList", "Simulation"]

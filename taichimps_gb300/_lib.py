@@ -126,6 +126,7 @@ _SIGS = {
     "tmps_history_remap": (c_i32, [ctypes.POINTER(NList), ctypes.POINTER(NList), c_vp, c_vp]),
     "tmps_contact": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp,
                              ctypes.POINTER(PairParams), c_f64, c_i32, c_i32, c_vp]),
+    "tmps_contact_count": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp, c_vp]),
     "tmps_virial_reduce": (c_i32, [ctypes.POINTER(Atoms), c_i32, c_vp, c_vp, ctypes.c_int64, c_vp]),
     "tmps_virial_workspace_bytes": (ctypes.c_int64, [c_i32]),
     "tmps_servo_step": (c_i32, [c_vp, c_vp, c_vp, c_f64, c_f64, c_f64, c_vp, c_vp]),

@@ -1,3 +1,4 @@
+from .contact_atom import ComputeContactAtom
 from .thermo import BOLTZMANN, Computes, virial_chunks
 
-__all__ = ["Computes", "virial_chunks", "BOLTZMANN"]
+__all__ = ["Computes", "ComputeContactAtom", "virial_chunks", "BOLTZMANN"]

@@ -144,9 +144,55 @@ bool params_ok(const tmps_pair_params* p) {
     return true;
 }
 
+// ComputeContactAtom.compute_kernel (computes/contact_atom.py:21-52): the
+// number of neighbors in geometric contact, rsq < (ri + rj)^2 and rsq > 1e-18,
+// each contact counted for both partners.  On the full list every atom counts
+// its own row; d = x_i - x_j is the exact negation of the partner's, so both
+// sides see the same rsq.
+__global__ void __launch_bounds__(kBlock) k_contact_count(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B,
+                                                          int32_t* __restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = A.n;
+    if (i >= n) return;
+    double prd[3];
+    int per[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        prd[k] = B->prd[k];
+        per[k] = B->per[k];
+    }
+    const double4 xi = ld4(A.xr, i);
+    const int nn = L.nnb[i];
+    int c = 0;
+    for (int k = 0; k < nn; ++k) {
+        const double4 xj = ld4(A.xr, L.nbr[(size_t)k * n + i] & kNbrIndexMask);
+        // Domain.minimum_image (domain.py:481-486) and the dot product, with
+        // explicit round-to-nearest operations: an integer result admits no
+        // contraction that could move a pair across the threshold
+        double d[3] = {__dsub_rn(xi.x, xj.x), __dsub_rn(xi.y, xj.y), __dsub_rn(xi.z, xj.z)};
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            if (per[q] == 1) d[q] = __dsub_rn(d[q], __dmul_rn(prd[q], round(__ddiv_rn(d[q], prd[q]))));
+        const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+        const double radsum = __dadd_rn(xi.w, xj.w);
+        if (rsq < __dmul_rn(radsum, radsum) && rsq > 1e-18) ++c;
+    }
+    count[i] = c;
+}
+
 }  // namespace
 
 extern "C" {
+
+int tmps_contact_count(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, int32_t* d_count,
+                       void* stream) {
+    if (!a || !nl || !d_box || !d_count || a->n < 0 || nl->n != a->n) return TMPS_ERR_BAD_ARG;
+    if (nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
+    if (a->n == 0) return TMPS_OK;
+    k_contact_count<<<grid_for(a->n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(*a, *nl, d_box, d_count);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
 
 int tmps_contact(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box,
                  const tmps_pair_params* p, double dt, int32_t shearupdate, int32_t accumulate,

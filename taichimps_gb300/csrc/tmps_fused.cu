@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
 // virial partials depend only on the flag words and the grid, not on
 // scheduling; the kinetic term of an unflagged atom is A's.
 template <int STYLE, bool MIXED>
-__global__ void __launch_bounds__(kBlockC)
+__global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
     k_cf(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
          tmps_engine* __restrict__ E, uint32_t* __restrict__ flags, const float* __restrict__ gap,
          const float* __restrict__ agap, double* __restrict__ part) {
@@ -556,6 +556,19 @@ __global__ void __launch_bounds__(kBlockC)
         __syncwarp();
             const int nn = mine ? L.nnb[i] : 0;
             const uint64_t touch = (hist && mine) ? L.touch[i] : 0ull;
+            // the row atom's own velocities (Cundall, kinetic term), issued with its row length
+            T rv[3] = {0, 0, 0}, rw[3] = {0, 0, 0}, rm = 0;
+            if (mine) {
+                if constexpr (MIXED) {
+                    const float4 v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
+                    rv[0] = v.x; rv[1] = v.y; rv[2] = v.z; rm = v.w;
+                    rw[0] = w.x; rw[1] = w.y; rw[2] = w.z;
+                } else {
+                    const double4 v = ld4(A.vm, i), w = ld4(A.om, i);
+                    rv[0] = v.x; rv[1] = v.y; rv[2] = v.z; rm = v.w;
+                    rw[0] = w.x; rw[1] = w.y; rw[2] = w.z;
+                }
+            }
             int incl = nn;
     #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -585,17 +598,46 @@ __global__ void __launch_bounds__(kBlockC)
                     const int e = L.nbr[(size_t)k * n + ia];
                     const int j = e & kNbrIndexMask;
                     const bool lo = ia < j;
+                    const bool was = k < 32 ? ((tlo >> k) & 1u) : ((thi >> (k - 32)) & 1u);
+                    const size_t so = (size_t)k * n + ia;
+                    // every load of the entry at once, whether or not it turns out to touch:
+                    // one round trip after the row entry instead of three
                     T xi[3], xj[3], ri, rj;
-                    int32_t ci = 0;
+                    int32_t ci = 0, cj = 0;
+                    float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
+                    T vi[3], wi[3], mi, vj[3], wj[3], mj;
+                    double shr[3] = {0, 0, 0};
                     if constexpr (MIXED) {
                         const float4 pi = ld4f(A.pos32, ia), pj = ld4f(A.pos32, j);
+                        il = ld4f(A.pos32lo, ia);
+                        jl = ld4f(A.pos32lo, j);
+                        const float4 v = ld4f(A.vel32, ia), w = ld4f(A.om32, ia);
+                        const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
+                        if (vremap) {
+                            ci = A.cell32[ia];
+                            cj = A.cell32[j];
+                        }
                         xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
                         xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
-                        if (vremap) ci = A.cell32[ia];
+                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
                     } else {
                         const double4 pi = ld4(A.xr, ia), pj = ld4(A.xr, j);
+                        const double4 v = ld4(A.vm, ia), w = ld4(A.om, ia);
+                        const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
                         xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
                         xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+                    }
+                    if (hist && was) {
+                        shr[0] = L.shear[so];
+                        shr[1] = L.shear[ss + so];
+                        shr[2] = L.shear[2 * ss + so];
                     }
                     // separation x_i - x_j
                     T d[3];
@@ -615,7 +657,6 @@ __global__ void __launch_bounds__(kBlockC)
                             }
                         }
                         if (vremap) {  // image count for the partner velocity shift
-                            const int32_t cj = A.cell32[j];
                             const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
                                                cell_z(ci) + off[2] - cell_z(cj)};
     #pragma unroll
@@ -646,7 +687,6 @@ __global__ void __launch_bounds__(kBlockC)
                             // separation, |d|^2, |d| and the overlap from the high and
                             // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
                             // FP32 difference of two unit-size numbers keeps 2^-24)
-                            const float4 il = ld4f(A.pos32lo, ia), jl = ld4f(A.pos32lo, j);
                             const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
                             float dh[3], dl[3];
     #pragma unroll
@@ -712,22 +752,6 @@ __global__ void __launch_bounds__(kBlockC)
                     }
                     if (near) {
                         contact = true;
-                        T vi[3], wi[3], mi, vj[3], wj[3], mj;
-                        if constexpr (MIXED) {
-                            const float4 v = ld4f(A.vel32, ia), w = ld4f(A.om32, ia);
-                            const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
-                            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                            vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                            wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-                        } else {
-                            const double4 v = ld4(A.vm, ia), w = ld4(A.om, ia);
-                            const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
-                            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                            vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                            wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-                        }
                         T dv[3] = {0, 0, 0};
                         if (vremap) {
                             // image count of x_a - x_b, then n . h_rate for partner b
@@ -748,13 +772,11 @@ __global__ void __launch_bounds__(kBlockC)
                             in.wb[c] = lo ? wj[c] : wi[c];
                         }
                         double sh[3] = {0, 0, 0};
-                        const size_t so = (size_t)k * n + ia;
-                        const bool was = k < 32 ? ((tlo >> k) & 1u) : ((thi >> (k - 32)) & 1u);
                         if (hist && was) {
                             const double sgd = lo ? 1.0 : -1.0;
-                            sh[0] = sgd * L.shear[so];
-                            sh[1] = sgd * L.shear[ss + so];
-                            sh[2] = sgd * L.shear[2 * ss + so];
+                            sh[0] = sgd * shr[0];
+                            sh[1] = sgd * shr[1];
+                            sh[2] = sgd * shr[2];
                         }
                         PairOut<T> out;
                         contact_law<T, STYLE>(P, dt, 1, in, sh, out);
@@ -807,16 +829,9 @@ __global__ void __launch_bounds__(kBlockC)
             }
             if (mine) {
                 if (hist && newtouch != touch) L.touch[i] = newtouch;
-                T vi[3], wi[3], mi;
-                if constexpr (MIXED) {
-                    const float4 v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
-                    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                    wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                } else {
-                    const double4 v = ld4(A.vm, i), w = ld4(A.om, i);
-                    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                    wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                }
+                const T* vi = rv;
+                const T* wi = rw;
+                const T mi = rm;
                 if (E->cundall) {  // FixDampingCundall.post_force_kernel
                     T gl, ga;
                     if constexpr (MIXED) {

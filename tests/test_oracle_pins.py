@@ -273,3 +273,25 @@ def test_pair_antisymmetry_all_styles(oracle):
         assert np.abs(res[0][0]).max() > 0.0
         for a, b in zip(res[0], res[1]):
             np.testing.assert_array_equal(a, b)
+
+
+def test_contact_count_brute_force(oracle):
+    """computes/contact_atom.py:21-52 restated in the oracle: the per-atom contact counts equal an
+    all-pairs count with the minimum image (each contact counted for both partners)."""
+    O = oracle
+    rng = np.random.default_rng(12)
+    box = 6.0
+    x = _random_packing(rng, n=64, box=box)
+    r = rng.uniform(0.7, 0.85, size=len(x))
+    dom = O.OracleDomain.make([0.0] * 3, [box] * 3)
+    atoms = O.OracleAtoms(x=x, radius=r, density=2.5)
+    nl = O.OracleNeighbor(dom, skin=0.1, max_neighbors=32)
+    nl.build(atoms)
+    got = nl.contact_count(atoms)
+    d = x[:, None, :] - x[None, :, :]
+    d -= box * np.where(np.abs(d / box) % 1 == 0.5, np.sign(d / box) * np.ceil(np.abs(d / box)), np.round(d / box))
+    rsq = (d ** 2).sum(-1)
+    rs = r[:, None] + r[None, :]
+    want = ((rsq < rs * rs) & (rsq > 1e-18)).sum(1)
+    assert got.sum() > 0
+    np.testing.assert_array_equal(got, want)
