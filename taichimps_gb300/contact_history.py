@@ -36,6 +36,7 @@ class ContactHistory:
         self._synced_build = -1     # build_count of the list this history belongs to
         self._saved_build = None    # build_count at save_state()
         self._nlist = None
+        self._restart = None        # records from load_restart, applied at the next build
 
     def _alloc(self, n: int, slots: int) -> None:
         if self._shape == (n, slots):
@@ -75,6 +76,11 @@ class ContactHistory:
     def restore_state(self, atom, nlist) -> None:
         """Carry the saved contacts onto the freshly built list (contact_history.py:147-154)."""
         if atom.nlocal == 0:
+            return
+        if self._restart is not None:
+            self._apply_restart(atom, nlist)
+            self._saved_build = None
+            self.setup_pending = False
             return
         carried = (self._saved_build is not None and nlist.build_count == self._saved_build + 1
                    and self._shape == (nlist._n, nlist.slots))
@@ -127,8 +133,9 @@ class ContactHistory:
     def shear_pairs(self):
         return _Array(self._pairs()[2])
 
-    def touching_by_atom(self, nlist, nlocal: int) -> list[list[tuple[int, np.ndarray]]]:
-        """Touching contacts of each atom as (partner tag, shear), both sides (restart form)."""
+    def _touching_slots(self, nlist):
+        """Every touching slot as arrays (row p, slot k, partner q) in internal order, with uid, tag
+        and the shear array on the host."""
         self.ensure(nlist)
         atom = nlist._atom
         nbr, nnb = nlist.full_rows()
@@ -136,19 +143,92 @@ class ContactHistory:
         tag = atom.buffers.tag.cpu().numpy()
         touch = self.touch.cpu().numpy().view(np.uint64)
         sh = self.shear.cpu().numpy()
+        S = nbr.shape[0]
+        bits = (touch[None, :] >> np.arange(S, dtype=np.uint64)[:, None]) & np.uint64(1)
+        live = (bits == 1) & (np.arange(S)[:, None] < nnb[None, :])
+        kk, pp = np.nonzero(live)
+        order = np.lexsort((kk, uid[pp]))  # by row atom (insertion order), then slot
+        kk, pp = kk[order], pp[order]
+        qq = nbr[kk, pp]
+        return pp, kk, qq, uid, tag, sh
+
+    def touching_by_atom(self, nlist, nlocal: int) -> list[list[tuple[int, np.ndarray]]]:
+        """The touching contacts of each local atom as (partner tag, shear), one entry per contact,
+        under its lower-index atom in that atom's i->j sense (contact_history.py:155-174): what the
+        reference's half list holds, for write_restart to expand into LAMMPS' both-sided records."""
+        pp, kk, qq, uid, tag, sh = self._touching_slots(nlist)
         out: list[list[tuple[int, np.ndarray]]] = [[] for _ in range(nlocal)]
-        for p in range(atom.nlocal):
-            for k in range(nnb[p]):
-                if (int(touch[p]) >> k) & 1 and uid[p] < nlocal:
-                    out[uid[p]].append((int(tag[nbr[k, p] & NBR_INDEX_MASK]), sh[:, k, p].copy()))
+        for p, k, q in zip(pp, kk, qq):
+            if uid[p] < uid[q] and uid[p] < nlocal:
+                out[uid[p]].append((int(tag[q]), sh[:, k, p].copy()))
         return out
 
     def contacts_by_tag(self, nlist) -> dict[tuple[int, int], np.ndarray]:
         """{(tag_i, tag_j): shear in the i->j sense} for every touching slot (both sides)."""
-        out = {}
-        for i_rows in [self.touching_by_atom(nlist, nlist._atom.nlocal)]:
-            tags = nlist._atom.tag.to_numpy()
-            for u, row in enumerate(i_rows):
-                for t, s in row:
-                    out[(int(tags[u]), t)] = s
-        return out
+        pp, kk, qq, uid, tag, sh = self._touching_slots(nlist)
+        return {(int(tag[p]), int(tag[q])): sh[:, k, p].copy() for p, k, q in zip(pp, kk, qq)}
+
+    def load_restart(self, partner_tags: list, values: list) -> None:
+        """Seed the history from a restart file, keyed by partner tag (contact_history.py:176-214,
+        the counterpart of FixNeighHistory::unpack_restart).  Entry i belongs to the i-th atom handed
+        to AtomSystem.add_particles; each record is in that atom's i->j sense (LAMMPS stores every
+        contact under both partners, the second copy negated).  The first neighbor build of the run
+        puts the values onto the list: a contact is restored from its lower-index atom's record, as
+        the reference's half list does, and its other copy is set to the exact negative."""
+        n = min(len(partner_tags), self.max_atoms)
+        us, ts, vs = [], [], []
+        for i in range(n):
+            t = np.asarray(partner_tags[i], dtype=np.int64).reshape(-1)
+            m = len(t)
+            if m > self.max_neighbors:
+                raise ValueError(f"atom {i} has {m} stored contacts but the history only "
+                                 f"has {self.max_neighbors} slots per atom")
+            w = np.zeros((m, 3))
+            if m:
+                v = np.asarray(values[i], dtype=np.float64).reshape(m, -1)
+                w[:, :min(3, v.shape[1])] = v[:, :3]
+            us.append(np.full(m, i, dtype=np.int64))
+            ts.append(t)
+            vs.append(w)
+        cat = lambda a, shape: np.concatenate(a) if a else np.zeros(shape)
+        self._restart = (cat(us, 0).astype(np.int64), cat(ts, 0).astype(np.int64), cat(vs, (0, 3)))
+        self.setup_pending = True
+
+    def _apply_restart(self, atom, nlist) -> None:
+        """Put loaded restart records onto the freshly built list (see load_restart)."""
+        u_file, t_file, v_file = self._restart
+        self._restart = None
+        self._alloc(nlist._n, nlist.slots)
+        self.reset()
+        self._synced_build = nlist.build_count
+        if len(u_file) == 0 or atom.nlocal == 0:
+            return
+        nbr, nnb = nlist.full_rows()
+        uid = atom.uid_host()
+        tag = atom.buffers.tag.cpu().numpy().astype(np.int64)
+        S, n = nbr.shape
+        kk, pp = np.nonzero(np.arange(S)[:, None] < nnb[None, :])
+        qq = nbr[kk, pp]
+        own = uid[pp] < uid[qq]
+        ko, po, qo = kk[own], pp[own], qq[own]
+        # look each owned slot up in the file: key (insertion index, partner tag)
+        fkey = (u_file << 32) | t_file
+        order = np.argsort(fkey, kind="stable")
+        fkey_s = fkey[order]
+        skey = (uid[po].astype(np.int64) << 32) | tag[qo]
+        at = np.searchsorted(fkey_s, skey)
+        hit = (at < len(fkey_s)) & (fkey_s[np.minimum(at, len(fkey_s) - 1)] == skey)
+        ko, po, qo, val = ko[hit], po[hit], qo[hit], v_file[order[at[hit]]]
+        # the other copy: row q's slot whose partner is p (slots keyed by row * n + partner)
+        mkey_all = pp.astype(np.int64) * n + qq
+        morder = np.argsort(mkey_all, kind="stable")
+        mk = np.searchsorted(mkey_all[morder], qo.astype(np.int64) * n + po)
+        km = kk[morder[mk]]
+        touch = np.zeros(n, dtype=np.uint64)
+        sh = np.zeros((3, S, n))
+        np.bitwise_or.at(touch, po, np.left_shift(np.uint64(1), ko.astype(np.uint64)))
+        np.bitwise_or.at(touch, qo, np.left_shift(np.uint64(1), km.astype(np.uint64)))
+        sh[:, ko, po] = val.T
+        sh[:, km, qo] = -val.T
+        self.touch.copy_(torch.from_numpy(touch.view(np.int64)))
+        self.shear.copy_(torch.from_numpy(sh))
