@@ -112,6 +112,7 @@ typedef struct tmps_nlist {
     int32_t* nnb;
     uint64_t* touch;
     double* shear;
+    double* rolling;         /* [3][slots][n] rolling displacement, or NULL (no rolling model) */
 } tmps_nlist;
 
 /* Contact law.  style: 0 gran/hooke, 1 gran/hooke/history, 2 gran/hertz,
@@ -126,6 +127,10 @@ typedef struct tmps_pair_params {
     int32_t pad_;
     double kn, kt, gamman, gammat, xmu;
     double damp, xt, mu;
+    /* rolling resistance of pair granular (GRANULAR/rolling.py:16-50): 0 none, 1 epsd */
+    int32_t rolling_id;
+    int32_t pad2_;
+    double k_roll, gamma_roll, mu_roll;
 } tmps_pair_params;
 
 /* Pressure servo / strain control for x, y, z (orthogonal box).

@@ -59,6 +59,8 @@ class OrPair(ctypes.Structure):
         ("normal_id", ctypes.c_int32), ("damping_id", ctypes.c_int32),
         ("tangential_id", ctypes.c_int32),
         ("damp", ctypes.c_double), ("xt", ctypes.c_double), ("mu", ctypes.c_double),
+        ("rolling_id", ctypes.c_int32),
+        ("k_roll", ctypes.c_double), ("gamma_roll", ctypes.c_double), ("mu_roll", ctypes.c_double),
     ]
 
 
@@ -278,6 +280,7 @@ class OracleHistory:
         self.max_nb = int(max_neighbors)
         self.partner = np.full(1, -1, dtype=np.int32)
         self.shear = np.zeros((1, 3))
+        self.rolling = np.zeros((1, 3))   # rolling displacement per pair (contact_history.py:58-59)
         self.setup_pending = False
         self._saved = None
 
@@ -288,10 +291,12 @@ class OracleHistory:
         cnt = np.zeros(n, dtype=np.int32)
         stag = np.zeros((n, self.max_nb), dtype=np.int32)
         ssh = np.zeros((n, self.max_nb, 3))
+        srl = np.zeros((n, self.max_nb, 3))
         if nl.npairs > 0:
             lib().or_history_save(n, nl.npairs, _p(nl.pair_i, _i32p), _p(self.partner, _i32p),
-                                  _p(self.shear), self.max_nb, _p(cnt, _i32p), _p(stag, _i32p), _p(ssh))
-        self._saved = (cnt, stag, ssh)
+                                  _p(self.shear), _p(self.rolling), self.max_nb, _p(cnt, _i32p),
+                                  _p(stag, _i32p), _p(ssh), _p(srl))
+        self._saved = (cnt, stag, ssh, srl)
 
     def restore_state(self, atoms: OracleAtoms, nl: OracleNeighbor) -> None:
         if atoms.n == 0:
@@ -299,16 +304,19 @@ class OracleHistory:
         m = max(nl.npairs, 1)
         self.partner = np.full(m, -1, dtype=np.int32)
         self.shear = np.zeros((m, 3))
+        self.rolling = np.zeros((m, 3))
         if self._saved is None:
             cnt = np.zeros(atoms.n, dtype=np.int32)
             stag = np.zeros((atoms.n, self.max_nb), dtype=np.int32)
             ssh = np.zeros((atoms.n, self.max_nb, 3))
+            srl = np.zeros((atoms.n, self.max_nb, 3))
         else:
-            cnt, stag, ssh = self._saved
+            cnt, stag, ssh, srl = self._saved
         if nl.npairs > 0:
             lib().or_history_restore(nl.npairs, _p(nl.pair_i, _i32p), _p(nl.pair_j, _i32p),
                                      _p(atoms.tag, _i32p), self.max_nb, _p(cnt, _i32p),
-                                     _p(stag, _i32p), _p(ssh), _p(self.partner, _i32p), _p(self.shear))
+                                     _p(stag, _i32p), _p(ssh), _p(srl), _p(self.partner, _i32p),
+                                     _p(self.shear), _p(self.rolling))
         self.setup_pending = False
 
     def touching(self, atoms: OracleAtoms, nl: OracleNeighbor) -> dict[tuple[int, int], np.ndarray]:
@@ -356,7 +364,7 @@ class OraclePair:
             self._granular(**kw)
 
     def _granular(self, normal, normal_coeffs, tangential="none", tangential_coeffs=None,
-                  damping="viscoelastic", limit_damping=False):
+                  damping="viscoelastic", limit_damping=False, rolling="none", rolling_coeffs=None):
         # granular.py:122-269
         nid = {"hooke": 0, "hertz": 1, "hertz/material": 2}[normal]
         did = {"none": 0, "velocity": 1, "mass_velocity": 2, "viscoelastic": 3, "tsuji": 4,
@@ -394,7 +402,13 @@ class OraclePair:
                 P.kt = 8.0 * _mix_g(emod, emod, poiss, poiss)
             else:
                 P.kt = float(k_raw)
-        self.uses_history = tid in (2, 3)
+        # rolling resistance (rolling.py:16-27): coefficients k_roll, gamma_roll, mu_roll
+        if rolling not in ("none", "sds", "epsd"):
+            raise ValueError(f"unknown rolling model {rolling!r}")
+        if rolling != "none":
+            P.rolling_id = 1
+            P.k_roll, P.gamma_roll, P.mu_roll = (float(c) for c in rolling_coeffs)
+        self.uses_history = tid in (2, 3) or rolling != "none"
 
     def compute(self, atoms: OracleAtoms, nl: OracleNeighbor, hist: OracleHistory, dom: OracleDomain,
                 dt: float, shearupdate: bool = True) -> None:
@@ -404,7 +418,7 @@ class OraclePair:
         lib().or_pair_compute(self.sid, ctypes.byref(self.P), ctypes.byref(box), nl.npairs,
                               _p(nl.pair_i, _i32p), _p(nl.pair_j, _i32p), _p(atoms.x), _p(atoms.v),
                               _p(atoms.omega), _p(atoms.radius), _p(atoms.rmass), _p(atoms.tag, _i32p),
-                              _p(hist.partner, _i32p), _p(hist.shear), ctypes.c_double(dt),
+                              _p(hist.partner, _i32p), _p(hist.shear), _p(hist.rolling), ctypes.c_double(dt),
                               1 if shearupdate else 0, _p(atoms.f), _p(atoms.torque), _p(atoms.virial))
 
 

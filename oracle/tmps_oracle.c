@@ -47,6 +47,9 @@ typedef struct {
     /* pair granular (granular.py:122-205): model ids and derived coefficients */
     int32_t normal_id, damping_id, tangential_id;
     double damp, xt, mu;
+    /* rolling resistance (GRANULAR/rolling.py:16-50): 0 none, 1 epsd */
+    int32_t rolling_id;
+    double k_roll, gamma_roll, mu_roll;
 } or_pair_t;
 
 enum { OR_HOOKE = 0, OR_HOOKE_HISTORY = 1, OR_HERTZ = 2, OR_HERTZ_HISTORY = 3, OR_GRANULAR = 4 };
@@ -312,8 +315,8 @@ int or_skin_check(int n, const double* x, const double* x0, double trigger_sq) {
 /* ContactHistory.save_state_kernel (contact_history.py:91-110): compact the
  * touching pairs (partner >= 0) into tag-keyed per-atom buffers. */
 void or_history_save(int n, int npairs, const int32_t* pair_i, const int32_t* partner,
-                     const double* shear, int max_nb, int32_t* save_count, int32_t* save_tag,
-                     double* save_shear) {
+                     const double* shear, const double* rolling, int max_nb, int32_t* save_count,
+                     int32_t* save_tag, double* save_shear, double* save_rolling) {
     for (int i = 0; i < n; ++i) save_count[i] = 0;
     for (int nc = 0; nc < npairs; ++nc) {
         int32_t ptag = partner[nc];
@@ -322,6 +325,8 @@ void or_history_save(int n, int npairs, const int32_t* pair_i, const int32_t* pa
             int m = save_count[i]++;
             save_tag[(size_t)i * max_nb + m] = ptag;
             for (int k = 0; k < 3; ++k) save_shear[((size_t)i * max_nb + m) * 3 + k] = shear[3 * nc + k];
+            if (rolling)
+                for (int k = 0; k < 3; ++k) save_rolling[((size_t)i * max_nb + m) * 3 + k] = rolling[3 * nc + k];
         }
     }
 }
@@ -330,7 +335,8 @@ void or_history_save(int n, int npairs, const int32_t* pair_i, const int32_t* pa
  * partner's tag up in the saved buffer of atom i; copy or zero. */
 void or_history_restore(int npairs, const int32_t* pair_i, const int32_t* pair_j, const int32_t* tag,
                         int max_nb, const int32_t* save_count, const int32_t* save_tag,
-                        const double* save_shear, int32_t* partner, double* shear) {
+                        const double* save_shear, const double* save_rolling, int32_t* partner,
+                        double* shear, double* rolling) {
     for (int nc = 0; nc < npairs; ++nc) {
         int i = pair_i[nc];
         int32_t jtag = tag[pair_j[nc]];
@@ -340,9 +346,12 @@ void or_history_restore(int npairs, const int32_t* pair_i, const int32_t* pair_j
         if (found >= 0) {
             partner[nc] = jtag;
             for (int k = 0; k < 3; ++k) shear[3 * nc + k] = save_shear[((size_t)i * max_nb + found) * 3 + k];
+            if (rolling)
+                for (int k = 0; k < 3; ++k) rolling[3 * nc + k] = save_rolling[((size_t)i * max_nb + found) * 3 + k];
         } else {
             partner[nc] = -1;
             shear[3 * nc] = shear[3 * nc + 1] = shear[3 * nc + 2] = 0.0;
+            if (rolling) rolling[3 * nc] = rolling[3 * nc + 1] = rolling[3 * nc + 2] = 0.0;
         }
     }
 }
@@ -397,14 +406,17 @@ static inline void rotate_rescale(double* vec, const double* n) {
 static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, int i, int j,
                      const double* x, const double* v, const double* om, const double* rad,
                      const double* rmass, const int32_t* tag, int32_t* partner, double* shear,
-                     double dt, int shearupdate, double* f, double* torque, double* virial) {
+                     double* rolling, double dt, int shearupdate, double* f, double* torque,
+                     double* virial) {
     const double* xi = x + 3 * i; const double* xj = x + 3 * j;
     const double* vi = v + 3 * i; const double* vj = v + 3 * j;
     const double* oi = om + 3 * i; const double* oj = om + 3 * j;
     double ri = rad[i], rj = rad[j], mi = rmass[i], mj = rmass[j];
+    int has_rolling = style == OR_GRANULAR && P->rolling_id != 0 && rolling != NULL;
     int has_hist = style == OR_HOOKE_HISTORY || style == OR_HERTZ_HISTORY ||
                    (style == OR_GRANULAR &&
-                    (P->tangential_id == T_LINEAR_HISTORY || P->tangential_id == T_MINDLIN));
+                    (P->tangential_id == T_LINEAR_HISTORY || P->tangential_id == T_MINDLIN)) ||
+                   has_rolling;
 
     double dpos[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
     double dvj[3];
@@ -415,10 +427,11 @@ static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, i
         if (has_hist) {
             partner[nc] = -1;
             shear[3 * nc] = shear[3 * nc + 1] = shear[3 * nc + 2] = 0.0;
+            if (has_rolling) rolling[3 * nc] = rolling[3 * nc + 1] = rolling[3 * nc + 2] = 0.0;
         }
         return;
     }
-    double ftot[3], fs[3], tor[3];
+    double ftot[3], fs[3], tor[3], troll[3] = {0.0, 0.0, 0.0};
     double armi, armj;  /* torque prefactors applied to tor */
 
     if (style != OR_GRANULAR) {
@@ -532,6 +545,8 @@ static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, i
         if (P->limit_damping == 1 && fntot < 0.0) fntot = 0.0;
         double fscrit = P->mu * fabs(fntot);
         fs[0] = fs[1] = fs[2] = 0.0;
+        /* a slot whose partner changed starts from zero history (shear and rolling) */
+        const int fresh = has_hist && partner[nc] != tag[j];
         if (P->tangential_id == T_LINEAR_NOHISTORY) {
             double damp_t = P->xt * dpf;
             double ft = 0.0;
@@ -543,7 +558,7 @@ static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, i
         } else if (P->tangential_id == T_LINEAR_HISTORY || P->tangential_id == T_MINDLIN) {
             int32_t jtag = tag[j];
             double h[3] = {shear[3 * nc], shear[3 * nc + 1], shear[3 * nc + 2]};
-            if (partner[nc] != jtag) {
+            if (fresh) {
                 h[0] = h[1] = h[2] = 0.0;
                 partner[nc] = jtag;
             }
@@ -570,6 +585,28 @@ static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, i
             }
             shear[3 * nc] = h[0]; shear[3 * nc + 1] = h[1]; shear[3 * nc + 2] = h[2];
         }
+        if (has_rolling) {
+            /* RollingResistance.compute_torque (rolling.py:30-50) with omega_rel = omega_i - omega_j,
+             * r_eff the effective radius and fn = |fntot|; the increment only on a history update */
+            double hr[3] = {rolling[3 * nc], rolling[3 * nc + 1], rolling[3 * nc + 2]};
+            if (fresh) {
+                hr[0] = hr[1] = hr[2] = 0.0;
+                partner[nc] = tag[j];
+            }
+            double wrel[3] = {oi[0] - oj[0], oi[1] - oj[1], oi[2] - oj[2]};
+            if (shearupdate != 0)
+                for (int k = 0; k < 3; ++k) hr[k] = hr[k] + wrel[k] * dt;
+            const double tr_mag = P->k_roll * norm3(hr);
+            const double tr_max = (P->mu_roll * reff) * fabs(fntot);
+            for (int k = 0; k < 3; ++k) troll[k] = (-P->k_roll) * hr[k] - P->gamma_roll * wrel[k];
+            if (tr_mag > tr_max && tr_mag > 1e-12) {
+                for (int k = 0; k < 3; ++k) {
+                    troll[k] = (-tr_max) * (hr[k] / tr_mag);
+                    hr[k] = (tr_max / P->k_roll) * (hr[k] / tr_mag);
+                }
+            }
+            rolling[3 * nc] = hr[0]; rolling[3 * nc + 1] = hr[1]; rolling[3 * nc + 2] = hr[2];
+        }
         for (int k = 0; k < 3; ++k) ftot[k] = fntot * n[k] + fs[k];
         double c[3];
         cross3(n, fs, c);
@@ -582,6 +619,8 @@ static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, i
     add3(f + 3 * j, ftot, -1.0);
     add3(torque + 3 * i, tor, armi);
     add3(torque + 3 * j, tor, armj);
+    add3(torque + 3 * i, troll, 1.0);
+    add3(torque + 3 * j, troll, -1.0);
     /* Pair::ev_tally_xyz as restated at hooke_history.py:219-229 */
     double vir[6] = {0.5 * (dpos[0] * ftot[0]), 0.5 * (dpos[1] * ftot[1]), 0.5 * (dpos[2] * ftot[2]),
                      0.5 * (dpos[0] * ftot[1]), 0.5 * (dpos[0] * ftot[2]), 0.5 * (dpos[1] * ftot[2])};
@@ -593,12 +632,12 @@ static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, i
 void or_pair_compute(int style, const or_pair_t* P, const or_box_t* b, int npairs,
                      const int32_t* pair_i, const int32_t* pair_j, const double* x, const double* v,
                      const double* om, const double* rad, const double* rmass, const int32_t* tag,
-                     int32_t* partner, double* shear, double dt, int shearupdate, double* f,
-                     double* torque, double* virial) {
+                     int32_t* partner, double* shear, double* rolling, double dt, int shearupdate,
+                     double* f, double* torque, double* virial) {
 #pragma omp parallel for if (g_nthreads > 1) schedule(static)
     for (int nc = 0; nc < npairs; ++nc)
         pair_one(style, P, b, nc, pair_i[nc], pair_j[nc], x, v, om, rad, rmass, tag, partner, shear,
-                 dt, shearupdate, f, torque, virial);
+                 rolling, dt, shearupdate, f, torque, virial);
 }
 
 /* ---------------------------------------------------------- fixes */

@@ -41,6 +41,8 @@ class GranularPair(ABC):
             history = getattr(nlist, "_private_history", None)
             if history is None:
                 history = nlist._private_history = ContactHistory(nlist.max_atoms, nlist.max_neighbors_per_atom)
+        if self.params.rolling_id:
+            history.enable_rolling()
         nl = history.cstruct(nlist)
         with _device.timed("contact"):
             rc = _device.lib().tmps_contact(atom.cstruct(), nl, self.domain.dbox, self.params, float(dt),

@@ -45,7 +45,7 @@ def mix_stiffness_g(e1: float, e2: float, poiss1: float, poiss2: float) -> float
 class PairGranular(GranularPair):
     def __init__(self, domain, normal: str, normal_coeffs, tangential: str = "none",
                  tangential_coeffs=None, damping: str = "viscoelastic", limit_damping: bool = False,
-                 float_type: Any = None) -> None:
+                 float_type: Any = None, rolling: str = "none", rolling_coeffs=None) -> None:
         super().__init__(domain, float_type=float_type)
         for kind, name, table in (("normal", normal, _NORMAL), ("damping", damping, _DAMPING),
                                   ("tangential", tangential, _TANGENTIAL)):
@@ -77,17 +77,33 @@ class PairGranular(GranularPair):
         self.uses_history = self.tangential_id in (TANGENTIAL_LINEAR_HISTORY, TANGENTIAL_MINDLIN)
         if self.tangential_id != TANGENTIAL_NONE:
             self._setup_tangential(tangential, list(tangential_coeffs or []))
+        # rolling resistance, RollingResistance (GRANULAR/rolling.py:16-50): k_roll, gamma_roll, mu_roll.
+        # The reference defines the model but never calls it from a pair style; here it is wired into
+        # pair granular as rolling.py writes it (see contact_law).
+        if rolling not in ("none", "sds", "epsd"):
+            raise ValueError(f"Unsupported pair granular rolling model {rolling!r}; implemented: "
+                             "['epsd', 'none', 'sds']")
+        self.rolling_id = 0 if rolling == "none" else 1
+        self.k_roll = self.gamma_roll = self.mu_roll = 0.0
+        if self.rolling_id:
+            rc = list(rolling_coeffs or [])
+            if len(rc) != 3:
+                raise ValueError("rolling takes k_roll, gamma_roll, mu_roll")
+            self.k_roll, self.gamma_roll, self.mu_roll = (float(c) for c in rc)
+            self.uses_history = True
         self.submodels = {
             "normal": (normal, [float(c) for c in normal_coeffs]),
             "damping": (damping, []),
             "tangential": (tangential, [-1.0 if c is None else float(c) for c in (tangential_coeffs or [])]),
-            "rolling": ("none", []), "twisting": ("none", []), "heat": ("none", []),
+            "rolling": (rolling, [float(c) for c in (rolling_coeffs or [])] if self.rolling_id else []),
+            "twisting": ("none", []), "heat": ("none", []),
         }
         p = self.params
         p.style = 4
         p.normal_id, p.damping_id, p.tangential_id = self.normal_id, self.damping_id, self.tangential_id
         p.limit_damping = self.limit_damping
         p.kn, p.kt, p.damp, p.xt, p.mu = self.kn, self.kt, self.damp, self.xt, self.mu
+        p.rolling_id, p.k_roll, p.gamma_roll, p.mu_roll = self.rolling_id, self.k_roll, self.gamma_roll, self.mu_roll
 
     def _damping_coefficient(self, normal: str) -> float:
         """The damping sub-model's constant (granular.py:207-238)."""

@@ -48,7 +48,7 @@ class NList(ctypes.Structure):
     """tmps_nlist"""
 
     _fields_ = [("n", c_i32), ("slots", c_i32), ("nbr", c_vp), ("nnb", c_vp), ("touch", c_vp),
-                ("shear", c_vp)]
+                ("shear", c_vp), ("rolling", c_vp)]
 
 
 class PairParams(ctypes.Structure):
@@ -59,6 +59,8 @@ class PairParams(ctypes.Structure):
         ("limit_damping", c_i32), ("pad_", c_i32),
         ("kn", c_f64), ("kt", c_f64), ("gamman", c_f64), ("gammat", c_f64), ("xmu", c_f64),
         ("damp", c_f64), ("xt", c_f64), ("mu", c_f64),
+        ("rolling_id", c_i32), ("pad2_", c_i32),
+        ("k_roll", c_f64), ("gamma_roll", c_f64), ("mu_roll", c_f64),
     ]
 
 

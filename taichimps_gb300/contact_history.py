@@ -33,6 +33,9 @@ class ContactHistory:
         self.setup_pending = False
         self._shape = None
         self.touch = self.shear = self._touch_alt = self._shear_alt = None
+        # rolling displacement per slot (contact_history.py:58-59), kept only for a rolling model
+        self.rolling_enabled = False
+        self.rolling = self._rolling_alt = None
         self._synced_build = -1     # build_count of the list this history belongs to
         self._saved_build = None    # build_count at save_state()
         self._nlist = None
@@ -45,12 +48,25 @@ class ContactHistory:
         self.shear = torch.zeros((3, slots, n), dtype=torch.float64, device=self.dev)
         self._touch_alt = torch.zeros_like(self.touch)
         self._shear_alt = torch.zeros_like(self.shear)
+        if self.rolling_enabled:
+            self.rolling = torch.zeros_like(self.shear)
+            self._rolling_alt = torch.zeros_like(self.shear)
         self._shape = (n, slots)
+
+    def enable_rolling(self) -> None:
+        """Keep a rolling displacement beside the shear (a pair with a rolling model asks for it)."""
+        if not self.rolling_enabled:
+            self.rolling_enabled = True
+            if self.shear is not None:
+                self.rolling = torch.zeros_like(self.shear)
+                self._rolling_alt = torch.zeros_like(self.shear)
 
     def reset(self) -> None:
         if self.touch is not None:
             self.touch.zero_()
             self.shear.zero_()
+            if self.rolling is not None:
+                self.rolling.zero_()
 
     def ensure(self, nlist) -> None:
         """Make the history match `nlist`'s current build (fresh zeros if it does not)."""
@@ -62,7 +78,7 @@ class ContactHistory:
 
     def cstruct(self, nlist) -> _lib.NList:
         self.ensure(nlist)
-        return nlist.cstruct(self.touch, self.shear)
+        return nlist.cstruct(self.touch, self.shear, rolling=self.rolling)
 
     def save_state(self, atom, nlist) -> None:
         """Mark the current contacts for carry-over across the next build."""
@@ -86,12 +102,14 @@ class ContactHistory:
                    and self._shape == (nlist._n, nlist.slots))
         if carried:
             L = _device.lib()
-            old = nlist.cstruct(self.touch, self.shear, prev=True)
-            new = nlist.cstruct(self._touch_alt, self._shear_alt)
+            old = nlist.cstruct(self.touch, self.shear, prev=True, rolling=self.rolling)
+            new = nlist.cstruct(self._touch_alt, self._shear_alt, rolling=self._rolling_alt)
             _lib.check(L.tmps_history_remap(old, new, nlist.order.data_ptr(), _device.stream()),
                        "tmps_history_remap")
             self.touch, self._touch_alt = self._touch_alt, self.touch
             self.shear, self._shear_alt = self._shear_alt, self.shear
+            if self.rolling is not None:
+                self.rolling, self._rolling_alt = self._rolling_alt, self.rolling
             self._synced_build = nlist.build_count
         else:
             self._alloc(nlist._n, nlist.slots)

@@ -22,7 +22,8 @@ __global__ void __launch_bounds__(kBlock)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = A.n;
     if (i >= n) return;
-    const bool hist = kHist && (STYLE != STYLE_GRANULAR || P.tangential_id >= 2);
+    const bool hist = kHist && (STYLE != STYLE_GRANULAR || P.tangential_id >= 2 || P.rolling_id != 0);
+    const bool roll = STYLE == STYLE_GRANULAR && P.rolling_id != 0;
     double prd[3], iprd[3];
     int per[3];
 #pragma unroll
@@ -79,21 +80,31 @@ __global__ void __launch_bounds__(kBlock)
         in.vb[0] = vb.x + dv[0]; in.vb[1] = vb.y + dv[1]; in.vb[2] = vb.z + dv[2];
         in.wa[0] = wa.x; in.wa[1] = wa.y; in.wa[2] = wa.z;
         in.wb[0] = wb.x; in.wb[1] = wb.y; in.wb[2] = wb.z;
-        double sh[3] = {0, 0, 0};
+        double sh[3] = {0, 0, 0}, rl[3] = {0, 0, 0};
         const size_t so = (size_t)k * n + i;
         if (hist && ((touch >> k) & 1ull)) {
             const double sg = lo ? 1.0 : -1.0;
             sh[0] = sg * L.shear[so];
             sh[1] = sg * L.shear[ss + so];
             sh[2] = sg * L.shear[2 * ss + so];
+            if (roll) {
+                rl[0] = sg * L.rolling[so];
+                rl[1] = sg * L.rolling[ss + so];
+                rl[2] = sg * L.rolling[2 * ss + so];
+            }
         }
         PairOut<double> out;
-        contact_law<double, STYLE>(P, dt, shearupdate, in, sh, out);
+        contact_law<double, STYLE>(P, dt, shearupdate, in, sh, rl, out);
         if (hist) {
             const double sg = lo ? 1.0 : -1.0;
             L.shear[so] = sg * sh[0];
             L.shear[ss + so] = sg * sh[1];
             L.shear[2 * ss + so] = sg * sh[2];
+            if (roll) {
+                L.rolling[so] = sg * rl[0];
+                L.rolling[ss + so] = sg * rl[1];
+                L.rolling[2 * ss + so] = sg * rl[2];
+            }
             newtouch |= 1ull << k;
         }
         const double sgn = lo ? 1.0 : -1.0;
@@ -102,6 +113,7 @@ __global__ void __launch_bounds__(kBlock)
         for (int c = 0; c < 3; ++c) {
             F[c] += sgn * out.f[c];
             Tq[c] += arm * out.tor[c];
+            Tq[c] += sgn * out.troll[c];
         }
         V[0] += 0.5 * (in.d[0] * out.f[0]);
         V[1] += 0.5 * (in.d[1] * out.f[1]);
@@ -138,7 +150,7 @@ bool params_ok(const tmps_pair_params* p) {
     if (p->style < 0 || p->style > 4) return false;
     if (p->style == 4) {
         if (p->normal_id < 0 || p->normal_id > 2 || p->damping_id < 0 || p->damping_id > 5 ||
-            p->tangential_id < 0 || p->tangential_id > 3)
+            p->tangential_id < 0 || p->tangential_id > 3 || p->rolling_id < 0 || p->rolling_id > 1)
             return false;
     }
     return true;
@@ -199,6 +211,7 @@ int tmps_contact(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
                  void* stream) {
     if (!a || !nl || !d_box || !p || a->n < 0 || nl->n != a->n || !params_ok(p)) return TMPS_ERR_BAD_ARG;
     if (nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
+    if (p->style == 4 && p->rolling_id != 0 && !nl->rolling) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
     const int g = grid_for(a->n, kBlock);
     cudaStream_t s = (cudaStream_t)stream;

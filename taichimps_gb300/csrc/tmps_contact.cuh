@@ -54,16 +54,18 @@ struct PairOut {
     T f[3];      // force on a (b gets -f)
     T tor[3];    // torque term; a gets arm_a * tor, b gets arm_b * tor
     T arm_a, arm_b;
+    T troll[3];  // rolling-resistance torque: a gets +troll, b gets -troll
 };
 
 // One contact (the caller has established rsq < (ra + rb)^2 and supplies r and
-// the overlap).  `sh` (canonical sense) is read and written only by history
-// styles; the caller passes zeros when the slot held no live contact (the
-// reference's partner != jtag reset).
+// the overlap).  `sh` and `rl` (canonical sense) are read and written only by
+// history styles and by the rolling model; the caller passes zeros when the
+// slot held no live contact (the reference's partner != jtag reset).
 template <typename T, int STYLE>
 TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, const PairIn<T>& in,
-                          double* sh, PairOut<T>& out) {
+                          double* sh, double* rl, PairOut<T>& out) {
     using S = StyleTraits<STYLE>;
+    out.troll[0] = out.troll[1] = out.troll[2] = T(0);
     if constexpr (S::legacy) {
         const T r = in.r;
         const T delta = in.delta;
@@ -255,6 +257,30 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
         for (int k = 0; k < 3; ++k) out.tor[k] = -c[k];
         out.arm_a = in.ra - T(0.5) * delta;
         out.arm_b = in.rb - T(0.5) * delta;
+        if (P.rolling_id == 1) {
+            // RollingResistance.compute_torque (rolling.py:30-50), as the reference writes
+            // it: omega_rel = omega_a - omega_b, r_eff, fn = |fntot|; the history (FP64,
+            // like the shear) advances only on a history update
+            T wrel[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) wrel[k] = in.wa[k] - in.wb[k];
+            if (shearupdate) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) rl[k] = rl[k] + (double)(wrel[k] * dt);
+            }
+            T h[3] = {(T)rl[0], (T)rl[1], (T)rl[2]};
+            const T tr_mag = T(P.k_roll) * norm3(h);
+            const T tr_max = (T(P.mu_roll) * reff) * fabs(fntot);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) out.troll[k] = (-T(P.k_roll)) * h[k] - T(P.gamma_roll) * wrel[k];
+            if (tr_mag > tr_max && tr_mag > T(1e-12)) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    out.troll[k] = (-tr_max) * (h[k] / tr_mag);
+                    rl[k] = (double)((tr_max / T(P.k_roll)) * (h[k] / tr_mag));
+                }
+            }
+        }
     }
 }
 

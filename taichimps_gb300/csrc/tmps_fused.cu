@@ -433,7 +433,8 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
     if (rebuild_due(E, s)) return;  // S marks the step aborted; the host rebuilds
     const int nb = E->nblocks;      // partials are component-major, [6][nb]
     constexpr bool kHist = STYLE == STYLE_HOOKE_HISTORY || STYLE == STYLE_HERTZ_HISTORY || STYLE == STYLE_GRANULAR;
-    const bool hist = kHist && (STYLE != STYLE_GRANULAR || P.tangential_id >= 2);
+    const bool hist = kHist && (STYLE != STYLE_GRANULAR || P.tangential_id >= 2 || P.rolling_id != 0);
+    const bool roll = STYLE == STYLE_GRANULAR && P.rolling_id != 0;
     const int n = A.n;
     T dt;
     if constexpr (MIXED) dt = E->dt_hi;
@@ -606,7 +607,7 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
                     int32_t ci = 0, cj = 0;
                     float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
                     T vi[3], wi[3], mi, vj[3], wj[3], mj;
-                    double shr[3] = {0, 0, 0};
+                    double shr[3] = {0, 0, 0}, rlr[3] = {0, 0, 0};
                     if constexpr (MIXED) {
                         const float4 pi = ld4f(A.pos32, ia), pj = ld4f(A.pos32, j);
                         il = ld4f(A.pos32lo, ia);
@@ -638,6 +639,11 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
                         shr[0] = L.shear[so];
                         shr[1] = L.shear[ss + so];
                         shr[2] = L.shear[2 * ss + so];
+                        if (roll) {
+                            rlr[0] = L.rolling[so];
+                            rlr[1] = L.rolling[ss + so];
+                            rlr[2] = L.rolling[2 * ss + so];
+                        }
                     }
                     // separation x_i - x_j
                     T d[3];
@@ -771,26 +777,34 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
                             in.wa[c] = lo ? wi[c] : wj[c];
                             in.wb[c] = lo ? wj[c] : wi[c];
                         }
-                        double sh[3] = {0, 0, 0};
+                        double sh[3] = {0, 0, 0}, rl[3] = {0, 0, 0};
                         if (hist && was) {
                             const double sgd = lo ? 1.0 : -1.0;
                             sh[0] = sgd * shr[0];
                             sh[1] = sgd * shr[1];
                             sh[2] = sgd * shr[2];
+                            rl[0] = sgd * rlr[0];
+                            rl[1] = sgd * rlr[1];
+                            rl[2] = sgd * rlr[2];
                         }
                         PairOut<T> out;
-                        contact_law<T, STYLE>(P, dt, 1, in, sh, out);
+                        contact_law<T, STYLE>(P, dt, 1, in, sh, rl, out);
                         if (hist) {
                             const double sgd = lo ? 1.0 : -1.0;
                             L.shear[so] = sgd * sh[0];
                             L.shear[ss + so] = sgd * sh[1];
                             L.shear[2 * ss + so] = sgd * sh[2];
+                            if (roll) {
+                                L.rolling[so] = sgd * rl[0];
+                                L.rolling[ss + so] = sgd * rl[1];
+                                L.rolling[2 * ss + so] = sgd * rl[2];
+                            }
                         }
                         const T arm = lo ? out.arm_a : out.arm_b;
     #pragma unroll
                         for (int c = 0; c < 3; ++c) {
                             fc[c] = sg * out.f[c];
-                            tc[c] = arm * out.tor[c];
+                            tc[c] = arm * out.tor[c] + sg * out.troll[c];
                         }
                         vc[0] = T(0.5) * (in.d[0] * out.f[0]);
                         vc[1] = T(0.5) * (in.d[1] * out.f[1]);
@@ -1582,6 +1596,7 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
     if (!a || !nl || !d_box || !d_eng || !p || !scratch || a->n < 0 || nl->n != a->n) return TMPS_ERR_BAD_ARG;
     if (!a->pos32 && !a->rinv) return TMPS_ERR_BAD_ARG;
     if (p->style < 0 || p->style > 4 || nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
+    if (p->style == 4 && p->rolling_id != 0 && !nl->rolling) return TMPS_ERR_BAD_ARG;
     const int n = a->n;
     const bool mixed = a->pos32 != nullptr;
     const int g2 = contact_blocks(n, p->style, mixed);
@@ -1621,7 +1636,8 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
         return TMPS_ERR_BAD_ARG;
     if (nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
     const int n = a->n;
-    const bool has_hist = p->style == 1 || p->style == 3 || (p->style == 4 && p->tangential_id >= 2);
+    const bool has_hist = p->style == 1 || p->style == 3 ||
+                          (p->style == 4 && (p->tangential_id >= 2 || p->rolling_id != 0));
     uint32_t* flags = (uint32_t*)scratch;
     float* gap = (float*)((char*)scratch + gap_offset(n));
     float* agap = (float*)((char*)scratch + atom_gap_offset(n));

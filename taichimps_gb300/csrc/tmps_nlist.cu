@@ -246,7 +246,8 @@ __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* 
 
 // ContactHistory save/restore (contact_history.py:91-139) in one pass: for
 // each slot of the new list, find the same partner among the old row's
-// touching slots and carry its shear over; anything else starts at zero.
+// touching slots and carry its shear (and rolling displacement, when both
+// lists hold one) over; anything else starts at zero.
 __global__ void __launch_bounds__(kBlock) k_history_remap(tmps_nlist o, tmps_nlist nw,
                                                           const int32_t* __restrict__ order) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -257,9 +258,10 @@ __global__ void __launch_bounds__(kBlock) k_history_remap(tmps_nlist o, tmps_nli
     const int onn = o.nnb[po];
     const int nn = nw.nnb[p];
     uint64_t bits = 0;
+    const bool roll = o.rolling != nullptr && nw.rolling != nullptr;
     for (int k = 0; k < nn; ++k) {
         const int qo = order[nw.nbr[(size_t)k * n + p] & kNbrIndexMask];
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0;
         if (otouch) {
             for (int ko = 0; ko < onn; ++ko) {
                 if (!((otouch >> ko) & 1ull)) continue;
@@ -268,6 +270,11 @@ __global__ void __launch_bounds__(kBlock) k_history_remap(tmps_nlist o, tmps_nli
                 s0 = o.shear[(size_t)ko * n + po];
                 s1 = o.shear[ss + (size_t)ko * n + po];
                 s2 = o.shear[2 * ss + (size_t)ko * n + po];
+                if (roll) {
+                    r0 = o.rolling[(size_t)ko * n + po];
+                    r1 = o.rolling[ss + (size_t)ko * n + po];
+                    r2 = o.rolling[2 * ss + (size_t)ko * n + po];
+                }
                 bits |= 1ull << k;
                 break;
             }
@@ -276,6 +283,11 @@ __global__ void __launch_bounds__(kBlock) k_history_remap(tmps_nlist o, tmps_nli
         nw.shear[(size_t)k * n + p] = s0;
         nw.shear[ns + (size_t)k * n + p] = s1;
         nw.shear[2 * ns + (size_t)k * n + p] = s2;
+        if (roll) {
+            nw.rolling[(size_t)k * n + p] = r0;
+            nw.rolling[ns + (size_t)k * n + p] = r1;
+            nw.rolling[2 * ns + (size_t)k * n + p] = r2;
+        }
     }
     nw.touch[p] = bits;
 }

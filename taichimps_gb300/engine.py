@@ -124,6 +124,8 @@ class FusedEngine:
         atom, nl = sim.atom, sim.neighbor
         n = atom.nlocal
         self._alloc(n)
+        if sim.pair_style.params.rolling_id:
+            sim.history.enable_rolling()
         if self.mixed:
             g = nl.grid_dim
             if np.any(g > 1023):

@@ -157,7 +157,8 @@ class NeighborList:
         self.cell_of = torch.zeros(n, **i32)
         self._n = n
 
-    def cstruct(self, touch: torch.Tensor | None, shear: torch.Tensor | None, prev: bool = False) -> _lib.NList:
+    def cstruct(self, touch: torch.Tensor | None, shear: torch.Tensor | None, prev: bool = False,
+                rolling: torch.Tensor | None = None) -> _lib.NList:
         s = _lib.NList()
         s.n = self._n
         s.slots = self.slots
@@ -165,6 +166,7 @@ class NeighborList:
         s.nnb = (self.prev_nnb if prev else self.nnb).data_ptr()
         s.touch = touch.data_ptr() if touch is not None else None
         s.shear = shear.data_ptr() if shear is not None else None
+        s.rolling = rolling.data_ptr() if rolling is not None else None
         return s
 
     # ------------------------------------------------------------ build

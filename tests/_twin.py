@@ -26,6 +26,11 @@ PAIR_STYLES = {
         damping="tsuji", limit_damping=True)),
     "granular/velocity": dict(style="granular", kw=dict(
         normal="hooke", normal_coeffs=[2e5, 5.0], tangential="none", damping="velocity")),
+    # the triaxial configuration's contact: hertz/material, coeff_restitution, mindlin, rolling EPSD
+    "granular/rolling": dict(style="granular", kw=dict(
+        normal="hertz/material", normal_coeffs=[5e6, 0.5, 0.3], tangential="mindlin",
+        tangential_coeffs=[None, 1.0, 0.5], damping="coeff_restitution", rolling="epsd",
+        rolling_coeffs=[1e3, 50.0, 0.1])),
 }
 
 

@@ -207,3 +207,30 @@ def test_pressure_record_each_step(gpu, oracle, precision):
     for k, s in enumerate(range(63, 71)):
         osim.step()
         assert rel_err(rows[k], osim.last_pressure) < tol, (s, rel_err(rows[k], osim.last_pressure))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_rolling_resistance(gpu, oracle, precision):
+    """The triaxial configuration's contact (pair granular hertz/material, coeff_restitution, mindlin,
+    rolling EPSD) through the fused step with Cundall and the servo, against the oracle; spinning
+    spheres so the rolling torque and its history matter."""
+    rng = np.random.default_rng(17)
+    x, r = dense_packing(rng, 343, 7.2, 0.5, 0.57)
+    w = rng.normal(scale=2.0, size=x.shape)
+    deform = dict(axes={d: {"style": "pressure", "ptarget": 1.0, "pgain": 1e-3} for d in "xyz"}, couple="xyz",
+                  max_rate=1e-1, remap="x")
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [7.2] * 3, w=w, pair="granular/rolling", dt=5e-5,
+                          cundall=(0.7, 0.7), deform=deform)
+    sim.precision = precision
+    sim.run(50)
+    osim.run(50)
+    assert sim.last_engine is not None
+    assert np.abs(osim.history.rolling).max() > 0
+    g, o = gpu_state(sim), oracle_state(osim)
+    if precision == "fp64":
+        for k in ("x", "v", "omega", "f", "torque"):
+            assert rel_err(g[k], o[k]) < 1e-10, (k, rel_err(g[k], o[k]))
+    else:
+        assert rel_err(g["f"], o["f"]) < MIXED_F, rel_err(g["f"], o["f"])
+        assert rel_err(g["torque"], o["torque"]) < MIXED_F, rel_err(g["torque"], o["torque"])
+        assert rel_err(g["omega"], o["omega"]) < MIXED_V, rel_err(g["omega"], o["omega"])

@@ -248,7 +248,10 @@ def test_pair_antisymmetry_all_styles(oracle):
               ("granular", dict(normal="hooke", normal_coeffs=[2e5, 30.0], tangential="linear_history",
                                 tangential_coeffs=[5e4, 0.5, 0.4], damping="mass_velocity")),
               ("granular", dict(normal="hertz", normal_coeffs=[2e5, 10.0], tangential="linear_nohistory",
-                                tangential_coeffs=[0.5, 0.4], damping="viscoelastic"))]
+                                tangential_coeffs=[0.5, 0.4], damping="viscoelastic")),
+              ("granular", dict(normal="hertz/material", normal_coeffs=[5e6, 0.5, 0.3], tangential="mindlin",
+                                tangential_coeffs=[None, 1.0, 0.5], damping="coeff_restitution",
+                                rolling="epsd", rolling_coeffs=[1e3, 50.0, 0.1]))]
     x = np.array([[1.0, 1.0, 1.0], [1.95, 1.1, 0.97]])
     rad = np.array([0.5, 0.52])
     v = rng.normal(size=(2, 3))
@@ -295,3 +298,45 @@ def test_contact_count_brute_force(oracle):
     want = ((rsq < rs * rs) & (rsq > 1e-18)).sum(1)
     assert got.sum() > 0
     np.testing.assert_array_equal(got, want)
+
+
+def test_rolling_resistance_torque(oracle):
+    """GRANULAR/rolling.py:30-50 (EPSD) in the oracle's pair granular: for two touching spheres at rest
+    with a relative spin, the first update gives torque_i = -k h - gamma w_rel with h = w_rel dt on atom i
+    and the opposite on atom j (uncapped), added to the tangential torque; the rolling history is
+    h; with mu_roll = 0 the cap rescales the history as rolling.py writes it."""
+    O = oracle
+    x = np.array([[1.0, 1.0, 1.0], [1.9, 1.0, 1.0]])
+    rad = np.array([0.5, 0.5])
+    w = np.array([[0.0, 0.0, 2.0], [0.0, 0.0, -1.0]])
+    dt = 1e-3
+    kroll, groll = 1e3, 50.0
+    out = {}
+    for mu_roll in (1e6, 0.0):
+        for rolling in ("none", "epsd"):
+            dom = O.OracleDomain.make([0.0] * 3, [5.0] * 3)
+            atoms = O.OracleAtoms(x=x, omega=w, radius=rad, density=2.5, tag=[1, 2])
+            nl = O.OracleNeighbor(dom, skin=0.1, max_neighbors=8)
+            nl.build(atoms)
+            hist = O.OracleHistory(8)
+            hist.restore_state(atoms, nl)
+            kw = dict(normal="hertz/material", normal_coeffs=[5e6, 0.5, 0.3], tangential="mindlin",
+                      tangential_coeffs=[None, 1.0, 0.5], damping="coeff_restitution")
+            if rolling != "none":
+                kw.update(rolling="epsd", rolling_coeffs=[kroll, groll, mu_roll])
+            pair = O.OraclePair("granular", **kw)
+            atoms.clear_forces()
+            pair.compute(atoms, nl, hist, dom, dt)
+            out[(mu_roll, rolling)] = (atoms.torque.copy(), hist.rolling[0].copy())
+    wrel = w[0] - w[1]
+    h = wrel * dt
+    troll = -kroll * h - groll * wrel
+    t_none, _ = out[(1e6, "none")]
+    t_roll, h_got = out[(1e6, "epsd")]
+    np.testing.assert_allclose(t_roll[0] - t_none[0], troll, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(t_roll[1] - t_none[1], -troll, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(h_got, h, rtol=1e-15)
+    # mu_roll = 0: tr_max = 0 < tr_mag, so torque = 0 and the history is rescaled to zero
+    t_cap, h_cap = out[(0.0, "epsd")]
+    np.testing.assert_allclose(t_cap, out[(0.0, "none")][0], rtol=1e-15, atol=0)
+    np.testing.assert_array_equal(h_cap, np.zeros(3))
