@@ -203,7 +203,26 @@ typedef struct tmps_engine {
     double* plog;            /* device address of a pinned host array, or NULL */
     int32_t plog_len;
     int32_t pad5_;
+    int64_t stop_step;       /* fused launches do nothing once step >= stop_step (batched runs) */
 } tmps_engine;
+
+/* One instance of a batched run (tmps_batch_*): the device state of one
+ * independent system -- its own atoms, list, pair coefficients, box, servo,
+ * fused-step engine and scratch, exactly what the single-instance calls take --
+ * and the range of blocks it owns in each batched grid.  Its grids are the
+ * ones a single-instance launch would use (tmps_batch_blocks), so a batched
+ * step and a single-instance step of the same instance are interchangeable. */
+typedef struct tmps_instance {
+    tmps_atoms a;
+    tmps_nlist nl;
+    tmps_pair_params p;
+    tmps_box* box;
+    tmps_engine* eng;
+    tmps_servo* servo;
+    void* scratch;           /* tmps_fused_scratch_bytes(n, style, mixed) bytes */
+    int32_t a_first, a_blocks; /* blocks [a_first, a_first + a_blocks) of the batched A grid */
+    int32_t c_first, c_blocks; /* ... of the batched C grid */
+} tmps_instance;
 
 /* ---- library ---------------------------------------------------------- */
 
@@ -383,6 +402,29 @@ int64_t tmps_fused_scratch_bytes(int32_t n, int32_t style, int32_t mixed);
  * every step (deform_pressure.py:1113-1219); this is that read without the
  * round trip. */
 int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void* stream);
+
+/* ---- batched runs ----------------------------------------------------------
+ * Many independent systems of uneven size (each with its own box, contact
+ * coefficients and servo) advance together: one launch of each of A, C and S
+ * per step covers every instance.  No reference counterpart (the reference
+ * runs one system per process); each instance's arithmetic is the
+ * single-instance fused step's.  d_inst is a device array of ninst
+ * tmps_instance; d_block_inst maps every block of the A (or C) grid to its
+ * instance.  All instances share the arithmetic form (mixed) and the pair
+ * style. */
+
+/* Blocks one instance of n atoms owns in the A and C grids. */
+int tmps_batch_blocks(int32_t n, int32_t style, int32_t mixed, int32_t* a_blocks, int32_t* c_blocks);
+
+int tmps_batch_a(const tmps_instance* d_inst, const int32_t* d_block_inst, int32_t nblocks, int32_t mixed,
+                 void* stream);
+int tmps_batch_c(const tmps_instance* d_inst, const int32_t* d_block_inst, int32_t nblocks, int32_t style,
+                 int32_t mixed, void* stream);
+/* S for every instance, one block each; a box driven non-positive sets
+ * TMPS_STATUS_BOX_NONPOSITIVE in *d_status. */
+int tmps_batch_servo(const tmps_instance* d_inst, int32_t ninst, int32_t* d_status, void* stream);
+/* d_state[2 i] = step, d_state[2 i + 1] = aborted of instance i (one copy for the host). */
+int tmps_batch_state(const tmps_instance* d_inst, int32_t ninst, int64_t* d_state, void* stream);
 
 /* Applies what the fused step leaves pending -- the second half-kick of the
  * last step and a remap x the servo asked for -- so the state is that of the

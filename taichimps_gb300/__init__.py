@@ -8,11 +8,12 @@ from .atom import AtomSystem
 from .computes import ComputeContactAtom, Computes
 from .contact_history import ContactHistory
 from .domain import Domain
+from .ensemble import BatchedEngine
 from .EXTRA_FIX import Fix, FixDampingCundall, FixDeformPressure, FixNVESphere
 from .GRANULAR import GranHertz, GranHertzHistory, GranHooke, GranHookeHistory, GranularPair, PairGranular
 from .neighbor import NeighborList
 from .simulation import Simulation
 
-__all__ = ["AtomSystem", "ComputeContactAtom", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
+__all__ = ["AtomSystem", "BatchedEngine", "ComputeContactAtom", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
            "FixDeformPressure", "FixNVESphere", "GranHertz", "GranHertzHistory", "GranHooke",
            "GranHookeHistory", "GranularPair", "PairGranular", "NeighborList", "Simulation"]

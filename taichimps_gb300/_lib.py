@@ -101,6 +101,17 @@ class Engine(ctypes.Structure):
         ("shift_bound", ctypes.c_float), ("maxd2_bits", ctypes.c_uint32), ("cull", c_i32),
         ("cull_tol", ctypes.c_float),
         ("plog", ctypes.c_void_p), ("plog_len", c_i32), ("pad5_", c_i32),
+        ("stop_step", ctypes.c_int64),
+    ]
+
+
+class Instance(ctypes.Structure):
+    """tmps_instance"""
+
+    _fields_ = [
+        ("a", Atoms), ("nl", NList), ("p", PairParams),
+        ("box", c_vp), ("eng", c_vp), ("servo", c_vp), ("scratch", c_vp),
+        ("a_first", c_i32), ("a_blocks", c_i32), ("c_first", c_i32), ("c_blocks", c_i32),
     ]
 
 
@@ -145,6 +156,11 @@ _SIGS = {
     "tmps_fused_scratch_bytes": (ctypes.c_int64, [c_i32, c_i32, c_i32]),
     "tmps_fused_settle": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp]),
     "tmps_fused_pressure_log": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
+    "tmps_batch_blocks": (c_i32, [c_i32, c_i32, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32)]),
+    "tmps_batch_a": (c_i32, [c_vp, c_vp, c_i32, c_i32, c_vp]),
+    "tmps_batch_c": (c_i32, [c_vp, c_vp, c_i32, c_i32, c_i32, c_vp]),
+    "tmps_batch_servo": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
+    "tmps_batch_state": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
 }
 
 _lib: ctypes.CDLL | None = None

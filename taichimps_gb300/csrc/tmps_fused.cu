@@ -115,6 +115,14 @@ __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Scratch layout of one instance: [flag words, one per 32-atom group + 1]
+// [per-group gaps][per-atom gaps][virial partials, component-major [6][blocks
+// of A and C]], each region on a 256-byte boundary.
+__host__ __device__ inline size_t lay_round256(size_t b) { return (b + 255) & ~size_t(255); }
+__host__ __device__ inline size_t lay_gap(int n) { return lay_round256((size_t)((n + 31) / 32 + 1) * sizeof(uint32_t)); }
+__host__ __device__ inline size_t lay_agap(int n) { return lay_gap(n) + lay_round256((size_t)((n + 31) / 32) * sizeof(float)); }
+__host__ __device__ inline size_t lay_part(int n) { return lay_agap(n) + lay_round256((size_t)n * sizeof(float)); }
+
 __device__ __forceinline__ bool rebuild_due(const tmps_engine* __restrict__ e, int64_t s) {
     const int64_t since = s - e->last_build_step;
     if (since <= 0) return false;  // built in this very step already
@@ -144,12 +152,12 @@ __device__ __forceinline__ bool force_live(const uint32_t* __restrict__ flags, i
 // every atom into per-block partials: an atom C finds contact-free ends the
 // step with that velocity, and C adds m (v(t+dt) v(t+dt) - v(t+dt/2)
 // v(t+dt/2)) for the rest (thermo.py:94-101).
-__global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* __restrict__ b,
-                                                  tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
-                                                  double* __restrict__ part) {
+__device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __restrict__ b,
+                                         tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
+                                         double* __restrict__ part, const int bid, const int nblk) {
     __shared__ double smem[6 * (kBlockA / 32)];
     pdl_enter();
-    if (e->aborted) return;
+    if (e->aborted || e->step >= e->stop_step) return;
     const int n = a.n;
     const int nb = e->nblocks;  // partials are component-major, [6][nb]
     const int lane = threadIdx.x & 31;
@@ -159,8 +167,8 @@ __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* _
     bool hit = false;
     float dd = 0.0f;
     double K[6] = {0, 0, 0, 0, 0, 0};
-    const int stride = gridDim.x * blockDim.x;
-    for (int b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); b0 < n; b0 += stride) {
+    const int stride = nblk * blockDim.x;
+    for (int b0 = bid * blockDim.x + (threadIdx.x & ~31); b0 < n; b0 += stride) {
         const int i = b0 + lane;
         if (i >= n) continue;
         double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
@@ -200,8 +208,14 @@ __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* _
     block_sum<6, kBlockA>(K, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) part[(size_t)c * nb + blockIdx.x] = K[c];
+        for (int c = 0; c < 6; ++c) part[(size_t)c * nb + bid] = K[c];
     }
+}
+
+__global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                  tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
+                                                  double* __restrict__ part) {
+    a64_body(a, b, e, flags, part, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ A, mixed
@@ -217,16 +231,16 @@ __device__ __forceinline__ int cell_z(int32_t c) { return (c >> 20) & 1023; }
 __device__ __forceinline__ float4 ld4f_cs(const float* p, int i) { return __ldcs(reinterpret_cast<const float4*>(p) + i); }
 __device__ __forceinline__ void st4f_cs(float* p, int i, float4 v) { __stcs(reinterpret_cast<float4*>(p) + i, v); }
 
-__global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
-                                                     tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
-                                                     double* __restrict__ part) {
+__device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __restrict__ b,
+                                         tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
+                                         double* __restrict__ part, const int bid, const int nblk) {
     // Double-word state (hi + lo, both FP32) updated with error-free FP32
     // transforms: the FP64 pipe of this part is ~70x narrower than FP32, and
     // a double<->float conversion costs as much as a DFMA, so this kernel
     // issues no FP64 instruction at all.
     __shared__ float2 smem[6 * (kBlockA / 32)];
     pdl_enter();
-    if (e->aborted) return;
+    if (e->aborted || e->step >= e->stop_step) return;
     const int n = a.n;
     const int nb = e->nblocks;  // partials are component-major, [6][nb]
     const int lane = threadIdx.x & 31;
@@ -238,8 +252,8 @@ __global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box
     bool hit = false;
     float dd = 0.0f;
     float Kh[6] = {0, 0, 0, 0, 0, 0}, Kl[6] = {0, 0, 0, 0, 0, 0};
-    const int stride = gridDim.x * blockDim.x;
-    for (int b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); b0 < n; b0 += stride) {
+    const int stride = nblk * blockDim.x;
+    for (int b0 = bid * blockDim.x + (threadIdx.x & ~31); b0 < n; b0 += stride) {
         const int i = b0 + lane;
         if (i >= n) continue;
         float4 p = ld4f(a.pos32, i), pl = ld4f_cs(a.pos32lo, i);
@@ -289,8 +303,14 @@ __global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box
     block_sum_dw<6, kBlockA>(Kh, Kl, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < 6; ++k) reinterpret_cast<float2*>(part)[(size_t)k * nb + blockIdx.x] = make_float2(Kh[k], Kl[k]);
+        for (int k = 0; k < 6; ++k) reinterpret_cast<float2*>(part)[(size_t)k * nb + bid] = make_float2(Kh[k], Kl[k]);
     }
+}
+
+__global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
+                                                     tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
+                                                     double* __restrict__ part) {
+    a32_body(a, b, e, flags, part, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------- C
@@ -418,17 +438,18 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
 // virial partials depend only on the flag words and the grid, not on
 // scheduling; the kinetic term of an unflagged atom is A's.
 template <int STYLE, bool MIXED>
-__global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
-    k_cf(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
-         tmps_engine* __restrict__ E, uint32_t* __restrict__ flags, const float* __restrict__ gap,
-         const float* __restrict__ agap, double* __restrict__ part) {
+__device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L, const tmps_pair_params& P,
+                                        const tmps_box* __restrict__ B, tmps_engine* __restrict__ E,
+                                        uint32_t* __restrict__ flags, const float* __restrict__ gap,
+                                        const float* __restrict__ agap, double* __restrict__ part, const int bid,
+                                        const int nblk) {
     using T = typename std::conditional<MIXED, float, double>::type;
     __shared__ double smem[6 * (kBlockC / 32)];
     __shared__ uint8_t owner[kBlockC / 32][32];
     __shared__ int32_t croster[kBlockC / 32][32];
     __shared__ uint32_t cwords[kBlockC / 32][kLive];
     pdl_enter();
-    if (E->aborted) return;
+    if (E->aborted || E->step >= E->stop_step) return;
     const int64_t s = E->step + 1;
     if (rebuild_due(E, s)) return;  // S marks the step aborted; the host rebuilds
     const int nb = E->nblocks;      // partials are component-major, [6][nb]
@@ -471,10 +492,10 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
     float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};  // mixed: per-thread double words
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int ngroups = (n + 31) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int nwarps = (nblk * blockDim.x) >> 5;
     const size_t ss = (size_t)L.slots * n;
     // consecutive groups (neighbours in space) go to consecutive blocks
-    const int gw = blockIdx.x + gridDim.x * wib;
+    const int gw = bid + nblk * wib;
     const bool cull = E->cull != 0;
     float thr = 0.0f;
     if (cull) {
@@ -1006,16 +1027,24 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
         block_sum_dw<6, kBlockC>(Vh, Vl, reinterpret_cast<float2*>(smem));
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) reinterpret_cast<float2*>(part)[(size_t)c * nb + blockIdx.x] = make_float2(Vh[c], Vl[c]);
+            for (int c = 0; c < 6; ++c) reinterpret_cast<float2*>(part)[(size_t)c * nb + bid] = make_float2(Vh[c], Vl[c]);
         }
     } else {
         block_sum<6, kBlockC>(Vd, smem);
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) part[(size_t)c * nb + blockIdx.x] = Vd[c];
+            for (int c = 0; c < 6; ++c) part[(size_t)c * nb + bid] = Vd[c];
         }
     }
-    if (threadIdx.x == 0 && blockIdx.x == 0) E->final_pending = 1;
+    if (threadIdx.x == 0 && bid == 0) E->final_pending = 1;
+}
+
+template <int STYLE, bool MIXED>
+__global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
+    k_cf(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
+         tmps_engine* __restrict__ E, uint32_t* __restrict__ flags, const float* __restrict__ gap,
+         const float* __restrict__ agap, double* __restrict__ part) {
+    cf_body<STYLE, MIXED>(A, L, P, B, E, flags, gap, agap, part, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------- S
@@ -1220,8 +1249,8 @@ __device__ __forceinline__ V sum_component(const V* row, int nb, int q, int lane
     return acc;
 }
 
-__global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps_engine* e, const char* scratch,
-                                               int32_t* status) {
+__device__ __forceinline__ void s_body(tmps_box* b, tmps_servo* sv, tmps_engine* e, const char* scratch,
+                                       int32_t* status) {
     __shared__ double tot[6];
     __shared__ double wsum[kWarpsS];
     __shared__ float2 wsumf[kWarpsS];
@@ -1234,7 +1263,7 @@ __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps
     pdl_enter();
     copy_words(&se, e);
     __syncthreads();
-    if (se.aborted) return;
+    if (se.aborted || se.step >= se.stop_step) return;
     const int64_t s = se.step + 1;
     if (rebuild_due(&se, s)) {
         if (threadIdx.x == 0) e->aborted = 1;
@@ -1302,6 +1331,71 @@ __global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps
     copy_words(e, &se);
     copy_words(b, &sb);
     copy_words(sv, &ssv);
+}
+
+__global__ void __launch_bounds__(kBlockS) k_s(tmps_box* b, tmps_servo* sv, tmps_engine* e, const char* scratch,
+                                               int32_t* status) {
+    s_body(b, sv, e, scratch, status);
+}
+
+// ---------------------------------------------------------------- batched
+// Every block of a batched grid belongs to one instance (block_inst) and runs
+// that instance's single-instance body with its instance-local block index,
+// over the instance's own arrays.  The descriptors are written by the host
+// between chunks, never by these kernels, so they are read before the
+// dependency wait.
+
+// The block's descriptor, staged in shared memory: the bodies then read its
+// fields with shared loads instead of holding a register copy of every one.
+__device__ __forceinline__ const tmps_instance& stage_instance(tmps_instance& si, const tmps_instance* inst, int i) {
+    copy_words(&si, &inst[i]);
+    __syncthreads();
+    return si;
+}
+
+__global__ void __launch_bounds__(kBlockA) kb_a64(const tmps_instance* __restrict__ inst,
+                                                   const int32_t* __restrict__ block_inst) {
+    __shared__ tmps_instance si;
+    const tmps_instance& I = stage_instance(si, inst, block_inst[blockIdx.x]);
+    char* sc = static_cast<char*>(I.scratch);
+    a64_body(I.a, I.box, I.eng, reinterpret_cast<const uint32_t*>(sc), reinterpret_cast<double*>(sc + lay_part(I.a.n)),
+             (int)blockIdx.x - I.a_first, I.a_blocks);
+}
+
+__global__ void __launch_bounds__(kBlockA, 4) kb_a32(const tmps_instance* __restrict__ inst,
+                                                      const int32_t* __restrict__ block_inst) {
+    __shared__ tmps_instance si;
+    const tmps_instance& I = stage_instance(si, inst, block_inst[blockIdx.x]);
+    char* sc = static_cast<char*>(I.scratch);
+    a32_body(I.a, I.box, I.eng, reinterpret_cast<const uint32_t*>(sc), reinterpret_cast<double*>(sc + lay_part(I.a.n)),
+             (int)blockIdx.x - I.a_first, I.a_blocks);
+}
+
+template <int STYLE, bool MIXED>
+__global__ void __launch_bounds__(kBlockC, 2)
+    kb_cf(const tmps_instance* __restrict__ inst, const int32_t* __restrict__ block_inst) {
+    __shared__ tmps_instance si;
+    const tmps_instance& I = stage_instance(si, inst, block_inst[blockIdx.x]);
+    char* sc = static_cast<char*>(I.scratch);
+    const int n = I.a.n;
+    // C's partials follow the instance's A blocks in its [6][nblocks] layout
+    double* part = reinterpret_cast<double*>(sc + lay_part(n)) + I.a_blocks;
+    cf_body<STYLE, MIXED>(I.a, I.nl, I.p, I.box, I.eng, reinterpret_cast<uint32_t*>(sc),
+                          reinterpret_cast<const float*>(sc + lay_gap(n)), reinterpret_cast<const float*>(sc + lay_agap(n)),
+                          part, (int)blockIdx.x - I.c_first, I.c_blocks);
+}
+
+__global__ void __launch_bounds__(kBlockS) kb_s(const tmps_instance* __restrict__ inst, int32_t* status) {
+    const tmps_instance& I = inst[blockIdx.x];
+    s_body(I.box, I.servo, I.eng, static_cast<const char*>(I.scratch), status);
+}
+
+__global__ void kb_state(const tmps_instance* __restrict__ inst, int ninst, int64_t* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    const tmps_engine* e = inst[i].eng;
+    out[2 * i] = e->step;
+    out[2 * i + 1] = e->aborted;
 }
 
 // -------------------------------------------------------- prepare / unpack
@@ -1528,15 +1622,12 @@ int contact_blocks(int n, int style, bool mixed) {
     const int b = grid_for(n, kBlockC);
     return b < contact_wave(style, mixed) ? b : contact_wave(style, mixed);
 }
-// Scratch layout: [flag words, one per 32-atom group + 1][per-group gaps]
-// [per-atom gaps][virial partials, 6 per block of A and of C's contact
-// pass], each region on a 256-byte boundary.  The first three depend on n
-// alone, so A finds the flag words at the base and S finds the partials
-// through tmps_engine.part_off.
-size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
-size_t gap_offset(int n) { return round256((size_t)((n + 31) / 32 + 1) * sizeof(uint32_t)); }
-size_t atom_gap_offset(int n) { return gap_offset(n) + round256((size_t)((n + 31) / 32) * sizeof(float)); }
-size_t part_offset(int n) { return atom_gap_offset(n) + round256((size_t)n * sizeof(float)); }
+// The scratch regions (lay_*): the first three depend on n alone, so A finds
+// the flag words at the base and S finds the partials through
+// tmps_engine.part_off.
+size_t gap_offset(int n) { return lay_gap(n); }
+size_t atom_gap_offset(int n) { return lay_agap(n); }
+size_t part_offset(int n) { return lay_part(n); }
 }  // namespace
 
 extern "C" {
@@ -1662,6 +1753,60 @@ int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void
         dptr = (double*)at.devicePointer;
     }
     k_set_log<<<1, 1, 0, (cudaStream_t)stream>>>(d_eng, dptr, len);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_batch_blocks(int32_t n, int32_t style, int32_t mixed, int32_t* a_b, int32_t* c_b) {
+    if (n < 0 || style < 0 || style > 4 || !a_b || !c_b) return TMPS_ERR_BAD_ARG;
+    *a_b = n > 0 ? a_blocks(n, mixed != 0) : 0;
+    *c_b = n > 0 ? contact_blocks(n, style, mixed != 0) : 0;
+    return TMPS_OK;
+}
+
+int tmps_batch_a(const tmps_instance* d_inst, const int32_t* d_block_inst, int32_t nblocks, int32_t mixed,
+                 void* stream) {
+    if (!d_inst || !d_block_inst || nblocks < 0) return TMPS_ERR_BAD_ARG;
+    if (nblocks == 0) return TMPS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (mixed) launch_pdl(kb_a32, nblocks, kBlockA, s, d_inst, d_block_inst);
+    else launch_pdl(kb_a64, nblocks, kBlockA, s, d_inst, d_block_inst);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_batch_c(const tmps_instance* d_inst, const int32_t* d_block_inst, int32_t nblocks, int32_t style,
+                 int32_t mixed, void* stream) {
+    if (!d_inst || !d_block_inst || nblocks < 0 || style < 0 || style > 4) return TMPS_ERR_BAD_ARG;
+    if (nblocks == 0) return TMPS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+#define TMPS_LAUNCH_BC(ST)                                                         \
+    if (mixed) launch_pdl(kb_cf<ST, true>, nblocks, kBlockC, s, d_inst, d_block_inst); \
+    else launch_pdl(kb_cf<ST, false>, nblocks, kBlockC, s, d_inst, d_block_inst);
+    switch (style) {
+        case 0: TMPS_LAUNCH_BC(0) break;
+        case 1: TMPS_LAUNCH_BC(1) break;
+        case 2: TMPS_LAUNCH_BC(2) break;
+        case 3: TMPS_LAUNCH_BC(3) break;
+        default: TMPS_LAUNCH_BC(4) break;
+    }
+#undef TMPS_LAUNCH_BC
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_batch_servo(const tmps_instance* d_inst, int32_t ninst, int32_t* d_status, void* stream) {
+    if (!d_inst || ninst < 0 || !d_status) return TMPS_ERR_BAD_ARG;
+    if (ninst == 0) return TMPS_OK;
+    launch_pdl(kb_s, ninst, kBlockS, (cudaStream_t)stream, d_inst, d_status);
+    note_launches(1);
+    return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
+}
+
+int tmps_batch_state(const tmps_instance* d_inst, int32_t ninst, int64_t* d_state, void* stream) {
+    if (!d_inst || ninst < 0 || !d_state) return TMPS_ERR_BAD_ARG;
+    if (ninst == 0) return TMPS_OK;
+    kb_state<<<grid_for(ninst, 128), 128, 0, (cudaStream_t)stream>>>(d_inst, ninst, d_state);
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }

@@ -118,8 +118,9 @@ class FusedEngine:
 
     # ------------------------------------------------------------ lifecycle
 
-    def begin(self) -> None:
-        """After Simulation.init_simulation(): hand the state to the fused step."""
+    def begin(self, stop_step: int | None = None) -> None:
+        """After Simulation.init_simulation(): hand the state to the fused step.  `stop_step`: fused
+        launches do nothing once the step count reaches it (batched runs)."""
         sim = self.sim
         atom, nl = sim.atom, sim.neighbor
         n = atom.nlocal
@@ -143,6 +144,7 @@ class FusedEngine:
             e.gamma_lin, e.gamma_ang = self.cundall.gamma_lin, self.cundall.gamma_ang
         e.trigger_sq = 0.25 * nl.skin * nl.skin
         e.remap_scale[0] = e.remap_scale[1] = e.remap_scale[2] = 1.0
+        e.stop_step = (1 << 62) if stop_step is None else int(stop_step)
         _device.push_struct(self._eng, e)
         if self.deform is not None:
             fx = self.deform
@@ -185,6 +187,20 @@ class FusedEngine:
         with _device.timed("fused_s"):
             rc = L.tmps_fused_servo(dbox, self._servo_ptr(), eng, self.part.data_ptr(), self.status.data_ptr(), st)
         _lib.check(rc, "tmps_fused_servo")
+
+    def instance(self, a_first: int, a_blocks: int, c_first: int, c_blocks: int) -> _lib.Instance:
+        """This system's descriptor for a batched run (tmps_instance)."""
+        sim = self.sim
+        d = _lib.Instance()
+        d.a = self.atoms()
+        d.nl = sim.history.cstruct(sim.neighbor)
+        d.p = sim.pair_style.params
+        d.box = sim.domain.dbox
+        d.eng = self._eng.data_ptr()
+        d.servo = self._servo_ptr()
+        d.scratch = self.part.data_ptr()
+        d.a_first, d.a_blocks, d.c_first, d.c_blocks = a_first, a_blocks, c_first, c_blocks
+        return d
 
     def _engine_state(self) -> _lib.Engine:
         return _device.pull_struct(self._eng, _lib.Engine)

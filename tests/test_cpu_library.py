@@ -37,7 +37,8 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts_match_header(tmp_path):
     from taichimps_gb300 import _lib
     structs = {"tmps_box": _lib.Box, "tmps_atoms": _lib.Atoms, "tmps_nlist": _lib.NList,
-               "tmps_pair_params": _lib.PairParams, "tmps_servo": _lib.Servo, "tmps_engine": _lib.Engine}
+               "tmps_pair_params": _lib.PairParams, "tmps_servo": _lib.Servo, "tmps_engine": _lib.Engine,
+               "tmps_instance": _lib.Instance}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
