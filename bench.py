@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="config2", choices=["config2", "ensemble"],
+                    help="config2: the 1M-sphere servo run (default); ensemble: the batched-instances run")
+    ap.add_argument("--instances", type=int, default=512, help="ensemble: number of instances")
     return ap.parse_args()
 
 
@@ -334,6 +337,82 @@ def reference_arm(args, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ----------------------------------------------------------------- ensemble
+
+ENSEMBLE_METRIC = "atom-steps/s, batched ensemble of independent servo packings vs looped single solves"
+
+
+def ensemble_instance(G, seed, k, precision):
+    """Instance k of the ensemble: sphere count log-uniform [500, 16000], kn log-uniform [1e4, 1e6], xmu
+    U[0.1, 0.8], kt 2/7 kn, gamman 50 (gammat 25, dampflag 1: not given, as in the other runs), d U[0.8, 1.2],
+    rho 2.5, phi 0.45, isotropic pressure servo to 1.0 (gain 1e-3, max/rate 1e-4, couple xyz, remap x)."""
+    from taichimps_gb300.packing import make_packing_box
+    rng = np.random.default_rng([seed, k])
+    n = int(round(math.exp(rng.uniform(math.log(500), math.log(16000)))))
+    kn = float(math.exp(rng.uniform(math.log(1e4), math.log(1e6))))
+    xmu = float(rng.uniform(0.1, 0.8))
+    pk = make_packing_box(n, 0.8, 1.2, 0.45, seed * 1_000_003 + k)
+    dom = G.Domain(boxlo=[0.0] * 3, boxhi=[float(v) for v in pk["L"]], boundary=("p", "p", "p"))
+    atom = G.AtomSystem(max_atoms=n)
+    atom.add_particles(x=pk["x"], radius=pk["radius"], density=2.5, v=pk["v"])
+    nl = G.NeighborList(domain=dom, skin=SKIN, max_atoms=n, max_neighbors_per_atom=16)
+    hist = G.ContactHistory(max_atoms=n, max_neighbors=16)
+    pair = G.GranHertzHistory(domain=dom, kn=kn, kt=kn * 2.0 / 7.0, gamman=50.0, gammat=25.0, xmu=xmu, dampflag=1)
+    sim = G.Simulation(domain=dom, atom=atom, neighbor=nl, history=hist, pair=pair, dt=DT, precision=precision)
+    sim.add_fix(G.FixNVESphere(domain=dom))
+    sim.add_fix(G.FixDeformPressure(domain=dom, **DEFORM))
+    return sim
+
+
+def run_ensemble(args):
+    """Both arms on the same instances: W warm-up steps (with the setup) through the arm, then K timed steps
+    continuing the run (run ... pre no): the batched engine, then every instance looped on its own."""
+    import torch
+    import taichimps_gb300 as G
+    K, W, m = args.steps, args.warmup, args.instances
+    prec = "mixed" if args.precision == "both" else args.precision
+    batch = [ensemble_instance(G, args.seed, k, prec) for k in range(m)]
+    natoms = sum(s.atom.nlocal for s in batch)
+    eng = G.BatchedEngine(batch, precision=prec)
+    eng.run(W)
+    for s in batch:
+        s.run_pre = False
+    torch.cuda.synchronize()
+    r0 = eng.graph_replays
+    t0 = time.perf_counter()
+    eng.run(K)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    launches_batch = 3 * eng.chunk * (eng.graph_replays - r0)
+    del eng, batch
+    torch.cuda.empty_cache()
+    looped = [ensemble_instance(G, args.seed, k, prec) for k in range(m)]
+    for s in looped:
+        s.run(W)
+        s.run_pre = False
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in looped:
+        s.run(K)
+    torch.cuda.synchronize()
+    t_loop = time.perf_counter() - t0
+    sizes = [s.atom.nlocal for s in looped]
+    return {"metric": ENSEMBLE_METRIC, "value": natoms * K / t_batch, "unit": UNIT, "n_gpus": 1, "steps": K,
+            "warmup": W, "ms_per_step": 1e3 * t_batch / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64 mixed" if prec == "mixed" else "f64",
+            "data": "synthetic: seeded FCC-site packings per instance in a lattice-shaped periodic box "
+                    "(taichimps_gb300.packing.make_packing_box)",
+            "config": {"workload": f"{m} independent periodic packings, gran/hertz/history with per-instance kn "
+                                   "(log-uniform 1e4..1e6) and xmu (U 0.1..0.8), isotropic pressure servo to 1.0, "
+                                   "dt 5e-5", "instances": m, "total_atoms": natoms,
+                       "atoms_min": min(sizes), "atoms_max": max(sizes), "precision": prec},
+            "looped_single_solves": {"value": natoms * K / t_loop, "seconds": t_loop,
+                                     "how": "Simulation.run of each instance in turn (its own fused step, CUDA "
+                                            "graphs), same steps"},
+            "speedup_vs_looped": t_loop / t_batch, "batched_seconds": t_batch,
+            "gpu_launches_batched": launches_batch}
+
+
 # ----------------------------------------------------------------- main
 
 
@@ -356,6 +435,14 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "ensemble":
+        if args.impl != "ours" or world > 1:
+            print(json.dumps({"impl": args.impl, "unavailable": "the ensemble workload runs on one GPU, ours only"}))
+            return
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps(run_ensemble(args)), flush=True)
+        return
     if args.impl == "reference":
         out = reference_arm(args, rank, world)
         if out is not None:

@@ -351,8 +351,8 @@ __device__ __forceinline__ void zero_force(const tmps_atoms& A, int i) {
 // build): per atom and per 32-atom group, the smallest gap |d| - (ri + rj)
 // over the rows, rounded down to FP32; -inf for an atom holding a live
 // contact (and its group) or when a periodic dimension has a single bin (the
-// image is then not fixed by the stencil).  Every flag word is set: each
-// atom's force may be nonzero.
+// image is then not fixed by the stencil).  Every atom's flag bit is set:
+// its force may be nonzero.
 __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, const tmps_box* __restrict__ B,
                                                      tmps_engine* __restrict__ E, int hist, int cull, uint32_t* flags,
                                                      float* gap, float* agap) {
@@ -394,7 +394,9 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
         for (int o = 16; o > 0; o >>= 1) gmin = fmin(gmin, __shfl_down_sync(0xffffffffu, gmin, o));
         if (lane == 0) {
             gap[g] = __double2float_rd(gmin);
-            flags[g] = 0xffffffffu;
+            // bits of existing atoms only: a set bit makes C clear that atom's force
+            const int rem = n - (g << 5);
+            flags[g] = rem >= 32 ? 0xffffffffu : (1u << rem) - 1u;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {

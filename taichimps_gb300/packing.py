@@ -29,13 +29,32 @@ def _fcc_sites(m: int) -> np.ndarray:
     return (g[:, None, :] + base[None, :, :]).reshape(-1, 3)
 
 
-def remove_overlaps(x: np.ndarray, radius: np.ndarray, L: float, max_iter: int = 500, margin: float = 1e-9):
-    """Push overlapping pairs apart until none overlaps (periodic cube of edge L).
+def remove_overlaps(x: np.ndarray, radius: np.ndarray, L, max_iter: int = 500, margin: float = 1e-9,
+                    relist: int = 0):
+    """Push overlapping pairs apart until none overlaps (periodic box of edge L, a scalar or three edges).
 
     Candidate pairs are found once (within 2 r_max plus a slack larger than
     the total displacement the pushes may add); later passes only look at
-    pairs with an atom that moved in the previous pass.
+    pairs with an atom that moved in the previous pass.  If the pushes moved
+    an atom beyond the slack, the candidate list is rebuilt and the removal
+    continues from there, up to `relist` times (else it raises).
     """
+    for attempt in range(relist + 1):
+        try:
+            return _remove_overlaps_once(x, radius, L, max_iter, margin)
+        except _BeyondSlack as e:
+            if attempt == relist:
+                raise RuntimeError("overlap removal moved atoms beyond the candidate-pair slack") from None
+            x = e.x
+
+
+class _BeyondSlack(Exception):
+    def __init__(self, x):
+        super().__init__("beyond slack")
+        self.x = x
+
+
+def _remove_overlaps_once(x, radius, L, max_iter, margin):
     from scipy.spatial import cKDTree
 
     x = np.mod(x, L)
@@ -58,7 +77,7 @@ def remove_overlaps(x: np.ndarray, radius: np.ndarray, L: float, max_iter: int =
             disp = x - x0
             disp -= L * np.round(disp / L)
             if np.sqrt((disp * disp).sum(1)).max() >= 0.5 * slack:
-                raise RuntimeError("overlap removal moved atoms beyond the candidate-pair slack")
+                raise _BeyondSlack(x)
             return x
         i, j, d, r, need = i[bad], j[bad], d[bad], r[bad], need[bad]
         r = np.maximum(r, 1e-12)
@@ -88,7 +107,45 @@ def make_packing(n: int, dmin: float, dmax: float, phi: float, seed: int, jitter
     a = L / m
     x = (sites[pick] + 0.25) * a + rng.uniform(-jitter, jitter, size=(n, 3)) * a
     radius = 0.5 * d
-    x = remove_overlaps(x, radius, L)
+    x = remove_overlaps(x, radius, L, relist=20)
+    v = rng.normal(0.0, vel_sigma, size=(n, 3)) if vel_sigma > 0.0 else np.zeros((n, 3))
+    return {"x": x, "radius": radius, "L": L, "v": v}
+
+
+def _fcc_sites_box(mx: int, my: int, mz: int) -> np.ndarray:
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(np.arange(mx), np.arange(my), np.arange(mz), indexing="ij"), -1).reshape(-1, 3)
+    return (g[:, None, :] + base[None, :, :]).reshape(-1, 3)
+
+
+def make_packing_box(n: int, dmin: float, dmax: float, phi: float, seed: int, jitter: float = 0.005,
+                     vel_sigma: float = 0.0):
+    """make_packing for any n: at solid fraction 0.45 with d up to 1.2 the FCC nearest-neighbour distance is
+    only just above the largest diameter, so the lattice must be nearly full.  The periodic box is shaped to
+    an FCC lattice of mx x my x mz cells (edges within 4:3 of each other) with the fewest sites >= n, at the
+    same solid fraction.  Returns dict(x, radius, L (three edges), v)."""
+    rng = np.random.default_rng(seed)
+    d = rng.uniform(dmin, dmax, size=n)
+    vol = float(np.sum(math.pi / 6.0 * d ** 3) / phi)
+    m0 = (n / 4.0) ** (1.0 / 3.0)
+    lo, hi = max(1, int(math.floor(0.7 * m0))), int(math.ceil(1.4 * m0)) + 1
+    best = None
+    for mx in range(lo, hi + 1):
+        for my in range(mx, hi + 1):
+            for mz in range(my, hi + 1):
+                sites = 4 * mx * my * mz
+                if sites < n or 3 * mz > 4 * mx:
+                    continue
+                if best is None or sites < best[0]:
+                    best = (sites, mx, my, mz)
+    _, mx, my, mz = best
+    a = (vol / (mx * my * mz)) ** (1.0 / 3.0)
+    L = a * np.array([mx, my, mz], dtype=np.float64)
+    sites = _fcc_sites_box(mx, my, mz)
+    pick = rng.choice(len(sites), size=n, replace=False)
+    x = (sites[pick] + 0.25) * a + rng.uniform(-jitter, jitter, size=(n, 3)) * a
+    radius = 0.5 * d
+    x = remove_overlaps(x, radius, L, relist=20)
     v = rng.normal(0.0, vel_sigma, size=(n, 3)) if vel_sigma > 0.0 else np.zeros((n, 3))
     return {"x": x, "radius": radius, "L": L, "v": v}
 
