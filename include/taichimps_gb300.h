@@ -436,6 +436,140 @@ int tmps_fused_settle(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, 
  * remap_pending. */
 int tmps_remap_x(const tmps_atoms* a, tmps_box* d_box, void* stream);
 
+/* ---- differentiable run (hand-written adjoint) --------------------------
+ * gran/hertz/history (GRANULAR/hertz_history.py:57-171) + fix nve/sphere
+ * (EXTRA_FIX/nve_sphere.py:43-96) + fix deform/pressure with x/y/z styles
+ * none, erate and pressure, couple and max/rate, remap x
+ * (EXTRA_FIX/deform_pressure.py:493-530, 583-702), in FP64 on a fully
+ * periodic orthogonal box.  Atoms stay in the caller's order (never
+ * re-sorted); contacts are a half pair list (i < j) sorted by (i, j) with
+ * the history in the i -> j sense.  Per-atom sums gather over the pairs in a
+ * fixed order (no atomics), so a run is bit-reproducible.  The adjoint of a
+ * step replays the forward's recorded masks (contact on, Coulomb slip,
+ * |shear| != 0, damping clamp; the servo's max/rate clamp): no smoothing.
+ * All arrays are device memory owned by the caller; [3][n] is
+ * component-major. */
+
+typedef struct tmps_adj_params {
+    double kn, kt, gamman, gammat, xmu;
+    double dt;
+    int32_t limit_damping;
+    int32_t pad_;
+} tmps_adj_params;
+
+typedef struct tmps_adj_servo {
+    int32_t style[3];    /* 0 none, 1 erate, 8 pressure (the codes of tmps_servo) */
+    int32_t couple;      /* 0 none, 1 xyz, 2 xy, 3 yz, 4 xz */
+    int32_t normalize;   /* normalize/pressure */
+    int32_t pad_;
+    double rate[3], ptarget[3], pgain[3];
+    double lo_start[3], hi_start[3];
+    double max_rate;
+} tmps_adj_servo;
+
+/* Box after a step (record s; record 0 is the box at setup), device. */
+typedef struct tmps_adj_rec {
+    double lo[3], prd[3], cum[3];
+    double w[6];         /* virial (pair + kinetic) total of step s, [xx, yy, zz, xy, xz, yz] */
+    double q;            /* deviatoric stress p_zz - (p_xx + p_yy) / 2 of step s */
+    double elapsed;      /* servo time of step s */
+    int32_t clamp;       /* bit d: axis d's servo rate hit max/rate */
+    int32_t pad_;
+} tmps_adj_rec;
+
+typedef struct tmps_adj_sys {
+    int32_t n;
+    int32_t npairs;
+    double* x;           /* [3][n] state at the end of the last step */
+    double* v;
+    double* w;
+    double* f;           /* forces and torques of the last step */
+    double* t;
+    const double* radius;   /* [n] */
+    const double* mass;     /* [n] */
+    double* shear;          /* [3][npairs] */
+    const int32_t* pi;      /* [npairs] */
+    const int32_t* pj;      /* [npairs] */
+    const int32_t* ibeg;    /* [n + 1]: pairs with pi == a are ibeg[a] .. ibeg[a + 1] - 1 */
+    const int32_t* jbeg;    /* [n + 1]: jlist[jbeg[a] .. jbeg[a + 1] - 1] are the pairs with pj == a */
+    const int32_t* jlist;   /* [npairs] */
+} tmps_adj_sys;
+
+/* One step's record for the reverse pass. */
+typedef struct tmps_adj_tape {
+    double* xh;          /* [3][n] after the first half-kick and the drift */
+    double* vh;
+    double* wh;
+    double* f;           /* [3][n] forces and torques the step computed */
+    double* t;
+    double* shear;       /* [3][npairs] history entering the contact pass */
+    uint8_t* mask;       /* [npairs] */
+} tmps_adj_tape;
+
+/* Adjoint state, carried backwards step by step. */
+typedef struct tmps_adj_bar {
+    double* x;           /* [3][n] */
+    double* v;
+    double* w;
+    double* f;
+    double* t;
+    double* shear;       /* [3][npairs] */
+    double* radius;      /* [n] dL/dr through radius directly (mass terms are in `mass`) */
+    double* mass;        /* [n] dL/dm */
+    double* params;      /* [8]: dL/d kn, kt, gamman, gammat, xmu */
+    double* box;         /* [2][9]: (lo, prd, cum) adjoints of the boxes of records n and n + 1, by parity */
+} tmps_adj_bar;
+
+/* Workspace for the adjoint-run calls (bytes). */
+int64_t tmps_adj_workspace_bytes(int32_t n, int32_t npairs);
+
+/* Pair list build (NeighborList.build_neighbor_list, neighbor.py:305-369, as
+ * a half list in the caller's order): pairs i < j with |d|^2 < (ri + rj +
+ * skin)^2 under the minimum image.  First call with d_pj = NULL fills
+ * d_count[i]; the second, with d_ibeg = exclusive prefix of the counts, fills
+ * d_pi / d_pj in (i, j) order. */
+int tmps_adj_pairs(int32_t n, const double* d_x, const double* d_radius, const tmps_adj_rec* d_box, double skin,
+                   int32_t* d_count, const int32_t* d_ibeg, int32_t* d_pi, int32_t* d_pj, void* stream);
+
+/* For each old pair, its index in a new list (-1 if gone); the history
+ * carried across a rebuild (contact_history.py:91-139 keyed by the pair). */
+int tmps_adj_pair_map(int32_t nold, const int32_t* d_old_pi, const int32_t* d_old_pj, const int32_t* d_new_ibeg,
+                      const int32_t* d_new_pj, int32_t* d_map, void* stream);
+/* reverse = 0: new[map[p]] = old[p] (new zeroed first); 1: old[p] = new[map[p]] or 0. */
+int tmps_adj_carry(int32_t nold, int32_t nnew, const int32_t* d_map, double* d_old, double* d_new, int32_t reverse,
+                   void* stream);
+
+/* Setup force evaluation (Simulation.setup: pair compute with shearupdate
+ * off) on the state: f, t and the history; `tape` records the history and
+ * the masks. */
+int tmps_adj_setup(const tmps_adj_sys* s, const tmps_adj_params* p, const tmps_adj_rec* d_box,
+                   const tmps_adj_tape* tape, void* work, void* stream);
+
+/* First half of step s: half-kick and drift into tape->xh/vh/wh; the
+ * largest |xh - d_xbuild|^2 goes to *d_disp (as FP64 bits, for the host's
+ * rebuild decision, neighbor.py:214-245). */
+int tmps_adj_initial(const tmps_adj_sys* s, const tmps_adj_params* p, const tmps_adj_tape* tape,
+                     const double* d_xbuild, uint64_t* d_disp, void* stream);
+
+/* Rest of step s: contacts (shearupdate on), second half-kick, pressure,
+ * servo and remap; writes d_rec[s] from d_rec[s - 1]. */
+int tmps_adj_finish(const tmps_adj_sys* s, const tmps_adj_params* p, const tmps_adj_servo* sv,
+                    const tmps_adj_tape* tape, tmps_adj_rec* d_rec, int64_t step, void* work, void* stream);
+
+/* Reverse of step s (from d_rec[s - 1] to d_rec[s]), given the adjoint of
+ * the state after it in `b`; leaves the adjoint of the state before it.
+ * `qbar` is dL/dq of step s; d_fprev / d_tprev the forces step s started
+ * from. */
+int tmps_adj_step_back(const tmps_adj_sys* s, const tmps_adj_params* p, const tmps_adj_servo* sv,
+                       const tmps_adj_tape* tape, const tmps_adj_rec* d_rec, int64_t step, const double* d_fprev,
+                       const double* d_tprev, double qbar, const tmps_adj_bar* b, void* work, void* stream);
+
+/* Reverse of the setup force evaluation: adds its radius, mass and
+ * parameter terms; `b->x`, `b->v`, `b->w` receive the adjoint of the
+ * initial state. */
+int tmps_adj_setup_back(const tmps_adj_sys* s, const tmps_adj_params* p, const tmps_adj_rec* d_box,
+                        const tmps_adj_tape* tape, const tmps_adj_bar* b, void* work, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

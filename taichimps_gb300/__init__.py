@@ -4,6 +4,7 @@ to GB300 (sm_103a CUDA behind a C ABI), behind the reference's own plug-in
 API (pair / fix / neighbor / history / compute classes driven by Simulation).
 """
 
+from .adjoint import AdjointRun, stress_curve
 from .atom import AtomSystem
 from .computes import ComputeContactAtom, Computes
 from .contact_history import ContactHistory
@@ -14,6 +15,6 @@ from .GRANULAR import GranHertz, GranHertzHistory, GranHooke, GranHookeHistory, 
 from .neighbor import NeighborList
 from .simulation import Simulation
 
-__all__ = ["AtomSystem", "BatchedEngine", "ComputeContactAtom", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
+__all__ = ["AdjointRun", "AtomSystem", "BatchedEngine", "ComputeContactAtom", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
            "FixDeformPressure", "FixNVESphere", "GranHertz", "GranHertzHistory", "GranHooke",
-           "GranHookeHistory", "GranularPair", "PairGranular", "NeighborList", "Simulation"]
+           "GranHookeHistory", "GranularPair", "PairGranular", "NeighborList", "Simulation", "stress_curve"]

@@ -115,6 +115,49 @@ class Instance(ctypes.Structure):
     ]
 
 
+class AdjParams(ctypes.Structure):
+    """tmps_adj_params"""
+
+    _fields_ = [("kn", c_f64), ("kt", c_f64), ("gamman", c_f64), ("gammat", c_f64), ("xmu", c_f64), ("dt", c_f64),
+                ("limit_damping", c_i32), ("pad_", c_i32)]
+
+
+class AdjServo(ctypes.Structure):
+    """tmps_adj_servo"""
+
+    _fields_ = [("style", c_i32 * 3), ("couple", c_i32), ("normalize", c_i32), ("pad_", c_i32),
+                ("rate", c_f64 * 3), ("ptarget", c_f64 * 3), ("pgain", c_f64 * 3),
+                ("lo_start", c_f64 * 3), ("hi_start", c_f64 * 3), ("max_rate", c_f64)]
+
+
+class AdjRec(ctypes.Structure):
+    """tmps_adj_rec"""
+
+    _fields_ = [("lo", c_f64 * 3), ("prd", c_f64 * 3), ("cum", c_f64 * 3), ("w", c_f64 * 6), ("q", c_f64),
+                ("elapsed", c_f64), ("clamp", c_i32), ("pad_", c_i32)]
+
+
+class AdjSys(ctypes.Structure):
+    """tmps_adj_sys"""
+
+    _fields_ = [("n", c_i32), ("npairs", c_i32), ("x", c_vp), ("v", c_vp), ("w", c_vp), ("f", c_vp), ("t", c_vp),
+                ("radius", c_vp), ("mass", c_vp), ("shear", c_vp), ("pi", c_vp), ("pj", c_vp), ("ibeg", c_vp),
+                ("jbeg", c_vp), ("jlist", c_vp)]
+
+
+class AdjTape(ctypes.Structure):
+    """tmps_adj_tape"""
+
+    _fields_ = [("xh", c_vp), ("vh", c_vp), ("wh", c_vp), ("f", c_vp), ("t", c_vp), ("shear", c_vp), ("mask", c_vp)]
+
+
+class AdjBar(ctypes.Structure):
+    """tmps_adj_bar"""
+
+    _fields_ = [("x", c_vp), ("v", c_vp), ("w", c_vp), ("f", c_vp), ("t", c_vp), ("shear", c_vp), ("radius", c_vp),
+                ("mass", c_vp), ("params", c_vp), ("box", c_vp)]
+
+
 TMPS_OK, TMPS_ERR_BAD_ARG, TMPS_ERR_CUDA, TMPS_ERR_TOO_LARGE = 0, 1, 2, 3
 NOALLOC_MAX_ATOMS, NOALLOC_MAX_CELLS = 1048576, 200000
 STATUS_NLIST_OVERFLOW, STATUS_NONFINITE, STATUS_BOX_NONPOSITIVE, STATUS_CELL_OVERFLOW = 1, 2, 4, 8
@@ -161,6 +204,21 @@ _SIGS = {
     "tmps_batch_c": (c_i32, [c_vp, c_vp, c_i32, c_i32, c_i32, c_vp]),
     "tmps_batch_servo": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
     "tmps_batch_state": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
+    "tmps_adj_workspace_bytes": (ctypes.c_int64, [c_i32, c_i32]),
+    "tmps_adj_pairs": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "tmps_adj_pair_map": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "tmps_adj_carry": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp]),
+    "tmps_adj_setup": (c_i32, [ctypes.POINTER(AdjSys), ctypes.POINTER(AdjParams), c_vp, ctypes.POINTER(AdjTape),
+                               c_vp, c_vp]),
+    "tmps_adj_initial": (c_i32, [ctypes.POINTER(AdjSys), ctypes.POINTER(AdjParams), ctypes.POINTER(AdjTape), c_vp,
+                                 c_vp, c_vp]),
+    "tmps_adj_finish": (c_i32, [ctypes.POINTER(AdjSys), ctypes.POINTER(AdjParams), ctypes.POINTER(AdjServo),
+                                ctypes.POINTER(AdjTape), c_vp, ctypes.c_int64, c_vp, c_vp]),
+    "tmps_adj_step_back": (c_i32, [ctypes.POINTER(AdjSys), ctypes.POINTER(AdjParams), ctypes.POINTER(AdjServo),
+                                   ctypes.POINTER(AdjTape), c_vp, ctypes.c_int64, c_vp, c_vp, c_f64,
+                                   ctypes.POINTER(AdjBar), c_vp, c_vp]),
+    "tmps_adj_setup_back": (c_i32, [ctypes.POINTER(AdjSys), ctypes.POINTER(AdjParams), c_vp,
+                                    ctypes.POINTER(AdjTape), ctypes.POINTER(AdjBar), c_vp, c_vp]),
 }
 
 _lib: ctypes.CDLL | None = None

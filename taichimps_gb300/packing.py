@@ -162,3 +162,58 @@ def config2(seed: int = 2, n: int = 1_000_000):
     p = make_packing(n, 0.8, 1.2, 0.45, seed)
     p["density"] = 2.5
     return p
+
+
+def compress_packing(n: int, seed: int, dmin: float = 0.8, dmax: float = 1.2, density: float = 2.5,
+                     kn: float = 1.0e5, xmu: float = 0.5, ptarget: float = 1.0, pgain: float = 1.0,
+                     max_rate: float = 0.005, cycles: int = 100, relax_cycles: int = 10, cycle_steps: int = 2000,
+                     dt: float = 5e-4, precision: str = "fp64", phi0: float = 0.3, jitter: float = 0.3):
+    """An isotropically compressed packing: `make_packing_box` at solid
+    fraction `phi0` with the sites jittered by `jitter` lattice constants (a
+    disordered gas; sites on an unjittered lattice would jam as a crystal of
+    the largest spheres), then gran/hertz/history (kn, kt = 2/7 kn, gamman 50,
+    gammat 25, xmu) with Cundall damping 0.7 and deform/pressure on x/y/z
+    (target `ptarget`, couple xyz, remap x).  The run is cut into cycles of
+    `cycle_steps` steps that each start at rest: Hertz collisions are nearly
+    elastic and Cundall damping does not slow a free sphere, so without the
+    quench the servo would stop on the kinetic pressure of a granular gas.
+    `cycles` at `max_rate`, then `relax_cycles` at a tenth of it.  The rate
+    is kept well below (equilibrium overlap) / (diameter x contact time) --
+    about 0.01 at kn 1e5 and p 1 -- or the contacts overshoot and the servo
+    stops on dynamic pressure.  Returns
+    positions wrapped into the final box, radii, box edges and lower corner,
+    the last pressure tensor and the solid fraction.  Runs on the GPU path."""
+    from . import (AtomSystem, ContactHistory, Domain, FixDampingCundall, FixDeformPressure, FixNVESphere,
+                   GranHertzHistory, NeighborList, Simulation)
+
+    p = make_packing_box(n, dmin, dmax, phi0, seed, jitter=jitter)
+    L0 = [float(v) for v in p["L"]]
+    state = {"x": p["x"], "lo": [0.0] * 3, "hi": L0}
+    tensor = np.zeros(6)
+    for c in range(cycles + relax_cycles):
+        rate = max_rate if c < cycles else 0.1 * max_rate
+        dom = Domain(boxlo=state["lo"], boxhi=state["hi"], boundary=("p", "p", "p"))
+        atom = AtomSystem(max_atoms=n)
+        atom.add_particles(x=state["x"], radius=p["radius"], density=density)
+        nl = NeighborList(domain=dom, skin=0.1, max_atoms=n, max_neighbors_per_atom=32)
+        hist = ContactHistory(max_atoms=n, max_neighbors=32)
+        pair = GranHertzHistory(domain=dom, kn=kn, kt=kn * 2.0 / 7.0, gamman=50.0, gammat=25.0, xmu=xmu,
+                                dampflag=1)
+        sim = Simulation(domain=dom, atom=atom, neighbor=nl, history=hist, pair=pair, dt=dt, precision=precision)
+        sim.add_fix(FixNVESphere(domain=dom))
+        sim.add_fix(FixDampingCundall(domain=dom, gamma_lin=0.7, gamma_ang=0.7))
+        fx = FixDeformPressure(domain=dom, axes={d: {"style": "pressure", "ptarget": ptarget, "pgain": pgain}
+                                                for d in "xyz"}, couple="xyz", max_rate=rate, remap="x")
+        sim.add_fix(fx)
+        fx.record_pressure(4)
+        sim.run(cycle_steps)
+        tensor = fx.pressure_history([sim.timestep])[0]
+        dom.pull()
+        lo = np.array(dom.boxlo, dtype=np.float64)
+        prd = np.array(dom.boxhi, dtype=np.float64) - lo
+        x = atom.x.to_numpy()
+        state = {"x": lo + np.mod(x - lo, prd), "lo": [float(a) for a in lo], "hi": [float(a) for a in lo + prd]}
+    lo, hi = np.array(state["lo"]), np.array(state["hi"])
+    vol_s = float(np.sum((4.0 / 3.0) * np.pi * p["radius"] ** 3))
+    return {"x": state["x"], "radius": p["radius"], "lo": lo, "L": hi - lo, "pressure": tensor,
+            "phi": vol_s / float(np.prod(hi - lo)), "density": density}
