@@ -68,7 +68,7 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="config2", choices=["config2", "ensemble"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "ensemble", "adjoint"],
                     help="config2: the 1M-sphere servo run (default); ensemble: the batched-instances run")
     ap.add_argument("--instances", type=int, default=512, help="ensemble: number of instances")
     return ap.parse_args()
@@ -430,11 +430,74 @@ def rel(a, b):
     return abs(a - b) / abs(b) if b != 0.0 else (0.0 if a == 0.0 else float("inf"))
 
 
+ADJOINT_METRIC = "seconds per gradient of a stress-curve loss (forward + adjoint), triaxial calibration run"
+
+
+def run_adjoint(args):
+    """The calibration run's gradient: a packing compressed by the quenched isotropic servo
+    (packing.compress_packing), then x/y pressure servo at 1.0 and z erate -1e-3 with remap x,
+    gran/hertz/history kn 1e5, kt 2/7 kn, gamman 50, gammat 25, xmu 0.5, dt 5e-5; the loss is the
+    squared difference of the deviatoric stress every 50 steps from the curve of kn 1.3e5, xmu 0.4.
+    Times the forward (with checkpoints every 100 steps) and the reverse (recompute + adjoint)."""
+    import torch
+    from taichimps_gb300.adjoint import AdjointRun, stress_curve
+    from taichimps_gb300.packing import compress_packing
+    n, steps = args.n, args.steps
+    t0 = time.perf_counter()
+    pk = compress_packing(n, seed=args.seed)
+    t_pack = time.perf_counter() - t0
+    axes = {"x": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
+            "y": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
+            "z": {"style": "erate", "rate": -1e-3}}
+    run = AdjointRun(pk["x"], pk["radius"], pk["density"], pk["lo"], pk["lo"] + pk["L"], dt=5e-5, steps=steps,
+                     axes=axes, max_rate=1e-2, sample_every=50, checkpoint_every=100)
+    base = dict(kn=1.0e5, kt=1.0e5 * 2.0 / 7.0, gamman=50.0, gammat=25.0, xmu=0.5)
+    target = run.forward(**dict(base, kn=1.3e5, xmu=0.4)).clone()
+    T = lambda a: torch.tensor(a, dtype=torch.float64, requires_grad=True)
+    ps = {k: T(v) for k, v in base.items()}
+    r = torch.tensor(pk["radius"], dtype=torch.float64, device="cuda", requires_grad=True)
+    times = []
+    for rep in range(2):  # the second is timed (the first compiles nothing but warms the allocator)
+        for v in ps.values():
+            v.grad = None
+        r.grad = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q = stress_curve(run, ps["kn"], ps["kt"], ps["gamman"], ps["gammat"], ps["xmu"], r)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        loss = ((q - target) ** 2).sum()
+        loss.backward()
+        torch.cuda.synchronize()
+        times.append((t1 - t0, time.perf_counter() - t1))
+    t_f, t_b = times[-1]
+    grads = {k: float(v.grad) for k, v in ps.items()}
+    return {"metric": ADJOINT_METRIC, "value": t_f + t_b, "unit": "s", "n_gpus": 1, "steps": steps, "warmup": 1,
+            "ms_per_step": 1e3 * (t_f + t_b) / steps, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded packing compressed to p = 1 by the quenched isotropic servo "
+                    "(taichimps_gb300.packing.compress_packing)",
+            "config": {"workload": f"triaxial calibration gradient, {n} spheres, {steps} steps, q every 50 steps, "
+                                   "checkpoints every 100", "n_atoms": n, "phi": pk["phi"],
+                       "pressure_start": [float(a) for a in pk["pressure"][:3]]},
+            "forward_s": t_f, "reverse_s": t_b, "pack_s": t_pack, "rebuilds": run.rebuilds,
+            "loss": float(loss), "grad": dict(grads, radius_norm=float(r.grad.norm())),
+            "forward_atom_steps_per_s": n * steps / t_f, "gradient_atom_steps_per_s": n * steps / (t_f + t_b)}
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "adjoint":
+        if args.impl != "ours" or world > 1:
+            print(json.dumps({"impl": args.impl, "unavailable": "the reference has no differentiable path"}))
+            return
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps(run_adjoint(args)), flush=True)
+        return
     if args.workload == "ensemble":
         if args.impl != "ours" or world > 1:
             print(json.dumps({"impl": args.impl, "unavailable": "the ensemble workload runs on one GPU, ours only"}))
