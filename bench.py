@@ -68,7 +68,7 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="config2", choices=["config2", "ensemble", "adjoint"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "ensemble", "adjoint", "triaxial"],
                     help="config2: the 1M-sphere servo run (default); ensemble: the batched-instances run")
     ap.add_argument("--instances", type=int, default=512, help="ensemble: number of instances")
     return ap.parse_args()
@@ -430,6 +430,106 @@ def rel(a, b):
     return abs(a - b) / abs(b) if b != 0.0 else (0.0 if a == 0.0 else float("inf"))
 
 
+TRIAXIAL_METRIC = "atom-steps/s, triaxial test (pair granular, rolling resistance) with logging every 100 steps"
+E_MOD, POISSON = 5.0e6, 0.3
+KN_EQUIV = (4.0 / 3.0) * E_MOD / (2.0 * (1.0 - POISSON ** 2))  # hertz/material's 4/3 E* (same elastic form)
+
+
+def triaxial_packing(n, seed):
+    """The config-2 procedure at this size, at the stiffness of hertz/material E 5e6, nu 0.3."""
+    from taichimps_gb300.packing import compress_packing
+    return compress_packing(n, seed=seed, kn=KN_EQUIV, max_rate=5e-4, dt=2e-4, cycles=100, cycle_steps=12000,
+                            relax_cycles=10, phi0=0.4, jitter=0.25, precision="mixed")
+
+
+def triaxial_sim(G, pk, precision):
+    """pair granular hertz/material (E 5e6, coeff_restitution 0.5, nu 0.3), mindlin (kt from G*, xt 1,
+    friction 0.5), rolling epsd (k_roll 1e3, gamma_roll 50, mu_roll 0.1); nve/sphere; deform/pressure:
+    x and y pressure 1.0 (gain 0.1, max/rate 1e-2), z erate -1e-3, remap x; dt 5e-5."""
+    n = len(pk["radius"])
+    dom = G.Domain(boxlo=[float(a) for a in pk["lo"]], boxhi=[float(a) for a in pk["lo"] + pk["L"]],
+                   boundary=("p", "p", "p"))
+    atom = G.AtomSystem(max_atoms=n)
+    atom.add_particles(x=pk["x"], radius=pk["radius"], density=pk["density"])
+    nl = G.NeighborList(domain=dom, skin=0.1, max_atoms=n, max_neighbors_per_atom=32)
+    hist = G.ContactHistory(max_atoms=n, max_neighbors=32)
+    pair = G.PairGranular(domain=dom, normal="hertz/material", normal_coeffs=[E_MOD, 0.5, POISSON],
+                          damping="coeff_restitution", tangential="mindlin", tangential_coeffs=[None, 1.0, 0.5],
+                          rolling="epsd", rolling_coeffs=[1e3, 50.0, 0.1])
+    sim = G.Simulation(domain=dom, atom=atom, neighbor=nl, history=hist, pair=pair, dt=5e-5, precision=precision)
+    sim.add_fix(G.FixNVESphere(domain=dom))
+    fx = G.FixDeformPressure(domain=dom, axes={"x": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
+                                               "y": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
+                                               "z": {"style": "erate", "rate": -1e-3}},
+                             max_rate=1e-2, remap="x")
+    sim.add_fix(fx)
+    return sim, fx
+
+
+def triaxial_log(G, sim, fx, steps, every):
+    """Runs `steps` steps; every `every` steps logs the deviatoric stress q = p_zz - (p_xx + p_yy)/2,
+    the volumetric strain eps_v = 1 - V / V0 (compression positive) and the coordination number."""
+    import torch
+    n = sim.atom.nlocal
+    cn = G.ComputeContactAtom(max_atoms=n)
+    dom = sim.domain
+    dom.pull()
+    v0 = float(np.prod(np.array(dom.boxhi) - np.array(dom.boxlo)))
+    fx.record_pressure(8)
+    log = []
+    t_run = 0.0
+    for k in range(steps // every):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.run(every)
+        torch.cuda.synchronize()
+        t_run += time.perf_counter() - t0
+        sim.run_pre = False
+        P = fx.pressure_history([sim.timestep])[0]
+        dom.pull()
+        vol = float(np.prod(np.array(dom.boxhi) - np.array(dom.boxlo)))
+        counts = cn.compute(sim.atom, dom, sim.neighbor)
+        log.append((sim.timestep, float(P[2] - 0.5 * (P[0] + P[1])), 1.0 - vol / v0,
+                    float(np.mean(counts))))
+    return np.array(log), t_run
+
+
+def run_triaxial(args):
+    import torch
+    import taichimps_gb300 as G
+    n, steps = args.n, args.steps
+    t0 = time.perf_counter()
+    pk = triaxial_packing(n, args.seed)
+    t_pack = time.perf_counter() - t0
+    out = {}
+    for prec in ("mixed", "fp64"):
+        sim, fx = triaxial_sim(G, pk, prec)
+        log, t_run = triaxial_log(G, sim, fx, steps, 100)
+        out[prec] = {"log": log, "t": t_run}
+        del sim, fx
+        torch.cuda.empty_cache()
+    m, f = out["mixed"]["log"], out["fp64"]["log"]
+    qs = max(np.abs(f[:, 1]).max(), 1e-300)
+    dev = lambda a, b, k: float(np.abs(a[:, k] - b[:, k]).max())
+    first = lambda a, b, k, j: float(np.abs(a[:j, k] - b[:j, k]).max())
+    return {"metric": TRIAXIAL_METRIC, "value": n * steps / out["mixed"]["t"], "unit": "atom-steps/s", "n_gpus": 1,
+            "steps": steps, "warmup": 0, "ms_per_step": 1e3 * out["mixed"]["t"] / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 mixed",
+            "data": "synthetic: seeded packing compressed to p = 1 by the quenched isotropic servo at the "
+                    "hertz/material stiffness (taichimps_gb300.packing.compress_packing)",
+            "config": {"workload": f"triaxial test, {n} spheres, pair granular hertz/material + mindlin + rolling "
+                                   f"epsd, x/y pressure 1.0, z erate -1e-3, {steps} steps, log every 100",
+                       "n_atoms": n, "phi": pk["phi"], "pressure_start": [float(a) for a in pk["pressure"][:3]]},
+            "fp64_atom_steps_per_s": n * steps / out["fp64"]["t"], "mixed_over_fp64": out["fp64"]["t"] / out["mixed"]["t"],
+            "pack_s": t_pack,
+            "mixed_vs_fp64": {"q_max_abs_dev_over_max_q": dev(m, f, 1) / qs,
+                              "q_first_10_logs_over_max_q": first(m, f, 1, 10) / qs,
+                              "eps_v_max_abs_dev": dev(m, f, 2), "cn_max_abs_dev": dev(m, f, 3)},
+            "log_every": 100,
+            "log_fp64": [[int(a), b, c, d] for a, b, c, d in f[::10]],
+            "log_mixed": [[int(a), b, c, d] for a, b, c, d in m[::10]]}
+
+
 ADJOINT_METRIC = "seconds per gradient of a stress-curve loss (forward + adjoint), triaxial calibration run"
 
 
@@ -490,6 +590,14 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "triaxial":
+        if args.impl != "ours" or world > 1:
+            print(json.dumps({"impl": args.impl, "unavailable": "the triaxial workload runs on one GPU, ours only"}))
+            return
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps(run_triaxial(args)), flush=True)
+        return
     if args.workload == "adjoint":
         if args.impl != "ours" or world > 1:
             print(json.dumps({"impl": args.impl, "unavailable": "the reference has no differentiable path"}))

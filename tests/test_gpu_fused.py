@@ -270,3 +270,45 @@ def test_partial_last_group_flags_and_no_spurious_rebuild(gpu, oracle, precision
     words = eng.part[:4 * ng].view(torch.int32).cpu().numpy().view(np.uint32)
     assert (int(words[-1]) >> (n % 32)) == 0
     eng.finish()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_triaxial_loading_matches_oracle(gpu, oracle, precision):
+    """The triaxial loading (pair granular with mindlin and rolling EPSD; x and y pressure-servoed at
+    1.0, z strain-controlled at erate -1e-3, remap x) through the fused step: the deviatoric stress
+    q = p_zz - (p_xx + p_yy)/2 of every step, the box and the coordination number after 120 steps
+    against the oracle."""
+    from taichimps_gb300 import ComputeContactAtom
+    rng = np.random.default_rng(29)
+    x, r = dense_packing(rng, 343, 7.2, 0.5, 0.56)
+    deform = dict(axes={"x": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
+                        "y": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
+                        "z": {"style": "erate", "rate": -1e-3}}, max_rate=1e-2, remap="x")
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [7.2] * 3, pair="granular/rolling", dt=5e-5,
+                          deform=deform)
+    sim.precision = precision
+    fix = sim.fixes[-1]
+    fix.record_pressure(128)
+    steps = 120
+    sim.run(steps)
+    rows = fix.pressure_history(range(1, steps + 1))
+    q = rows[:, 2] - 0.5 * (rows[:, 0] + rows[:, 1])
+    osim.setup(steps)
+    oq = []
+    for _ in range(steps):
+        osim.step()
+        P = osim.last_pressure
+        oq.append(P[2] - 0.5 * (P[0] + P[1]))
+    oq = np.array(oq)
+    assert np.abs(oq).max() > 0
+    tol = 1e-10 if precision == "fp64" else MIXED_P
+    assert np.abs(q - oq).max() / np.abs(oq).max() < tol, np.abs(q - oq).max() / np.abs(oq).max()
+    sim.domain.pull()
+    np.testing.assert_allclose(np.array(sim.domain.boxhi) - np.array(sim.domain.boxlo), osim.domain.prd,
+                               rtol=1e-12 if precision == "fp64" else 1e-9)
+    cn = ComputeContactAtom(max_atoms=len(x)).compute(sim.atom, sim.domain, sim.neighbor)
+    ocn = osim.neighbor.contact_count(osim.atoms)
+    if precision == "fp64":
+        np.testing.assert_array_equal(cn, ocn)
+    else:
+        assert abs(cn.mean() - ocn.mean()) <= 0.02 * ocn.mean()
