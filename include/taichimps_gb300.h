@@ -436,6 +436,36 @@ int tmps_fused_settle(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, 
  * remap_pending. */
 int tmps_remap_x(const tmps_atoms* a, tmps_box* d_box, void* stream);
 
+/* ---- granular walls ------------------------------------------------------
+ * The wall is a contact partner of zero radius and infinite mass: radsum =
+ * Reff = r_i, meff = m_i, moment arm the full radius.  One history slot per
+ * atom, indexed by the atom's insertion index (tmps_atoms.uid) so it follows
+ * the atom through the neighbor build's re-sort. */
+typedef struct tmps_wall_params {
+    int32_t kind;            /* 0 plane (FixWallGran), 1 cylinder side (FixWallGranRegion) */
+    int32_t axis;            /* plane: normal axis; cylinder: cylinder axis (0, 1, 2) */
+    int32_t side;            /* plane: -1 wall below the atoms (normal +axis), +1 above;
+                                cylinder: -1 atoms inside, +1 outside */
+    int32_t history;         /* keep the shear history (the .../history styles) */
+    int32_t hertz;           /* cylinder: hertz normal, forces scaled by sqrt(r_i delta) */
+    int32_t limit_damping;
+    int32_t shear_axis;      /* plane: axis of the in-plane wall velocity, or -1 */
+    int32_t has_axis_bounds; /* cylinder: only atoms with axis_lo <= x_axis <= axis_hi */
+    double coord;            /* plane: wall position this step */
+    double vwall_n;          /* plane: wall velocity along its normal axis this step (wiggle) */
+    double vwall_s;          /* plane: in-plane wall velocity (shear) */
+    double c1, c2, radius;   /* cylinder: centre in the cross-section, radius */
+    double axis_lo, axis_hi;
+    double kn, kt, gamman, gammat, xmu;
+} tmps_wall_params;
+
+/* FixWallGran.post_force_kernel (EXTRA_FIX/wall_gran.py:143-228) for kind 0,
+ * FixWallGranRegion.post_force_kernel (EXTRA_FIX/wall_gran_region.py:134-276)
+ * for kind 1: adds the wall force and torque to f / torque.  d_shear
+ * double[3][nslots], d_touch int32[nslots] (nslots > every uid). */
+int tmps_wall_gran(const tmps_atoms* a, const tmps_wall_params* p, double dt, int32_t history_update,
+                   double* d_shear, int32_t* d_touch, int32_t nslots, void* stream);
+
 /* ---- differentiable run (hand-written adjoint) --------------------------
  * gran/hertz/history (GRANULAR/hertz_history.py:57-171) + fix nve/sphere
  * (EXTRA_FIX/nve_sphere.py:43-96) + fix deform/pressure with x/y/z styles

@@ -469,6 +469,83 @@ class OracleCundall:
                          _p(atoms.torque), _p(atoms.v), _p(atoms.omega))
 
 
+class _WallC(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in ("kind", "axis", "side", "history", "hertz", "limit_damping",
+                                             "shear_axis", "has_axis_bounds")] + \
+               [(k, ctypes.c_double) for k in ("coord", "vwall_n", "vwall_s", "c1", "c2", "radius", "axis_lo",
+                                                "axis_hi", "kn", "kt", "gamman", "gammat", "xmu")]
+
+
+class _OracleWall:
+    history_update = True
+
+    def _run(self, atoms, dt, w: _WallC):
+        if self.shear is None or len(self.touch) != atoms.n:
+            self.shear = np.zeros((atoms.n, 3))
+            self.touch = np.zeros(atoms.n, dtype=np.int32)
+        lib().or_wall(ctypes.byref(w), atoms.n, ctypes.c_double(dt), 1 if self.history_update else 0,
+                      _p(atoms.x), _p(atoms.v), _p(atoms.omega), _p(atoms.radius), _p(atoms.rmass),
+                      _p(atoms.f), _p(atoms.torque), _p(self.shear), _p(self.touch, _i32p))
+
+
+class OracleWallGran(_OracleWall):
+    """FixWallGran (EXTRA_FIX/wall_gran.py:39-242): plane wall, history or not, shear / wiggle motion."""
+
+    def __init__(self, wall_axis, wall_side, wall_coord, kn, gamman, kt, gammat, xmu, dampflag=1, history=True,
+                 limit_damping=False, shear_axis=-1, shear_vel=0.0, wiggle_amplitude=0.0, wiggle_period=0.0):
+        self.w = _WallC(kind=0, axis=int(wall_axis), side=int(wall_side), history=1 if history else 0, hertz=0,
+                        limit_damping=1 if limit_damping else 0, shear_axis=int(shear_axis), has_axis_bounds=0,
+                        vwall_s=float(shear_vel), kn=float(kn), kt=float(kt), gamman=float(gamman),
+                        gammat=0.0 if int(dampflag) == 0 else float(gammat), xmu=float(xmu))
+        self.wall_coord = float(wall_coord)
+        self.amp, self.period = float(wiggle_amplitude), float(wiggle_period)
+        self.elapsed = 0.0
+        self.shear = self.touch = None
+
+    def setup(self, nsteps_total, dt, n):
+        self.elapsed = 0.0
+
+    def post_force(self, atoms, dt):
+        # wall_gran.py:230-239
+        coord, vn = self.wall_coord, 0.0
+        if self.amp != 0.0:
+            omega_w = 2.0 * math.pi / self.period
+            arg = omega_w * self.elapsed
+            coord += self.amp * (1.0 - math.cos(arg))
+            vn = self.amp * omega_w * math.sin(arg)
+        self.w.coord, self.w.vwall_n = coord, vn
+        self._run(atoms, dt, self.w)
+        self.elapsed += dt
+
+
+class OracleWallGranRegion(_OracleWall):
+    """FixWallGranRegion (EXTRA_FIX/wall_gran_region.py:33-290): the side of a cylinder region."""
+
+    def __init__(self, axis=2, c1=0.0, c2=0.0, radius=1.0, side="in", axis_lo=None, axis_hi=None, fstyle="hooke",
+                 kn=1e5, gamman=0.0, kt=None, gammat=None, xmu=0.0, dampflag=1, history=None, limit_damping=False):
+        if isinstance(axis, str):
+            axis = {"x": 0, "y": 1, "z": 2}[axis.lower()]
+        if isinstance(side, str):
+            sd = -1 if side.lower() in ("in", "inside", "-1") else 1
+        else:
+            sd = -1 if side < 0 else 1
+        fstyle = fstyle.lower()
+        gt = float(gammat) if gammat is not None else 0.5 * float(gamman)
+        self.w = _WallC(kind=1, axis=int(axis), side=sd,
+                        history=1 if (fstyle.endswith("history") if history is None else history) else 0,
+                        hertz=1 if "hertz" in fstyle else 0, limit_damping=1 if limit_damping else 0, shear_axis=-1,
+                        has_axis_bounds=1 if (axis_lo is not None or axis_hi is not None) else 0,
+                        c1=float(c1), c2=float(c2), radius=float(radius),
+                        axis_lo=float(axis_lo) if axis_lo is not None else -1e30,
+                        axis_hi=float(axis_hi) if axis_hi is not None else 1e30,
+                        kn=float(kn), kt=float(kt) if kt is not None else 2.0 / 7.0 * float(kn), gamman=float(gamman),
+                        gammat=0.0 if int(dampflag) == 0 else gt, xmu=float(xmu))
+        self.shear = self.touch = None
+
+    def post_force(self, atoms, dt):
+        self._run(atoms, dt, self.w)
+
+
 PRESSURE_STYLES = ("pressure", "pressure/mean")
 
 
@@ -711,17 +788,24 @@ class OracleSim:
         self.setup_done = True
         self.atoms.clear_forces()
         self._reneighbor(force=True)
-        self.pair.compute(self.atoms, self.neighbor, self.history, self.domain, self.dt, shearupdate=False)
+        if self.pair is not None:
+            self.pair.compute(self.atoms, self.neighbor, self.history, self.domain, self.dt, shearupdate=False)
+        # simulation.py:198-203: the setup force evaluation does not advance fix histories
+        for fx in self.fixes:
+            fx.history_update = False
         for fx in self.fixes:
             if hasattr(fx, "post_force"):
                 fx.post_force(self.atoms, self.dt)
+        for fx in self.fixes:
+            fx.history_update = True
 
     def step(self) -> None:
         self.timestep += 1
         self.integrator.initial_integrate(self.atoms, self.dt)
         self._reneighbor()
         self.atoms.clear_forces()
-        self.pair.compute(self.atoms, self.neighbor, self.history, self.domain, self.dt)
+        if self.pair is not None:
+            self.pair.compute(self.atoms, self.neighbor, self.history, self.domain, self.dt)
         for fx in self.fixes:
             if hasattr(fx, "post_force"):
                 fx.post_force(self.atoms, self.dt)

@@ -733,3 +733,162 @@ void or_remap_x(int n, double* x, const double old_lo[3], const double old_prd[3
             x[3 * i + k] = new_prd[k] * lam + new_lo[k];
         }
 }
+
+/* Granular walls.  FixWallGran.post_force_kernel (EXTRA_FIX/wall_gran.py:143-228)
+ * for kind 0 (plane) and FixWallGranRegion.post_force_kernel
+ * (EXTRA_FIX/wall_gran_region.py:134-276) for kind 1 (cylinder side); every
+ * expression in the reference's order.  Per-atom history shear[n][3],
+ * touch[n]. */
+typedef struct or_wall_t {
+    int kind, axis, side, history, hertz, limit_damping, shear_axis, has_axis_bounds;
+    double coord, vwall_n, vwall_s, c1, c2, radius, axis_lo, axis_hi;
+    double kn, kt, gamman, gammat, xmu;
+} or_wall_t;
+
+static double wdot(const double* a, const double* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+static void wcross(const double* a, const double* b, double* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* linear_history_classic (with the cylinder's contact-radius factor) or the
+ * history-free dashpot with the Coulomb cap */
+static void wall_tangential(const or_wall_t* P, double dt, int upd, const double* n, const double* vtr, double vrel,
+                            double fscrit, double damp_t, double poly, double* sh, int* touch, double* fs) {
+    if (P->history) {
+        double hist[3] = {sh[0], sh[1], sh[2]}, fdamp[3];
+        if (*touch == 0) {
+            hist[0] = hist[1] = hist[2] = 0.0;
+            *touch = 1;
+        }
+        if (upd)
+            for (int k = 0; k < 3; ++k) hist[k] = hist[k] + vtr[k] * dt;
+        double shrmag = sqrt(wdot(hist, hist));
+        if (upd) {
+            double hn = wdot(hist, n);
+            for (int k = 0; k < 3; ++k) hist[k] = hist[k] - hn * n[k];
+        }
+        for (int k = 0; k < 3; ++k) {
+            fdamp[k] = -damp_t * vtr[k];
+            fs[k] = P->kind == 0 ? -P->kt * hist[k] + fdamp[k] : (-P->kt * poly) * hist[k] + fdamp[k];
+        }
+        double magfs = sqrt(wdot(fs, fs));
+        if (magfs > fscrit) {
+            if (shrmag != 0.0) {
+                double s = fscrit / magfs, kk = P->kind == 0 ? P->kt : P->kt * poly;
+                for (int k = 0; k < 3; ++k) {
+                    fs[k] = fs[k] * s;
+                    hist[k] = -(fs[k] - fdamp[k]) / kk;
+                }
+            } else {
+                fs[0] = fs[1] = fs[2] = 0.0;
+            }
+        }
+        for (int k = 0; k < 3; ++k) sh[k] = hist[k];
+    } else {
+        double ft = 0.0;
+        if (vrel != 0.0) ft = fmin(fscrit, damp_t * vrel) / vrel;
+        for (int k = 0; k < 3; ++k) fs[k] = -ft * vtr[k];
+    }
+}
+
+void or_wall(const or_wall_t* P, int n, double dt, int upd, const double* x, const double* v, const double* om,
+             const double* radius, const double* rmass, double* f, double* torque, double* shear, int32_t* touch_) {
+    for (int i = 0; i < n; ++i) {
+        const double* xi = x + 3 * i;
+        const double* vi = v + 3 * i;
+        const double* wi = om + 3 * i;
+        double ri = radius[i], mi = rmass[i];
+        double sh[3] = {0, 0, 0};
+        int touch = 0;
+        if (P->history) {
+            for (int k = 0; k < 3; ++k) sh[k] = shear[3 * i + k];
+            touch = touch_[i];
+        }
+        int contact = 0;
+        double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
+        if (P->kind == 0) {
+            double nrm[3] = {0, 0, 0}, vwall[3] = {0, 0, 0};
+            nrm[P->axis] = P->side == 1 ? -1.0 : 1.0;
+            vwall[P->axis] = P->vwall_n;
+            if (P->shear_axis >= 0) vwall[P->shear_axis] = P->vwall_s;
+            double dist = P->side == -1 ? xi[P->axis] - P->coord : P->coord - xi[P->axis];
+            double delta = ri - dist;
+            if (delta > 0.0) {
+                contact = 1;
+                double vr[3], vt[3], wr[3], c[3], vtr[3], fs[3], nf[3];
+                for (int k = 0; k < 3; ++k) vr[k] = vi[k] - vwall[k];
+                double vnnr = wdot(vr, nrm);
+                for (int k = 0; k < 3; ++k) {
+                    vt[k] = vr[k] - vnnr * nrm[k];
+                    wr[k] = ri * wi[k];
+                }
+                wcross(wr, nrm, c);
+                for (int k = 0; k < 3; ++k) vtr[k] = vt[k] - c[k];
+                double vrel = sqrt(wdot(vtr, vtr));
+                double damp_prefactor = mi * P->gamman;
+                double fntot = P->kn * delta - damp_prefactor * vnnr;
+                if (P->limit_damping == 1) fntot = fmax(fntot, 0.0);
+                double fscrit = P->xmu * fabs(fntot);
+                double damp_t = mi * P->gammat;
+                wall_tangential(P, dt, upd, nrm, vtr, vrel, fscrit, damp_t, 1.0, sh, &touch, fs);
+                wcross(nrm, fs, nf);
+                for (int k = 0; k < 3; ++k) {
+                    F[k] = fntot * nrm[k] + fs[k];
+                    T[k] = -ri * nf[k];
+                }
+            }
+        } else {
+            double pa = xi[P->axis];
+            if (!(P->has_axis_bounds == 1 && (pa < P->axis_lo || pa > P->axis_hi))) {
+                int a1 = P->axis == 0 ? 1 : 0, a2 = P->axis == 2 ? 1 : 2;
+                double d1 = xi[a1] - P->c1, d2 = xi[a2] - P->c2;
+                double r_perp = sqrt(d1 * d1 + d2 * d2);
+                if (r_perp > 1e-14) {
+                    double inv = 1.0 / r_perp, u1 = d1 * inv, u2 = d2 * inv;
+                    double sg = P->side == -1 ? -1.0 : 1.0;
+                    double nrm[3] = {0, 0, 0};
+                    nrm[a1] = sg * u1;
+                    nrm[a2] = sg * u2;
+                    double delta = P->side == -1 ? ri - (P->radius - r_perp) : ri - (r_perp - P->radius);
+                    if (delta > 0.0) {
+                        contact = 1;
+                        double c[3], vr[3], vrt[3], fs[3], nf[3];
+                        wcross(wi, nrm, c);
+                        for (int k = 0; k < 3; ++k) vr[k] = vi[k] - ri * c[k];
+                        double vn = wdot(vr, nrm);
+                        for (int k = 0; k < 3; ++k) vrt[k] = vr[k] - vn * nrm[k];
+                        double vrel = sqrt(wdot(vrt, vrt));
+                        double poly = P->hertz ? sqrt(ri * delta) : 1.0;
+                        double fn_elastic = P->kn * delta * poly;
+                        double damp_prefactor = mi * P->gamman * poly;
+                        double fntot = fn_elastic - damp_prefactor * vn;
+                        if (P->limit_damping == 1) fntot = fmax(fntot, 0.0);
+                        double fscrit = P->xmu * fabs(fntot);
+                        double damp_t = mi * P->gammat * poly;
+                        wall_tangential(P, dt, upd, nrm, vrt, vrel, fscrit, damp_t, poly, sh, &touch, fs);
+                        wcross(nrm, fs, nf);
+                        for (int k = 0; k < 3; ++k) {
+                            F[k] = fntot * nrm[k] + fs[k];
+                            T[k] = -ri * nf[k];
+                        }
+                    }
+                }
+            }
+        }
+        if (contact) {
+            for (int k = 0; k < 3; ++k) {
+                f[3 * i + k] += F[k];
+                torque[3 * i + k] += T[k];
+            }
+        } else {
+            touch = 0;
+            sh[0] = sh[1] = sh[2] = 0.0;
+        }
+        if (P->history) {
+            for (int k = 0; k < 3; ++k) shear[3 * i + k] = sh[k];
+            touch_[i] = touch;
+        }
+    }
+}

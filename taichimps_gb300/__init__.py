@@ -10,11 +10,12 @@ from .computes import ComputeContactAtom, Computes
 from .contact_history import ContactHistory
 from .domain import Domain
 from .ensemble import BatchedEngine
-from .EXTRA_FIX import Fix, FixDampingCundall, FixDeformPressure, FixNVESphere
+from .EXTRA_FIX import (Fix, FixDampingCundall, FixDeformPressure, FixNVESphere, FixWallGran,
+                        FixWallGranRegion)
 from .GRANULAR import GranHertz, GranHertzHistory, GranHooke, GranHookeHistory, GranularPair, PairGranular
 from .neighbor import NeighborList
 from .simulation import Simulation
 
 __all__ = ["AdjointRun", "AtomSystem", "BatchedEngine", "ComputeContactAtom", "Computes", "ContactHistory", "Domain", "Fix", "FixDampingCundall",
-           "FixDeformPressure", "FixNVESphere", "GranHertz", "GranHertzHistory", "GranHooke",
+           "FixDeformPressure", "FixNVESphere", "FixWallGran", "FixWallGranRegion", "GranHertz", "GranHertzHistory", "GranHooke",
            "GranHookeHistory", "GranularPair", "PairGranular", "NeighborList", "Simulation", "stress_curve"]

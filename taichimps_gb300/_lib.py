@@ -115,6 +115,16 @@ class Instance(ctypes.Structure):
     ]
 
 
+class WallParams(ctypes.Structure):
+    """tmps_wall_params"""
+
+    _fields_ = [("kind", c_i32), ("axis", c_i32), ("side", c_i32), ("history", c_i32), ("hertz", c_i32),
+                ("limit_damping", c_i32), ("shear_axis", c_i32), ("has_axis_bounds", c_i32),
+                ("coord", c_f64), ("vwall_n", c_f64), ("vwall_s", c_f64), ("c1", c_f64), ("c2", c_f64),
+                ("radius", c_f64), ("axis_lo", c_f64), ("axis_hi", c_f64), ("kn", c_f64), ("kt", c_f64),
+                ("gamman", c_f64), ("gammat", c_f64), ("xmu", c_f64)]
+
+
 class AdjParams(ctypes.Structure):
     """tmps_adj_params"""
 
@@ -204,6 +214,8 @@ _SIGS = {
     "tmps_batch_c": (c_i32, [c_vp, c_vp, c_i32, c_i32, c_i32, c_vp]),
     "tmps_batch_servo": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
     "tmps_batch_state": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
+    "tmps_wall_gran": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(WallParams), c_f64, c_i32, c_vp, c_vp, c_i32,
+                               c_vp]),
     "tmps_adj_workspace_bytes": (ctypes.c_int64, [c_i32, c_i32]),
     "tmps_adj_pairs": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "tmps_adj_pair_map": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

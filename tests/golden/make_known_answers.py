@@ -82,6 +82,74 @@ def _function(path: Path, name: str) -> ast.FunctionDef:
     raise KeyError(f"{name} not in {path}")
 
 
+def _eval(node, names: dict):
+    """Arithmetic of literals, resolved names, unary minus and np.sqrt (what the wall tests write)."""
+    if isinstance(node, ast.Constant):
+        return node.value
+    if isinstance(node, (ast.List, ast.Tuple)):
+        return [_eval(e, names) for e in node.elts]
+    if isinstance(node, ast.Name):
+        return names[node.id]
+    if isinstance(node, ast.UnaryOp) and isinstance(node.op, ast.USub):
+        return -_eval(node.operand, names)
+    if isinstance(node, ast.BinOp):
+        a, b = _eval(node.left, names), _eval(node.right, names)
+        return {ast.Add: a + b if not isinstance(a, list) else None, ast.Sub: a - b if not isinstance(a, list) else None,
+                ast.Mult: a * b if not isinstance(a, list) else None,
+                ast.Div: a / b if not isinstance(a, list) else None}[type(node.op)]
+    if isinstance(node, ast.Call) and getattr(node.func, "attr", None) == "sqrt":
+        return _eval(node.args[0], names) ** 0.5
+    raise ValueError(ast.dump(node))
+
+
+def _wall_case(fn: ast.FunctionDef, ctor: str) -> dict:
+    """Constructor keywords, particle 0's state, the step and the asserted values of one wall test."""
+    names, arrays, fields, expected, kwargs, dt = {}, {}, {}, [], None, None
+    for node in sorted((n for n in ast.walk(fn) if isinstance(n, ast.stmt)), key=lambda n: n.lineno):
+        if isinstance(node, ast.Assign) and len(node.targets) == 1:
+            t = node.targets[0]
+            if isinstance(t, ast.Name):
+                v = node.value
+                if isinstance(v, ast.Call) and getattr(v.func, "attr", None) == "full":
+                    arrays[t.id] = _eval(v.args[1], names)
+                else:
+                    try:
+                        names[t.id] = _eval(v, names)
+                    except (ValueError, KeyError):
+                        pass
+            elif isinstance(t, ast.Subscript) and isinstance(t.value, ast.Name):
+                try:
+                    arrays[t.value.id] = _eval(node.value, names)
+                except (ValueError, KeyError):
+                    pass
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Call):
+            f = node.func
+            name = f.attr if isinstance(f, ast.Attribute) else getattr(f, "id", None)
+            if name == ctor:
+                kwargs = {k.arg: _eval(k.value, names) for k in node.keywords if k.arg != "domain"}
+            elif name == "from_numpy" and isinstance(f.value, ast.Attribute):
+                arg = node.args[0]
+                if isinstance(arg, ast.Call) and getattr(arg.func, "attr", None) == "full":
+                    fields[f.value.attr] = _eval(arg.args[1], names)
+                elif isinstance(arg, ast.Name) and arg.id in arrays:
+                    fields[f.value.attr] = arrays[arg.id]
+            elif name == "post_force":
+                dt = _eval(node.args[1], names)
+        if isinstance(node, ast.Assert) and isinstance(node.test, ast.Call):
+            c = node.test
+            if getattr(c.func, "attr", None) == "isclose" and isinstance(c.args[0], ast.Subscript):
+                expected.append({"line": node.lineno, "of": c.args[0].value.id,
+                                 "k": ast.literal_eval(c.args[0].slice), "value": _eval(c.args[1], names)})
+    # particle 0 of the arrays the test set by index (x_np[0] = ...), zero where it set none
+    x0 = fields.get("x", [0.0, 0.0, 0.0])
+    v0 = fields.get("v", [0.0, 0.0, 0.0])
+    return {"fix": kwargs, "x": x0 if not isinstance(x0, float) else [x0] * 3,
+            "v": v0 if not isinstance(v0, float) else [v0] * 3,
+            "radius": fields["radius"], "rmass": fields["rmass"], "dt": dt,
+            "expected": sorted(expected, key=lambda e: e["line"])}
+
+
 def main(ref: Path) -> dict:
     rel = lambda p: str(p.relative_to(ref))
     out = {"source": "literal inputs and expected values of the reference's tests, read as text",
@@ -135,6 +203,25 @@ def main(ref: Path) -> dict:
         "cite": f"{rel(p)}:{fn.lineno}-{fn.end_lineno}", "domain": dom, "particles": parts, "skin": nl["skin"],
         # atom 0's neighbors (reference half list: j > i): atom 1 only
         "neighbors_of_0": [1],
+    }
+    p = ref / "tests" / "test_wall_region.py"
+    for name in ("test_fix_wall_gran_region_cylinder_in", "test_fix_wall_gran_region_cylinder_out",
+                 "test_fix_wall_gran_region_friction_and_torque", "test_fix_wall_gran_region_hertz"):
+        fn = _function(p, name)
+        case = _wall_case(fn, "FixWallGranRegion")
+        case["cite"] = f"{rel(p)}:{fn.lineno}-{fn.end_lineno}"
+        out["cases"]["wall_region_" + name.split("region_", 1)[1]] = case
+
+    p = ref / "tests" / "test_additional_models.py"
+    fn = _function(p, "test_pair_granular_and_wall")
+    c = _calls(fn)
+    pline, parts = c["add_particles"][0]
+    wline, wall = c["FixWallGran"][0]
+    out["cases"]["wall_plane_sign"] = {
+        "cite": f"{rel(p)}:{fn.lineno}-{wline + 5}", "particles": parts, "fix": wall,
+        "dt": [kw for _, kw in c["post_force"]][0]["dt"],
+        # the test asserts only that the wall pushes the particle away: f_x > 0
+        "expected_sign_fx": 1,
     }
     return out
 

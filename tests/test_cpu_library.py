@@ -40,7 +40,7 @@ def test_struct_layouts_match_header(tmp_path):
                "tmps_pair_params": _lib.PairParams, "tmps_servo": _lib.Servo, "tmps_engine": _lib.Engine,
                "tmps_instance": _lib.Instance, "tmps_adj_params": _lib.AdjParams, "tmps_adj_servo": _lib.AdjServo,
                "tmps_adj_rec": _lib.AdjRec, "tmps_adj_sys": _lib.AdjSys, "tmps_adj_tape": _lib.AdjTape,
-               "tmps_adj_bar": _lib.AdjBar}
+               "tmps_adj_bar": _lib.AdjBar, "tmps_wall_params": _lib.WallParams}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

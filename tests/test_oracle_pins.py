@@ -340,3 +340,51 @@ def test_rolling_resistance_torque(oracle):
     t_cap, h_cap = out[(0.0, "epsd")]
     np.testing.assert_allclose(t_cap, out[(0.0, "none")][0], rtol=1e-15, atol=0)
     np.testing.assert_array_equal(h_cap, np.zeros(3))
+
+
+WALL_CASES = [k for k in GOLDEN if k.startswith("wall_region_")]
+
+
+@pytest.mark.parametrize("case", WALL_CASES)
+def test_wall_region_known_answers(oracle, case):
+    """The reference's cylinder-wall known answers (tests/test_wall_region.py): one post_force call on
+    one particle; the reference asserts at rtol 1e-4."""
+    c = GOLDEN[case]
+    at = oracle.OracleAtoms(x=[c["x"]], radius=c["radius"], density=1.0, v=[c["v"]])
+    at.rmass[:] = c["rmass"]
+    fix = oracle.OracleWallGranRegion(**c["fix"])
+    fix.post_force(at, c["dt"])
+    got = {"f_res": at.f[0], "torque_res": at.torque[0]}
+    for e in c["expected"]:
+        assert got[e["of"]][e["k"]] == pytest.approx(e["value"], rel=1e-4, abs=1e-5), e
+
+
+def test_wall_plane_known_sign(oracle):
+    """tests/test_additional_models.py: a particle overlapping a plane wall at x = 0 is pushed away."""
+    c = GOLDEN["wall_plane_sign"]
+    p = c["particles"]
+    at = oracle.OracleAtoms(x=p["x"], radius=p["radius"], density=p["density"], v=p["v"])
+    fix = oracle.OracleWallGran(**c["fix"])
+    fix.post_force(at, c["dt"])
+    assert np.sign(at.f[0, 0]) == c["expected_sign_fx"]
+    # hooke, no damping: kn * (r - x)
+    assert at.f[0, 0] == pytest.approx(c["fix"]["kn"] * (p["radius"][0] - p["x"][0][0]), rel=1e-12)
+
+
+def test_wall_history_sticks_then_slides(oracle):
+    """Plane wall, hooke/history: the shear spring grows while the tangential force is under the Coulomb
+    bound, then the force saturates at xmu |fn| and the spring is rescaled to match (wall_gran.py:196-212)."""
+    at = oracle.OracleAtoms(x=[[0.5, 0.5, 0.09]], radius=0.1, density=1.0, v=[[1.0, 0.0, 0.0]])
+    fix = oracle.OracleWallGran(wall_axis=2, wall_side=-1, wall_coord=0.0, kn=1e4, gamman=0.0, kt=2e3,
+                                gammat=0.0, xmu=0.5)
+    fts = []
+    for _ in range(40):
+        at.f[:] = 0.0
+        fix.post_force(at, 1e-2)
+        fts.append(at.f[0, 0])
+    fn = 1e4 * 0.01
+    assert fts[0] == pytest.approx(-2e3 * 1.0 * 1e-2, rel=1e-12)   # kt |v| dt while sticking
+    assert fts[1] == pytest.approx(2.0 * fts[0], rel=1e-12)
+    assert fts[2] == pytest.approx(-0.5 * fn, rel=1e-12)          # capped at xmu |fn|
+    assert fts[-1] == pytest.approx(-0.5 * fn, rel=1e-12)
+    assert np.linalg.norm(fix.shear[0]) == pytest.approx(0.5 * fn / 2e3, rel=1e-12)
