@@ -135,7 +135,10 @@ typedef struct tmps_pair_params {
 
 /* Pressure servo / strain control for x, y, z (orthogonal box).
  * Styles: 0 none, 1 erate, 2 trate, 3 vel, 4 wiggle, 5 final, 6 delta,
- * 7 scale, 8 pressure, 9 pressure/mean (deform_pressure.py:76-82). */
+ * 7 scale, 8 pressure, 9 pressure/mean, 10 volume (deform_pressure.py:76-82).
+ * The volume style and the box style (isotropic volume or mean-pressure
+ * control of the whole box) run after the per-axis updates, in one thread,
+ * when `post` is set (deform_pressure.py:858-1001). */
 typedef struct tmps_servo {
     int32_t style[3];
     int32_t couple;     /* 0 none, 1 xyz, 2 xy, 3 yz, 4 xz */
@@ -152,7 +155,19 @@ typedef struct tmps_servo {
     int64_t nsteps_total; /* run length for final/delta/scale */
     int64_t step_count;   /* end_of_step calls, for nevery */
     int32_t nevery;
-    int32_t pad_;
+    int32_t post;         /* volume or box styles present: run the post-pass */
+    /* volume style links (_setup_volume_links, deform_pressure.py:358-380):
+     * vsub 0 one_from_one, 1 one_from_two, 2 two_from_one */
+    int32_t vsub[3], vfixed[3], vdyn1[3], vdyn2[3];
+    int32_t vol_balance_p;
+    int32_t box_style;    /* 0 none, 1 volume, 2 pressure (set_box) */
+    double vol_start;     /* box volume at setup */
+    double box_ptarget, box_pgain;
+    double box_vshift[3]; /* cumulative_vshift of the box pressure style */
+    /* last step's strain rate and pressure per axis (vol/balance/p) */
+    double prior_rate[3], prior_pressure[3];
+    int32_t saved;        /* prior_* hold a step */
+    int32_t pad2_;
 } tmps_servo;
 
 /* State of the fused step (tmps_fused_*), device-resident.  One step of

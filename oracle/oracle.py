@@ -568,22 +568,41 @@ class _Axis:
     lo_target: float = 0.0
     hi_target: float = 0.0
     cumulative_shift: float = 0.0
+    # volume style and vol/balance/p (deform_pressure.py:358-385, 905-956)
+    vol_start: float = 0.0
+    substyle: str = ""
+    fixed: int = -1
+    dynamic1: int = -1
+    dynamic2: int = -1
+    saved: bool = False
+    prior_rate: float = 0.0
+    prior_pressure: float = 0.0
+    pressure_now: float = 0.0
+    cumulative_vshift: list = field(default_factory=lambda: [0.0, 0.0, 0.0])
 
 
 class OracleDeform:
     """
     FixDeformPressure restricted to orthogonal x/y/z styles none, erate, trate,
-    vel, wiggle, final, delta, scale, pressure, pressure/mean with couple,
-    max/rate, normalize/pressure and remap x|v|none.  The arithmetic is that
-    of the host path (deform_pressure.py:758-857, 1113-1219); the device path
+    vel, wiggle, final, delta, scale, pressure, pressure/mean and volume, the
+    box style (volume or pressure), with couple, max/rate, normalize/pressure,
+    vol/balance/p and remap x|v|none.  The arithmetic is that of the host path
+    (deform_pressure.py:758-1001, 1113-1219); the device path
     (deform_pressure.py:598-702) computes the same expressions.
     """
 
     def __init__(self, domain: OracleDomain, axes: dict, couple="none", max_rate=0.0,
-                 normalize_pressure=False, remap="x", nevery=1):
+                 normalize_pressure=False, remap="x", nevery=1, box=None, vol_balance_p=False):
         self.domain = domain
         self.axes = [_Axis() for _ in range(3)]
-        for name, spec in axes.items():
+        self.set_box = _Axis()
+        if box is not None:
+            self.set_box.style = box["style"]
+            for k, v in box.items():
+                if k != "style":
+                    setattr(self.set_box, k, float(v))
+        self.vol_balance_p = bool(vol_balance_p)
+        for name, spec in (axes or {}).items():
             a = self.axes["xyz".index(name)]
             for k, v in spec.items():
                 setattr(a, k, v if isinstance(v, str) else float(v)) if k != "style" else setattr(a, "style", v)
@@ -602,6 +621,23 @@ class OracleDeform:
                     s.style = self.axes[ref].style
                     s.ptarget = self.axes[ref].ptarget
                     s.pgain = self.axes[ref].pgain
+        # _setup_volume_links (deform_pressure.py:358-385)
+        for i in range(3):
+            s = self.axes[i]
+            if s.style != "volume":
+                continue
+            o1, o2 = (i + 1) % 3, (i + 2) % 3
+            s1, s2 = self.axes[o1].style, self.axes[o2].style
+            if s1 == "none":
+                s.substyle, s.fixed, s.dynamic1 = "one_from_one", o1, o2
+            elif s2 == "none":
+                s.substyle, s.fixed, s.dynamic1 = "one_from_one", o2, o1
+            elif s1 == "volume":
+                s.substyle, s.fixed, s.dynamic1 = "two_from_one", o1, o2
+            elif s2 == "volume":
+                s.substyle, s.fixed, s.dynamic1 = "two_from_one", o2, o1
+            else:
+                s.substyle, s.dynamic1, s.dynamic2 = "one_from_two", o1, o2
         self.nsteps = 0
         self.step_count = 0
         self.nsteps_total = 0
@@ -620,6 +656,10 @@ class OracleDeform:
             s.hi_start = float(dom.boxhi[i])
             s.lo_target, s.hi_target = s.lo_start, s.hi_start
             s.cumulative_shift = 0.0
+            s.vol_start = dom.volume
+            s.saved = False
+        self.set_box.vol_start = dom.volume
+        self.set_box.cumulative_vshift = [0.0, 0.0, 0.0]
         dom.h_rate = self._strain_h_rate(dt)
         dom.vremap = self.remap == "v"
         self.chunks = virial_chunks(natoms)
@@ -647,6 +687,94 @@ class OracleDeform:
                 h[i] = (stop - length) / delt
         return h
 
+    def _adjust_linked_rates(self, e_larger, e_smaller, e3, vi, v, dt):
+        # deform_pressure.py:858-870
+        m = self.max_rate
+        e_lim_pos = (vi - v * (1 + m * dt)) / (v * (1 + m * dt) * dt)
+        e_lim_neg = (vi - v * (1 - m * dt)) / (v * (1 - m * dt) * dt)
+        if e_larger * e3 >= 0:
+            if e_larger > 0.0:
+                return e_lim_neg, -m
+            return e_lim_pos, m
+        if e_larger > 0.0:
+            return m, e_lim_pos
+        return -m, e_lim_neg
+
+    def _apply_volume(self, prd, dt):
+        # deform_pressure.py:872-956
+        linked_done, e2_linked = False, 0.0
+        for i in range(3):
+            s = self.axes[i]
+            if s.style != "volume":
+                continue
+            v0 = s.vol_start
+            if s.substyle == "one_from_one":
+                d1, fx = self.axes[s.dynamic1], self.axes[s.fixed]
+                half = 0.5 * (v0 / (d1.hi_target - d1.lo_target) / (fx.hi_start - fx.lo_start))
+            elif s.substyle == "one_from_two":
+                d1, d2 = self.axes[s.dynamic1], self.axes[s.dynamic2]
+                half = 0.5 * (v0 / (d1.hi_target - d1.lo_target) / (d2.hi_target - d2.lo_target))
+            elif not self.vol_balance_p:
+                d1, fx = self.axes[s.dynamic1], self.axes[s.fixed]
+                half = 0.5 * math.sqrt(v0 * (s.hi_start - s.lo_start) / (d1.hi_target - d1.lo_target)
+                                       / (fx.hi_start - fx.lo_start))
+            else:
+                fx, d1 = self.axes[s.fixed], self.axes[s.dynamic1]
+                l1i, l2i, l3i = float(prd[i]), float(prd[s.fixed]), float(prd[s.dynamic1])
+                l3 = d1.hi_target - d1.lo_target
+                vi = l1i * l2i * l3i
+                v = l3 * l1i * l2i
+                e3 = (l3 / l3i - 1.0) / dt
+                e1i, e2i = s.prior_rate, fx.prior_rate
+                p1, p2 = s.pressure_now, fx.pressure_now
+                p1i, p2i = s.prior_pressure, fx.prior_pressure
+                if e3 == 0.0:
+                    half = 0.5 * l1i
+                elif e1i == 0.0 or e2i == 0.0 or (p2 == p2i and p1 == p1i):
+                    half = 0.5 * math.sqrt(s.vol_start * l1i / l3 / l2i)
+                elif linked_done:
+                    half = 0.5 * l1i * (1.0 + e2_linked * dt)
+                else:
+                    denominator = p2 - p2i + e2i * ((p1 - p1i) / e1i)
+                    if denominator != 0.0:
+                        e1 = (((p2 - p2i) * (vi - v) / (v * dt)) - e2i * (p1 - p2)) / denominator
+                    else:
+                        e1 = e2i
+                    e2 = (vi - v * (1 + e1 * dt)) / (v * (1 + e1 * dt) * dt)
+                    if self.max_rate != 0.0 and (abs(e1) > self.max_rate or abs(e2) > self.max_rate):
+                        if abs(e1) > abs(e2):
+                            e1, e2 = self._adjust_linked_rates(e1, e2, e3, vi, v, dt)
+                        else:
+                            e2, e1 = self._adjust_linked_rates(e2, e1, e3, vi, v, dt)
+                    half = 0.5 * l1i * (1.0 + e1 * dt)
+                    linked_done, e2_linked = True, e2
+            mid = 0.5 * (s.lo_start + s.hi_start)
+            s.lo_target, s.hi_target = mid - half, mid + half
+
+    def _apply_box(self, tensor, dt):
+        # deform_pressure.py:958-991
+        sb = self.set_box
+        if sb.style == "volume":
+            v = 1.0
+            for i in range(3):
+                v *= self.axes[i].hi_target - self.axes[i].lo_target
+            scale = (sb.vol_start / v) ** (1.0 / 3.0)
+            for i in range(3):
+                s = self.axes[i]
+                half = 0.5 * (s.hi_target - s.lo_target) * scale
+                mid = 0.5 * (s.lo_start + s.hi_start)
+                s.lo_target, s.hi_target = mid - half, mid + half
+            return
+        v_rate = self._limit(sb.pgain * (float(np.mean(tensor[:3])) - sb.ptarget), sb.ptarget)
+        for i in range(3):
+            s = self.axes[i]
+            shift = (s.hi_target - s.lo_target) * dt * v_rate
+            sb.cumulative_vshift[i] += shift
+            if s.style == "none":
+                s.lo_target, s.hi_target = s.lo_start, s.hi_start
+            s.lo_target -= 0.5 * sb.cumulative_vshift[i]
+            s.hi_target += 0.5 * sb.cumulative_vshift[i]
+
     def _limit(self, rate, ptarget):
         # deform_pressure.py:737-752
         if self.normalize:
@@ -667,7 +795,8 @@ class OracleDeform:
         if self.step_count % self.nevery != 0:
             return np.zeros(6)
         axes = self.axes
-        needs_p = any(s.style in PRESSURE_STYLES for s in axes)
+        needs_p = (any(s.style in PRESSURE_STYLES for s in axes) or self.set_box.style == "pressure"
+                   or self.vol_balance_p)
         tensor = np.zeros(6)
         p = np.zeros(3)
         if needs_p:
@@ -689,6 +818,14 @@ class OracleDeform:
                         p[i] = tensor[i]
                     elif axes[i].style == "pressure/mean":
                         p[i] = scalar
+            # deform_pressure.py:1144-1151
+            for i in range(3):
+                s = axes[i]
+                s.pressure_now = float(tensor[i])
+                if not s.saved:
+                    s.saved = True
+                    s.prior_rate = 0.0
+                    s.prior_pressure = float(tensor[i])
         old_prd = dom.prd.copy()
         old_lo = dom.boxlo.copy()
         elapsed = self.nsteps * dt
@@ -732,6 +869,9 @@ class OracleDeform:
                 s.cumulative_shift += dt * rate * float(old_prd[i])
                 s.lo_target = s.lo_start - 0.5 * s.cumulative_shift
                 s.hi_target = s.hi_start + 0.5 * s.cumulative_shift
+        self._apply_volume(old_prd, dt)
+        if self.set_box.style != "none":
+            self._apply_box(tensor, dt)
         new_lo = np.array([axes[i].lo_target for i in range(3)])
         new_hi = np.array([axes[i].hi_target for i in range(3)])
         new_prd = new_hi - new_lo
@@ -739,6 +879,12 @@ class OracleDeform:
             raise RuntimeError(
                 f"fix deform/pressure drove a box dimension to {new_prd}, which is not positive; "
                 "check the gain, max/rate or strain rate")
+        if needs_p:
+            # deform_pressure.py:1177-1184
+            for i in range(3):
+                s = axes[i]
+                s.prior_pressure = float(tensor[i])
+                s.prior_rate = ((s.hi_target - s.lo_target) / old_prd[i] - 1.0) / dt
         h_rate = np.zeros(6)
         h_rate[:3] = (new_prd - old_prd) / dt
         if self.remap == "x" and atoms.n > 0:

@@ -14,9 +14,11 @@ waits.  A box driven non-positive is recorded in a device status word and
 raised at the next synchronisation point (a rebuild or the end of the run)
 with the reference's message.
 
-Styles the reference keeps on its host path for rarely used features --
-``volume``, ``variable``, ``box``, tilt factors, ``vol/balance/p`` -- are
-outside this path and raise NotImplementedError.
+The ``volume`` style (with ``vol/balance/p``) and the ``box`` style
+(isotropic volume or mean-pressure control of the whole box), which the
+reference keeps on its host path, run on the device too: a one-thread pass
+after the per-axis targets (csrc/tmps_servo.cuh).  ``variable`` (host-side
+expressions) and tilt factors (triclinic boxes) raise NotImplementedError.
 """
 
 from __future__ import annotations
@@ -32,7 +34,10 @@ from .. import _device, _lib
 from .base import Fix
 
 STYLE_CODE = {"none": 0, "erate": 1, "trate": 2, "vel": 3, "wiggle": 4, "final": 5, "delta": 6,
-              "scale": 7, "pressure": 8, "pressure/mean": 9}
+              "scale": 7, "pressure": 8, "pressure/mean": 9, "volume": 10}
+BOX_STYLES = ("none", "volume", "pressure")
+BOX_CODE = {"none": 0, "volume": 1, "pressure": 2}
+VSUB_CODE = {"one_from_one": 0, "one_from_two": 1, "two_from_one": 2}
 PRESSURE_STYLES = ("pressure", "pressure/mean")
 NEEDS_RUN_LENGTH = ("final", "scale", "delta")
 COUPLE_CODE = {"none": 0, "xyz": 1, "xy": 2, "yz": 3, "xz": 4}
@@ -56,6 +61,11 @@ class AxisSet:
     lo_start: float = 0.0
     hi_start: float = 0.0
     coupled: bool = False
+    # volume style links (deform_pressure.py:358-380)
+    substyle: str = ""
+    fixed: int = -1
+    dynamic1: int = -1
+    dynamic2: int = -1
 
 
 class FixDeformPressure(Fix):
@@ -72,18 +82,16 @@ class FixDeformPressure(Fix):
             raise ValueError(f"couple must be one of {tuple(COUPLE_CODE)}, got {couple!r}")
         if remap not in REMAP_CODE:
             raise ValueError("remap must be 'x', 'v' or 'none'")
-        if box is not None and box.get("style", "none") != "none":
-            raise NotImplementedError("fix deform/pressure `box` style is outside the GB300 path")
-        if vol_balance_p:
-            raise NotImplementedError("vol/balance/p is outside the GB300 path")
         self.couple = couple
         self.remap = remap
         self.flip = bool(flip)
         self.max_rate = float(max_rate)
         self.normalize_pressure = bool(normalize_pressure)
+        self.vol_balance_p = bool(vol_balance_p)
         self.var_eval = var_eval
         self.sets = [AxisSet() for _ in range(3)]
-        if axes is None:
+        self.set_box = AxisSet()
+        if axes is None and box is None:
             # legacy isotropic form (deform_pressure.py:190-199)
             target = 50000.0 if p_target is None else float(p_target)
             gain = 1e-4 if p_gain is None else float(p_gain)
@@ -92,7 +100,7 @@ class FixDeformPressure(Fix):
             if couple == "none":
                 self.couple = "xyz"
         else:
-            self._configure(axes)
+            self._configure(axes or {}, box)
         self._validate()
         self.dev = _device.device()
         self._dservo = _device.struct_buffer(_lib.Servo())
@@ -105,10 +113,11 @@ class FixDeformPressure(Fix):
         self._started = False
         self.on_device = True
         self.device_reason = ""
+        self._vol_start = 0.0
         # optional per-step record of the pressure tensor in pinned host memory (record_pressure)
         self.pressure_log: torch.Tensor | None = None
 
-    def _configure(self, axes: dict) -> None:
+    def _configure(self, axes: dict, box: dict | None = None) -> None:
         for name, spec in axes.items():
             if name in ("yz", "xz", "xy"):
                 if spec.get("style", "none") != "none":
@@ -120,8 +129,9 @@ class FixDeformPressure(Fix):
             if style == "erate/rescale":
                 raise ValueError("fix deform erate/rescale exists for NEMD with fix nvt/sllod, "
                                  "which taichimps does not have")
-            if style in ("volume", "variable"):
-                raise NotImplementedError(f"fix deform/pressure style {style!r} is outside the GB300 path")
+            if style == "variable":
+                raise NotImplementedError("fix deform/pressure style 'variable' (host-side expressions) is "
+                                          "outside the GB300 path")
             if style not in STYLE_CODE:
                 raise ValueError(f"Unsupported fix deform/pressure style {style!r} for {name}")
             s = self.sets["xyz".index(name)]
@@ -132,6 +142,14 @@ class FixDeformPressure(Fix):
                 if not hasattr(s, key):
                     raise ValueError(f"Unknown parameter {key!r} for dimension {name}")
                 setattr(s, key, float(value))
+        if box is not None:
+            style = box["style"]
+            if style not in BOX_STYLES:
+                raise ValueError(f"Unsupported fix deform/pressure box style {style!r}; implemented: {BOX_STYLES}")
+            self.set_box.style = style
+            for key, value in box.items():
+                if key != "style":
+                    setattr(self.set_box, key, float(value))
 
     def _validate(self) -> None:
         """deform_pressure.py:284-356, for the x/y/z entries."""
@@ -140,7 +158,7 @@ class FixDeformPressure(Fix):
                 raise ValueError(f"fix deform/pressure gain for {'xyz'[i]} must be positive")
             if s.style == "wiggle" and s.tperiod <= 0.0:
                 raise ValueError(f"fix deform/pressure wiggle for {'xyz'[i]} needs a period")
-        has_p = any(s.style in PRESSURE_STYLES for s in self.sets)
+        has_p = any(s.style in PRESSURE_STYLES for s in self.sets) or self.set_box.style == "pressure"
         if self.normalize_pressure and not has_p:
             raise ValueError("normalize/pressure only applies to pressure-controlled dimensions")
         if self.max_rate < 0.0:
@@ -162,6 +180,44 @@ class FixDeformPressure(Fix):
                     raise ValueError("cannot couple non-pressure-controlled dimensions")
                 elif s.pgain != self.sets[ref].pgain or s.ptarget != self.sets[ref].ptarget:
                     raise ValueError("coupled dimensions must have identical target and gain")
+        # deform_pressure.py:316-330
+        volume_dims = [i for i in range(3) if self.sets[i].style == "volume"]
+        if volume_dims and any(s.style == "pressure/mean" for s in self.sets):
+            raise ValueError("cannot ask fix deform/pressure for constant volume and a mean pressure at the same time")
+        if self.set_box.style != "none":
+            bad = ("final", "delta", "scale", "pressure/mean", "variable", "volume")
+            for i in range(3):
+                if self.sets[i].style in bad:
+                    raise ValueError("fix deform/pressure box may only be combined with x/y/z styles vel, erate, "
+                                     f"trate, wiggle and pressure, not {self.sets[i].style!r}")
+            if self.set_box.style == "pressure" and self.set_box.pgain <= 0.0:
+                raise ValueError("fix deform/pressure gain for box must be positive")
+        if self.vol_balance_p and not volume_dims:
+            raise ValueError("vol/balance/p only applies with the volume style")
+        self._setup_volume_links()
+
+    def _setup_volume_links(self) -> None:
+        """Which dimensions a `volume` axis derives its size from (deform_pressure.py:358-385)."""
+        for i in range(3):
+            s = self.sets[i]
+            if s.style != "volume":
+                continue
+            o1, o2 = (i + 1) % 3, (i + 2) % 3
+            s1, s2 = self.sets[o1].style, self.sets[o2].style
+            if s1 in ("none", "volume") and s2 in ("none", "volume"):
+                raise ValueError("the volume style needs at least one other deformed dimension")
+            if s1 == "none":
+                s.substyle, s.fixed, s.dynamic1 = "one_from_one", o1, o2
+            elif s2 == "none":
+                s.substyle, s.fixed, s.dynamic1 = "one_from_one", o2, o1
+            elif s1 == "volume":
+                s.substyle, s.fixed, s.dynamic1 = "two_from_one", o1, o2
+            elif s2 == "volume":
+                s.substyle, s.fixed, s.dynamic1 = "two_from_one", o2, o1
+            else:
+                s.substyle, s.dynamic1, s.dynamic2 = "one_from_two", o1, o2
+            if self.vol_balance_p and s.substyle != "two_from_one":
+                raise ValueError("vol/balance/p needs two dimensions holding the volume constant")
 
     def note_atom_count(self, nlocal: int) -> None:
         self._nlocal_hint = int(nlocal)
@@ -203,6 +259,15 @@ class FixDeformPressure(Fix):
         sv.remap = REMAP_CODE[self.remap]
         sv.max_rate = self.max_rate
         sv.nsteps, sv.nsteps_total, sv.step_count, sv.nevery = self.nsteps, self.nsteps_total, self.step_count, self.nevery
+        for i, s in enumerate(self.sets):
+            sv.vsub[i] = VSUB_CODE.get(s.substyle, 0)
+            sv.vfixed[i], sv.vdyn1[i], sv.vdyn2[i] = max(s.fixed, 0), max(s.dynamic1, 0), max(s.dynamic2, 0)
+        sv.vol_balance_p = 1 if self.vol_balance_p else 0
+        sv.box_style = BOX_CODE[self.set_box.style]
+        sv.box_ptarget, sv.box_pgain = self.set_box.ptarget, self.set_box.pgain
+        sv.vol_start = self._vol_start
+        sv.post = 1 if (sv.box_style != 0 or any(s.style == "volume" for s in self.sets)) else 0
+        sv.saved = 0
         return sv
 
     def setup(self, nsteps_total: int = 0, dt: float = 0.0) -> None:
@@ -212,6 +277,7 @@ class FixDeformPressure(Fix):
         self.nsteps = 0
         self.nsteps_total = int(nsteps_total)
         self._started = True
+        self._vol_start = float(dom.volume)
         for i, s in enumerate(self.sets):
             s.lo_start = float(dom.boxlo[i])
             s.hi_start = float(dom.boxhi[i])

@@ -76,7 +76,12 @@ class Servo(ctypes.Structure):
         ("lo_start", c_f64 * 3), ("hi_start", c_f64 * 3), ("cum", c_f64 * 3),
         ("pressure", c_f64 * 6),
         ("nsteps", ctypes.c_int64), ("nsteps_total", ctypes.c_int64), ("step_count", ctypes.c_int64),
-        ("nevery", c_i32), ("pad_", c_i32),
+        ("nevery", c_i32), ("post", c_i32),
+        ("vsub", c_i32 * 3), ("vfixed", c_i32 * 3), ("vdyn1", c_i32 * 3), ("vdyn2", c_i32 * 3),
+        ("vol_balance_p", c_i32), ("box_style", c_i32),
+        ("vol_start", c_f64), ("box_ptarget", c_f64), ("box_pgain", c_f64), ("box_vshift", c_f64 * 3),
+        ("prior_rate", c_f64 * 3), ("prior_pressure", c_f64 * 3),
+        ("saved", c_i32), ("pad2_", c_i32),
     ]
 
 

@@ -21,6 +21,7 @@
 //          accumulation; FP64 kept for the velocity and position updates, the
 //          per-contact shear history and the virial reduction.
 #include "tmps_contact.cuh"
+#include "tmps_servo.cuh"
 
 using namespace tmps;
 
@@ -1145,12 +1146,23 @@ __device__ void servo_chain_warp(const tmps_box& b, tmps_servo& sv, const tmps_e
             nlo = ls - 0.5 * sv.cum[d];
             nhi = hs + 0.5 * sv.cum[d];
         }
-        nprd = nhi - nlo;
         o.lo[d] = nlo;
         o.hi[d] = nhi;
-        o.prd[d] = nprd;
         o.olo[d] = lo;
         o.oprd[d] = prd;
+    }
+    if (sv.post) {
+        // volume and box styles: one lane over the three axes' targets
+        __syncwarp();
+        if (lane == 0) {
+            const double tt[6] = {t0, t1, t2, 0.0, 0.0, 0.0};
+            servo_post(sv, o.oprd, tt, dt, o.lo, o.hi);
+        }
+        __syncwarp();
+    }
+    if (lane < 3) {
+        nprd = o.hi[d] - o.lo[d];
+        o.prd[d] = nprd;
     }
     const bool bad = __any_sync(0xffffffffu, !(nprd > 0.0));
     if (lane == 0) o.bad = bad ? 1 : 0;

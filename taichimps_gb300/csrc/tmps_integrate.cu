@@ -8,6 +8,7 @@
 #include <cstdio>
 
 #include "tmps_common.cuh"
+#include "tmps_servo.cuh"
 
 using namespace tmps;
 
@@ -258,6 +259,8 @@ __global__ void k_servo(tmps_box* b, tmps_servo* s, const double* vir, double el
             nhi[d] = hs + 0.5 * s->cum[d];
         }
     }
+    // volume and box styles (cross-axis, after the per-axis targets)
+    if (s->post) servo_post(*s, prd, t, dt, nlo, nhi);
     double nprd[3];
     bool bad = false;
     for (int d = 0; d < 3; ++d) {

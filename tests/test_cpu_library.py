@@ -113,8 +113,21 @@ def test_deform_validation_cpu():
         FixDeformPressure(None, axes={"x": {"style": "pressure", "ptarget": 1.0, "pgain": 0.0}})
     with pytest.raises(ValueError, match="couple"):
         FixDeformPressure(None, axes={"x": {"style": "erate", "rate": 0.1}}, couple="xy")
-    with pytest.raises(NotImplementedError):
+    # the reference's validation of the volume and box styles (deform_pressure.py:316-385)
+    with pytest.raises(ValueError, match="at least one other deformed dimension"):
         FixDeformPressure(None, axes={"x": {"style": "volume"}})
+    with pytest.raises(ValueError, match="vol/balance/p only applies"):
+        FixDeformPressure(None, axes={"x": {"style": "erate", "rate": 0.1}}, vol_balance_p=True)
+    with pytest.raises(ValueError, match="two dimensions holding the volume"):
+        FixDeformPressure(None, axes={"x": {"style": "volume"}, "z": {"style": "erate", "rate": 0.1}},
+                          vol_balance_p=True)
+    with pytest.raises(ValueError, match="box may only be combined"):
+        FixDeformPressure(None, axes={"x": {"style": "final", "flo": 0.0, "fhi": 1.0}}, box={"style": "volume"})
+    with pytest.raises(ValueError, match="constant volume and a mean"):
+        FixDeformPressure(None, axes={"x": {"style": "volume"}, "z": {"style": "pressure/mean", "ptarget": 1.0,
+                                                                      "pgain": 1e-3}})
+    with pytest.raises(NotImplementedError):
+        FixDeformPressure(None, axes={"x": {"style": "variable"}})
     with pytest.raises(NotImplementedError):
         FixDeformPressure(None, axes={"xy": {"style": "erate", "rate": 0.1}})
     with pytest.raises(ValueError, match="nvt/sllod"):
