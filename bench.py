@@ -355,7 +355,7 @@ def ensemble_instance(G, seed, k, precision):
     dom = G.Domain(boxlo=[0.0] * 3, boxhi=[float(v) for v in pk["L"]], boundary=("p", "p", "p"))
     atom = G.AtomSystem(max_atoms=n)
     atom.add_particles(x=pk["x"], radius=pk["radius"], density=2.5, v=pk["v"])
-    nl = G.NeighborList(domain=dom, skin=SKIN, max_atoms=n, max_neighbors_per_atom=16)
+    nl = G.NeighborList(domain=dom, skin=SKIN, max_atoms=n, max_neighbors_per_atom=16, slots="auto")
     hist = G.ContactHistory(max_atoms=n, max_neighbors=16)
     pair = G.GranHertzHistory(domain=dom, kn=kn, kt=kn * 2.0 / 7.0, gamman=50.0, gammat=25.0, xmu=xmu, dampflag=1)
     sim = G.Simulation(domain=dom, atom=atom, neighbor=nl, history=hist, pair=pair, dt=DT, precision=precision)

@@ -99,9 +99,15 @@ class ContactHistory:
             self.setup_pending = False
             return
         carried = (self._saved_build is not None and nlist.build_count == self._saved_build + 1
-                   and self._shape == (nlist._n, nlist.slots))
+                   and self._shape == (nlist._n, nlist.prev_slots))
         if carried:
             L = _device.lib()
+            if nlist.slots != nlist.prev_slots:
+                # the list changed its slot count (slots="auto"): new-sized targets for the carry
+                n = nlist._n
+                self._shear_alt = torch.zeros((3, nlist.slots, n), dtype=torch.float64, device=self.dev)
+                if self.rolling is not None:
+                    self._rolling_alt = torch.zeros_like(self._shear_alt)
             old = nlist.cstruct(self.touch, self.shear, prev=True, rolling=self.rolling)
             new = nlist.cstruct(self._touch_alt, self._shear_alt, rolling=self._rolling_alt)
             _lib.check(L.tmps_history_remap(old, new, nlist.order.data_ptr(), _device.stream()),
@@ -110,6 +116,11 @@ class ContactHistory:
             self.shear, self._shear_alt = self._shear_alt, self.shear
             if self.rolling is not None:
                 self.rolling, self._rolling_alt = self._rolling_alt, self.rolling
+            if nlist.slots != nlist.prev_slots:
+                self._shear_alt = torch.zeros_like(self.shear)
+                if self.rolling is not None:
+                    self._rolling_alt = torch.zeros_like(self.shear)
+                self._shape = (nlist._n, nlist.slots)
             self._synced_build = nlist.build_count
         else:
             self._alloc(nlist._n, nlist.slots)

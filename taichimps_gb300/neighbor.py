@@ -14,6 +14,7 @@ the reference, ``num_neighbors`` / ``neighbors`` / ``npairs`` / ``pair_i`` /
 
 from __future__ import annotations
 
+import math
 from functools import lru_cache
 from typing import Any
 
@@ -96,7 +97,7 @@ def setup_grid_dims(prd, periodicity, max_cutoff: float, skin: float, max_cells:
 class NeighborList:
     def __init__(self, domain, skin: float = 0.001, max_atoms: int = 100000,
                  max_neighbors_per_atom: int = 64, max_neighbors: int | None = None,
-                 float_type: Any = None, slots: int | None = None) -> None:
+                 float_type: Any = None, slots: int | str | None = None) -> None:
         self.domain = domain
         self.skin = float(skin)
         self.max_atoms = int(max_atoms)
@@ -104,9 +105,17 @@ class NeighborList:
         self.float_type = float_type
         # Full-list slots per atom.  A full row holds both halves of the
         # reference's half list, so twice its cap, at most one 64-bit touch mask.
-        self.slots = int(slots) if slots is not None else min(MAX_SLOTS, 2 * self.max_neighbors_per_atom)
+        # slots="auto": sized from the longest row of each build (shrunk to
+        # 1.25x it plus a margin, grown and rebuilt when a row overflows)
+        # instead of a fixed cap; the history follows every change.
+        self.auto_slots = slots == "auto"
+        if self.auto_slots:
+            self.slots = MAX_SLOTS
+        else:
+            self.slots = int(slots) if slots is not None else min(MAX_SLOTS, 2 * self.max_neighbors_per_atom)
         if not 1 <= self.slots <= MAX_SLOTS:
             raise ValueError(f"slots must be in [1, {MAX_SLOTS}]")
+        self.prev_slots = self.slots
         self.max_grid_cells = 200000
         self.delay, self.every, self.check = 0, 1, True
         self.last_build_step = -1
@@ -144,6 +153,13 @@ class NeighborList:
 
     # ---------------------------------------------------------- storage
 
+    @staticmethod
+    def fit_slots(longest: int) -> int:
+        """Slots for a build whose longest row has `longest` entries: 1.25x plus a margin of 4, a
+        multiple of 4, within [8, 64]."""
+        want = int(math.ceil(1.25 * longest)) + 4
+        return max(8, min(MAX_SLOTS, (want + 3) // 4 * 4))
+
     def _alloc(self, n: int) -> None:
         if n == self._n:
             return
@@ -161,7 +177,7 @@ class NeighborList:
                 rolling: torch.Tensor | None = None) -> _lib.NList:
         s = _lib.NList()
         s.n = self._n
-        s.slots = self.slots
+        s.slots = self.prev_slots if prev else self.slots
         s.nbr = (self.prev_nbr if prev else self.nbr).data_ptr()
         s.nnb = (self.prev_nnb if prev else self.nnb).data_ptr()
         s.touch = touch.data_ptr() if touch is not None else None
@@ -191,18 +207,31 @@ class NeighborList:
         # the list built last time becomes `prev`, for the history carry-over
         self.nbr, self.prev_nbr = self.prev_nbr, self.nbr
         self.nnb, self.prev_nnb = self.prev_nnb, self.nnb
-        self.status.zero_()
-        nl = self.cstruct(None, None)
-        src, dst = atom.cstruct(atom.buffers), atom.cstruct(atom.alt_buffers)
-        rc = L.tmps_nlist_build(src, dst, self.domain.dbox, ncell, self.skin, self._rank_t.data_ptr(),
-                                self.order.data_ptr(), self.cell_of.data_ptr(), nl, self._ws.data_ptr(),
-                                wsb, self.status.data_ptr(), _device.stream())
-        _lib.check(rc, "tmps_nlist_build")
+        self.prev_slots = self.slots
+        while True:
+            if self.nbr.shape[0] < self.slots:
+                self.nbr = torch.zeros((self.slots, n), dtype=torch.int32, device=self.dev)
+            self.status.zero_()
+            nl = self.cstruct(None, None)
+            src, dst = atom.cstruct(atom.buffers), atom.cstruct(atom.alt_buffers)
+            rc = L.tmps_nlist_build(src, dst, self.domain.dbox, ncell, self.skin, self._rank_t.data_ptr(),
+                                    self.order.data_ptr(), self.cell_of.data_ptr(), nl, self._ws.data_ptr(),
+                                    wsb, self.status.data_ptr(), _device.stream())
+            _lib.check(rc, "tmps_nlist_build")
+            status = int(self.status.item())
+            if not (status & _lib.STATUS_NLIST_OVERFLOW and self.auto_slots and self.slots < MAX_SLOTS):
+                break
+            # a row overflowed: grow and rebuild from the same (untouched) source buffers
+            self.slots = MAX_SLOTS
         atom.swap_buffers()
         self._atom = atom
-        status = int(self.status.item())
         if status & _lib.STATUS_NONFINITE:
             raise RuntimeError("Neighbor build found a non-finite particle position")
+        if self.auto_slots and not status & _lib.STATUS_NLIST_OVERFLOW:
+            fit = self.fit_slots(int(self.nnb.max().item()))
+            if fit < self.slots:
+                self.nbr = self.nbr[:fit].clone()
+                self.slots = fit
         if status & _lib.STATUS_NLIST_OVERFLOW:
             raise RuntimeError(
                 "Neighbor list overflow: more than "
