@@ -19,6 +19,14 @@ import torch
 
 from . import _device, _lib
 
+def _sphere_mass(rad: np.ndarray, dens: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """rmass = (4/3) pi r^3 density and inertia 0.4 m r r (atom.py:110-111), numpy's pow for r^3 as
+    in the reference."""
+    vol = (4.0 / 3.0) * np.pi * (rad ** 3)
+    mass = vol * dens
+    inertia = ((0.4 * mass) * rad) * rad
+    return mass, inertia
+
 
 class _Buffers:
     """One complete set of per-atom device arrays (two exist: build permutes A -> B)."""
@@ -194,9 +202,7 @@ class AtomSystem:
         dens = np.full(n_new, float(density)) if np.isscalar(density) else np.asarray(density, dtype=np.float64)
         types = (np.full(n_new, int(atom_type), dtype=np.int32) if np.isscalar(atom_type)
                  else np.asarray(atom_type, dtype=np.int32))
-        vol = (4.0 / 3.0) * np.pi * (rad ** 3)
-        mass = vol * dens
-        inertia = ((0.4 * mass) * rad) * rad
+        mass, inertia = _sphere_mass(rad, dens)
         start = self.nlocal
         tags = (np.arange(start + 1, start + n_new + 1, dtype=np.int32) if tag is None
                 else np.asarray(tag, dtype=np.int32))
@@ -262,33 +268,41 @@ class AtomSystem:
 
     def _add_first_tensors(self, tens, radius, density, tag, atom_type) -> None:
         """add_particles into an empty system from float64 [n, 3] tensors (x; v and omega optional):
-        records assembled on the device; mass and inertia computed on the host as in add_particles."""
+        records, mass and inertia assembled on the device, in the reference's expression order
+        ((4/3 pi) r^3 density, ((0.4 m) r) r) with r^3 as r r r -- within an ulp of numpy's pow,
+        which the array path uses -- so a large system does not wait on element-wise host math."""
         dev = self.device
         xt = tens["x"]
         n = int(xt.shape[0])
         if n > self.max_atoms:
             raise ValueError(f"Exceeded max_atoms capacity: {n} > {self.max_atoms}")
-        rad = np.asarray(radius, dtype=np.float64)
-        if rad.ndim == 0:
-            rad = np.full(n, float(rad))
-        dens = np.full(n, float(density)) if np.isscalar(density) else np.asarray(density, dtype=np.float64)
+        if torch.is_tensor(radius):
+            rad_d = radius.to(dev, dtype=torch.float64, non_blocking=True).reshape(-1)
+        else:
+            rad_np = np.asarray(radius, dtype=np.float64)
+            rad_d = (torch.full((n,), float(rad_np), dtype=torch.float64, device=dev) if rad_np.ndim == 0
+                     else torch.from_numpy(np.ascontiguousarray(rad_np)).to(dev))
+        if rad_d.numel() == 1 and n != 1:
+            rad_d = rad_d.expand(n).contiguous()
         types = (np.full(n, int(atom_type), dtype=np.int32) if np.isscalar(atom_type)
                  else np.asarray(atom_type, dtype=np.int32))
-        vol = (4.0 / 3.0) * np.pi * (rad ** 3)
-        mass = vol * dens
-        inertia = ((0.4 * mass) * rad) * rad
-        tags = np.arange(1, n + 1, dtype=np.int32) if tag is None else np.asarray(tag, dtype=np.int32)
         nb = _Buffers(n, dev)
         nb.xr[:, :3] = xt.to(dev, non_blocking=True)
         if "v" in tens:
             nb.vm[:, :3] = tens["v"].to(dev, non_blocking=True)
         if "omega" in tens:
             nb.om[:, :3] = tens["omega"].to(dev, non_blocking=True)
-        up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
-        nb.xr[:, 3] = up(rad)
-        nb.vm[:, 3] = up(mass)
-        nb.om[:, 3] = up(inertia)
-        nb.tag.copy_(up(tags))
+        dens_d = (float(density) if np.isscalar(density)
+                  else torch.from_numpy(np.ascontiguousarray(np.asarray(density, dtype=np.float64))).to(dev))
+        vol = ((4.0 / 3.0) * np.pi) * ((rad_d * rad_d) * rad_d)
+        mass = vol * dens_d
+        nb.xr[:, 3] = rad_d
+        nb.vm[:, 3] = mass
+        nb.om[:, 3] = ((0.4 * mass) * rad_d) * rad_d
+        if tag is None:
+            nb.tag.copy_(torch.arange(1, n + 1, dtype=torch.int32, device=dev))
+        else:
+            nb.tag.copy_(torch.from_numpy(np.asarray(tag, dtype=np.int32)).to(dev))
         nb.uid.copy_(torch.arange(n, dtype=torch.int32, device=dev))
         self._buf = nb
         self._alt = _Buffers(n, dev)
@@ -296,7 +310,7 @@ class AtomSystem:
         self.mask_host = np.ones(n, dtype=np.int32)
         self.nlocal = n
         self._uid_cache = None
-        self.max_radius = float(rad.max()) if n else 0.0
+        self.max_radius = float(rad_d.max()) if n else 0.0
         for cb in self._listeners:
             cb()
 
