@@ -647,6 +647,9 @@ def main():
     bytes_atom = algorithmic_bytes(dom_name, head, r["n_nb"], r["n_c"], r["flagged"])
     achieved = bytes_atom * n / (kern[dom_name] * 1e-3) / 1e9 if kern.get(dom_name) else None
     traffic = ncu_traffic(dom_name, head)
+    c_bytes = algorithmic_bytes("fused_c", head, r["n_nb"], r["n_c"], r["flagged"])
+    c_achieved = c_bytes * n / (kern["fused_c"] * 1e-3) / 1e9 if kern.get("fused_c") else None
+    c_traffic = ncu_traffic("fused_c", head)
     e2e = None if args.no_e2e else run_e2e(args, p, head)
     cpu = None
     p_oracle = None
@@ -686,6 +689,14 @@ def main():
                      "traffic_source": traffic["source"] if traffic else None,
                      "algorithmic_bytes_per_launch": bytes_atom * n, "bytes_per_atom": bytes_atom,
                      "kernel_ms": kern[dom_name], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
+        # the contact kernel on its own: the nominal bytes of a contact kernel over the full rows
+        # (S + 4 n_nb + 52 n_c per atom, see algorithmic_bytes) per C launch; C's bound check skips
+        # most of them, so this says how fast the contact work is against what it would have to move
+        "contact_kernel": {"kernel": KERNEL_NAMES[("fused_c", head)], "bound": "hbm (nominal bytes)",
+                           "achieved": c_achieved, "peak": peak, "unit": "GB/s",
+                           "frac": (c_achieved / peak) if c_achieved else None,
+                           "nominal_bytes_per_atom": c_bytes, "kernel_ms": kern.get("fused_c"),
+                           "traffic": c_traffic["bytes"] if c_traffic else None},
         "speedup_mixed_vs_fp64": (values["mixed"] / values["fp64"]) if len(values) == 2 else None,
         "oracle_mean_pressure": None if p_oracle is None else scal(p_oracle),
         "pressure_compared_after_steps": r["steps_run"],
