@@ -178,6 +178,23 @@ def ncu_traffic(kernel: str, precision: str):
     return {"bytes": k["dram_bytes_read"] + k["dram_bytes_write"], "source": f"ncu: {d.get('command', '')}"}
 
 
+def max_over_ranks(ms: float, world: int, device: str = "cuda") -> float:
+    """The timed region of a replica run ends when the slowest rank's does: the maximum over ranks
+    (the only collective of the replica path), then a barrier."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def replica_seed(seed: int, rank: int) -> int:
+    """Each rank runs its own packing (independent replicas, no data-path exchange)."""
+    return seed + rank
+
+
 def run_gpu_arm(args, p, precision, rank, world):
     """W warm-up + K timed steps of one run through Simulation (the fused step), one precision."""
     import torch
@@ -220,11 +237,7 @@ def run_gpu_arm(args, p, precision, rank, world):
     timed = {k: [a.elapsed_time(b) for a, b in v] for k, v in _device.TIMED.items()}
     _device.TIMED = None
     eng.finish()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
+    ms = max_over_ranks(ms, world)
     sim.check_device_status()
     n_nb, n_c = list_stats(sim)
     sim.domain.pull()
@@ -624,7 +637,7 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
-    p = config2(seed=args.seed + rank, n=args.n)
+    p = config2(seed=replica_seed(args.seed, rank), n=args.n)
     forms = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
     runs = {}
     for prec in forms:
