@@ -1,0 +1,73 @@
+"""
+Long runs against the oracle: 2,000 steps of a dense Hertz packing under the
+isotropic pressure servo with Cundall damping (remap x; rebuilds along the
+way), on the GPU in both forms and in the oracle.  The dynamics are chaotic,
+so the comparison is of the quantities the reference reports, within stated
+tolerances:
+
+  box strain at the end                                      FP64 1e-9, mixed 1e-6 relative to the strain
+  mean pressure over the last 500 steps                      FP64 1e-8, mixed 1e-5 relative
+  coordination number at the end                             FP64 exact, mixed within 1%
+"""
+
+import numpy as np
+import pytest
+
+from _twin import dense_packing, make_twin
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 2000
+
+
+@pytest.fixture(scope="module")
+def oracle_run(oracle):
+    rng = np.random.default_rng(101)
+    x, r = dense_packing(rng, 1000, 10.0, 0.5, 0.56)
+    deform = dict(axes={d: {"style": "pressure", "ptarget": 1.0, "pgain": 1e-3} for d in "xyz"}, couple="xyz",
+                  max_rate=1e-1, remap="x")
+    _, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [10.0] * 3, pair="hertz/history", dt=5e-5,
+                        cundall=(0.7, 0.7), deform=deform)
+    osim.setup(STEPS)
+    prd, press = [], []
+    for _ in range(STEPS):
+        osim.step()
+        prd.append(osim.domain.prd.copy())
+        press.append(np.mean(osim.last_pressure[:3]))
+    cn = osim.neighbor.contact_count(osim.atoms)
+    return dict(x=x, r=r, deform=deform, prd=np.array(prd), press=np.array(press), cn=cn,
+                builds=osim.neighbor.build_count)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_long_run_matches_oracle(gpu, oracle, oracle_run, precision):
+    from taichimps_gb300 import ComputeContactAtom
+    o = oracle_run
+    sim, _ = make_twin(oracle, o["x"], o["r"], 2.5, [0.0] * 3, [10.0] * 3, pair="hertz/history", dt=5e-5,
+                       cundall=(0.7, 0.7), deform=o["deform"])
+    sim.precision = precision
+    fix = sim.fixes[-1]
+    fix.record_pressure(STEPS + 1)
+    sim.run(STEPS)
+    rows = fix.pressure_history(range(1, STEPS + 1))
+    sim.domain.pull()
+    prd = np.array(sim.domain.boxhi) - np.array(sim.domain.boxlo)
+    assert sim.neighbor.build_count > 1 and o["builds"] > 1
+    # box strain at the end
+    strain_o = o["prd"][-1] / 10.0 - 1.0
+    strain_g = prd / 10.0 - 1.0
+    assert np.abs(strain_o).max() > 1e-4
+    tol_s = 1e-9 if precision == "fp64" else 1e-6
+    assert np.abs(strain_g - strain_o).max() <= tol_s * np.abs(strain_o).max(), (strain_g, strain_o)
+    # mean pressure over the last 500 steps
+    pg = np.mean(rows[-500:, :3])
+    po = np.mean(o["press"][-500:])
+    tol_p = 1e-8 if precision == "fp64" else 1e-5
+    assert abs(pg - po) <= tol_p * abs(po), (pg, po)
+    # coordination number at the end
+    cn = ComputeContactAtom(max_atoms=len(o["x"])).compute(sim.atom, sim.domain, sim.neighbor)
+    assert cn.mean() > 1.0
+    if precision == "fp64":
+        np.testing.assert_array_equal(cn, o["cn"])
+    else:
+        assert abs(cn.mean() - o["cn"].mean()) <= 0.01 * o["cn"].mean()
