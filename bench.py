@@ -451,8 +451,9 @@ KN_EQUIV = (4.0 / 3.0) * E_MOD / (2.0 * (1.0 - POISSON ** 2))  # hertz/material'
 def triaxial_packing(n, seed):
     """The config-2 procedure at this size, at the stiffness of hertz/material E 5e6, nu 0.3."""
     from taichimps_gb300.packing import compress_packing
-    return compress_packing(n, seed=seed, kn=KN_EQUIV, max_rate=5e-4, dt=2e-4, cycles=100, cycle_steps=12000,
-                            relax_cycles=10, phi0=0.4, jitter=0.25, precision="mixed")
+    # strain capacity cycles x cycle_steps x dt x max_rate = 0.18 (0.4 -> 0.57 needs ~0.11)
+    return compress_packing(n, seed=seed, kn=KN_EQUIV, max_rate=5e-4, dt=2e-4, cycles=40, cycle_steps=45000,
+                            relax_cycles=6, phi0=0.4, jitter=0.25, precision="mixed")
 
 
 def triaxial_sim(G, pk, precision):
