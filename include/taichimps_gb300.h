@@ -371,6 +371,15 @@ int tmps_servo_step(tmps_box* d_box, tmps_servo* d_servo, const double* d_virial
 int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* d_eng,
                        const int32_t* cell_of, void* stream);
 
+/* The per-contact histories (shear, rolling) of the touching slots between
+ * their two storages: to_dw 1 turns each double into an FP32 double word
+ * (hi, lo) in the same 8 bytes -- the mixed form's contact pass reads and
+ * writes them that way -- and to_dw 0 turns them back into doubles (exact for
+ * values of at most 48 significant bits).  Call with 1 after
+ * tmps_fused_prepare of a mixed run, with 0 before the history is carried
+ * across a rebuild, saved or read, and at the end of the run. */
+int tmps_mixed_history(const tmps_nlist* nl, int32_t to_dw, void* stream);
+
 /* Back from the mixed form to absolute FP64 positions in xr, and the FP32
  * force and torque into f / torque. */
 int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream);

@@ -204,6 +204,7 @@ _SIGS = {
     "tmps_remap_x": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
     "tmps_fused_prepare": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp, c_vp]),
     "tmps_mixed_unpack": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
+    "tmps_mixed_history": (c_i32, [ctypes.POINTER(NList), c_i32, c_vp]),
     "tmps_fused_bounds": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
                                   ctypes.POINTER(PairParams), c_i32, c_vp, c_vp]),
     "tmps_fused_a": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp, c_vp]),

@@ -38,6 +38,57 @@ TMPS_DEV void cross3(const T* a, const T* b, T* o) {
     o[2] = a[0] * b[1] - a[1] * b[0];
 }
 
+// Storage of a per-contact history component.  The FP64 form keeps it in a
+// double; the mixed form keeps it as an FP32 double word (hi + lo, ~48 bits)
+// so that its contact pass, which is otherwise all FP32, issues no FP64
+// instruction for it: increments are added with an error-free two-sum,
+// values the law computes in FP32 replace it outright (as a double would get
+// the same FP32 value), and a read gives hi (hi + lo rounded to FP32).
+struct DW {
+    float hi, lo;
+};
+
+template <typename H>
+struct Hist;
+
+template <>
+struct Hist<double> {
+    template <typename T>
+    TMPS_DEV static T get(double h) { return (T)h; }
+    template <typename T>
+    TMPS_DEV static void add(double& h, T v) { h = h + (double)v; }
+    template <typename T>
+    TMPS_DEV static void set(double& h, T v) { h = (double)v; }
+    // h = ratio (h + dc) - dc, the legacy Coulomb rescale (hooke_history.py:183-187)
+    template <typename T>
+    TMPS_DEV static void rescale(double& h, T ratio, T dc) { h = (double)ratio * (h + (double)dc) - (double)dc; }
+};
+
+template <>
+struct Hist<DW> {
+    template <typename T>
+    TMPS_DEV static T get(DW h) { return (T)h.hi; }
+    template <typename T>
+    TMPS_DEV static void add(DW& h, T v) {
+        // two-sum of hi and v, the error and lo folded back (fast two-sum)
+        const float a = h.hi, b = (float)v;
+        const float s = a + b;
+        const float bb = s - a;
+        const float e = (a - (s - bb)) + (b - bb);
+        const float t = e + h.lo;
+        const float hi = s + t;
+        h.lo = t - (hi - s);
+        h.hi = hi;
+    }
+    template <typename T>
+    TMPS_DEV static void set(DW& h, T v) {
+        h.hi = (float)v;
+        h.lo = 0.0f;
+    }
+    template <typename T>
+    TMPS_DEV static void rescale(DW& h, T ratio, T dc) { set(h, (float)(ratio * (h.hi + dc) - dc)); }
+};
+
 template <typename T>
 struct PairIn {
     T d[3];      // x_a - x_b, minimum image
@@ -61,9 +112,10 @@ struct PairOut {
 // the overlap).  `sh` and `rl` (canonical sense) are read and written only by
 // history styles and by the rolling model; the caller passes zeros when the
 // slot held no live contact (the reference's partner != jtag reset).
-template <typename T, int STYLE>
+template <typename T, int STYLE, typename H = double>
 TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, const PairIn<T>& in,
-                          double* sh, double* rl, PairOut<T>& out) {
+                          H* sh, H* rl, PairOut<T>& out) {
+    using HS = Hist<H>;
     using S = StyleTraits<STYLE>;
     out.troll[0] = out.troll[1] = out.troll[2] = T(0);
     if constexpr (S::legacy) {
@@ -107,17 +159,17 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             T shf[3];
             if (shearupdate) {
 #pragma unroll
-                for (int k = 0; k < 3; ++k) sh[k] = sh[k] + (double)(vtr[k] * dt);
+                for (int k = 0; k < 3; ++k) HS::add(sh[k], vtr[k] * dt);
             }
 #pragma unroll
-            for (int k = 0; k < 3; ++k) shf[k] = (T)sh[k];
+            for (int k = 0; k < 3; ++k) shf[k] = HS::template get<T>(sh[k]);
             const T shrmag = norm3(shf);
             if (shearupdate) {
                 const T rsht = dot3(shf, in.d) * rsqinv;
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    sh[k] = sh[k] - (double)(rsht * in.d[k]);
-                    shf[k] = (T)sh[k];
+                    HS::add(sh[k], -(rsht * in.d[k]));
+                    shf[k] = HS::template get<T>(sh[k]);
                 }
             }
 #pragma unroll
@@ -134,7 +186,7 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         const T dc = (geff * vtr[k]) / T(P.kt);
-                        sh[k] = (double)ratio * (sh[k] + (double)dc) - (double)dc;
+                        HS::rescale(sh[k], ratio, dc);
                         fs[k] = ratio * fs[k];
                     }
                 } else {
@@ -209,7 +261,7 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             const T damp_t = T(P.xt) * dpf;
             T hf[3];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) hf[k] = (T)sh[k];
+            for (int k = 0; k < 3; ++k) hf[k] = HS::template get<T>(sh[k]);
             if (shearupdate) {
                 const T rsht = dot3(hf, nv);
                 if (fabs(rsht) * keff > T(1e-10) * fscrit) {
@@ -222,12 +274,12 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
                     T scale = T(0);
                     if (prjmag > T(0)) scale = shrmag / prjmag;
 #pragma unroll
-                    for (int k = 0; k < 3; ++k) sh[k] = (double)(o[k] * scale);
+                    for (int k = 0; k < 3; ++k) HS::set(sh[k], o[k] * scale);
                 }
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    sh[k] = sh[k] + (double)(vtr[k] * dt);
-                    hf[k] = (T)sh[k];
+                    HS::add(sh[k], vtr[k] * dt);
+                    hf[k] = HS::template get<T>(sh[k]);
                 }
             }
             T fdamp[3];
@@ -242,7 +294,7 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         fs[k] = fs[k] * sc;
-                        sh[k] = (double)((-(fs[k] - fdamp[k])) / keff);
+                        HS::set(sh[k], (-(fs[k] - fdamp[k])) / keff);
                     }
                 } else {
                     fs[0] = fs[1] = fs[2] = T(0);
@@ -266,9 +318,9 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             for (int k = 0; k < 3; ++k) wrel[k] = in.wa[k] - in.wb[k];
             if (shearupdate) {
 #pragma unroll
-                for (int k = 0; k < 3; ++k) rl[k] = rl[k] + (double)(wrel[k] * dt);
+                for (int k = 0; k < 3; ++k) HS::add(rl[k], wrel[k] * dt);
             }
-            T h[3] = {(T)rl[0], (T)rl[1], (T)rl[2]};
+            T h[3] = {HS::template get<T>(rl[0]), HS::template get<T>(rl[1]), HS::template get<T>(rl[2])};
             const T tr_mag = T(P.k_roll) * norm3(h);
             const T tr_max = (T(P.mu_roll) * reff) * fabs(fntot);
 #pragma unroll
@@ -277,7 +329,7 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     out.troll[k] = (-tr_max) * (h[k] / tr_mag);
-                    rl[k] = (double)((tr_max / T(P.k_roll)) * (h[k] / tr_mag));
+                    HS::set(rl[k], (tr_max / T(P.k_roll)) * (h[k] / tr_mag));
                 }
             }
         }

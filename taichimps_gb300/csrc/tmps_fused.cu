@@ -111,6 +111,11 @@ __device__ __forceinline__ void block_sum_dw(float (&h)[NV], float (&l)[NV], flo
 // complete and its writes to be visible (griddepcontrol.wait: a hardware
 // wait, no spin), and only then touches memory and lets its own successor be
 // scheduled.  Waits chain, so every earlier kernel has completed too.
+// A history component in the row atom's own sense: the two copies of a
+// contact are exact negatives (for a double word, both words negated).
+__device__ __forceinline__ double hsign(double h, bool keep) { return keep ? h : -h; }
+__device__ __forceinline__ DW hsign(DW h, bool keep) { return keep ? h : DW{-h.hi, -h.lo}; }
+
 __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -631,7 +636,9 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                     int32_t ci = 0, cj = 0;
                     float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
                     T vi[3], wi[3], mi, vj[3], wj[3], mj;
-                    double shr[3] = {0, 0, 0}, rlr[3] = {0, 0, 0};
+                    // histories: doubles in the FP64 form, FP32 double words in the mixed form
+                    using HT = typename std::conditional<MIXED, DW, double>::type;
+                    HT shr[3] = {}, rlr[3] = {};
                     if constexpr (MIXED) {
                         const float4 pi = ld4f(A.pos32, ia), pj = ld4f(A.pos32, j);
                         il = ld4f(A.pos32lo, ia);
@@ -660,13 +667,15 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                         wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
                     }
                     if (hist && was) {
-                        shr[0] = L.shear[so];
-                        shr[1] = L.shear[ss + so];
-                        shr[2] = L.shear[2 * ss + so];
+                        const HT* hs = reinterpret_cast<const HT*>(L.shear);
+                        shr[0] = hs[so];
+                        shr[1] = hs[ss + so];
+                        shr[2] = hs[2 * ss + so];
                         if (roll) {
-                            rlr[0] = L.rolling[so];
-                            rlr[1] = L.rolling[ss + so];
-                            rlr[2] = L.rolling[2 * ss + so];
+                            const HT* hr = reinterpret_cast<const HT*>(L.rolling);
+                            rlr[0] = hr[so];
+                            rlr[1] = hr[ss + so];
+                            rlr[2] = hr[2 * ss + so];
                         }
                     }
                     // separation x_i - x_j
@@ -801,27 +810,26 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                             in.wa[c] = lo ? wi[c] : wj[c];
                             in.wb[c] = lo ? wj[c] : wi[c];
                         }
-                        double sh[3] = {0, 0, 0}, rl[3] = {0, 0, 0};
+                        HT sh[3] = {}, rl[3] = {};
                         if (hist && was) {
-                            const double sgd = lo ? 1.0 : -1.0;
-                            sh[0] = sgd * shr[0];
-                            sh[1] = sgd * shr[1];
-                            sh[2] = sgd * shr[2];
-                            rl[0] = sgd * rlr[0];
-                            rl[1] = sgd * rlr[1];
-                            rl[2] = sgd * rlr[2];
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) {
+                                sh[c] = hsign(shr[c], lo);
+                                rl[c] = hsign(rlr[c], lo);
+                            }
                         }
                         PairOut<T> out;
                         contact_law<T, STYLE>(P, dt, 1, in, sh, rl, out);
                         if (hist) {
-                            const double sgd = lo ? 1.0 : -1.0;
-                            L.shear[so] = sgd * sh[0];
-                            L.shear[ss + so] = sgd * sh[1];
-                            L.shear[2 * ss + so] = sgd * sh[2];
+                            HT* hs = reinterpret_cast<HT*>(L.shear);
+                            hs[so] = hsign(sh[0], lo);
+                            hs[ss + so] = hsign(sh[1], lo);
+                            hs[2 * ss + so] = hsign(sh[2], lo);
                             if (roll) {
-                                L.rolling[so] = sgd * rl[0];
-                                L.rolling[ss + so] = sgd * rl[1];
-                                L.rolling[2 * ss + so] = sgd * rl[2];
+                                HT* hr = reinterpret_cast<HT*>(L.rolling);
+                                hr[so] = hsign(rl[0], lo);
+                                hr[ss + so] = hsign(rl[1], lo);
+                                hr[2 * ss + so] = hsign(rl[2], lo);
                             }
                         }
                         const T arm = lo ? out.arm_a : out.arm_b;
@@ -1642,9 +1650,52 @@ int contact_blocks(int n, int style, bool mixed) {
 size_t gap_offset(int n) { return lay_gap(n); }
 size_t atom_gap_offset(int n) { return lay_agap(n); }
 size_t part_offset(int n) { return lay_part(n); }
+// The mixed form's histories between their two storages: doubles (the FP64
+// form, the per-hook kernels, the rebuild carry-over, restart) and FP32
+// double words (the mixed contact pass).  Only the entries of touching slots
+// hold a history; to_dw 1: double -> (hi, lo), 0: (hi, lo) -> double, exact
+// both ways for values of at most 48 significant bits.
+__global__ void __launch_bounds__(256) k_history_form(tmps_nlist L, int to_dw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = L.n;
+    if (i >= n) return;
+    const uint64_t t = L.touch[i];
+    if (!t) return;
+    const size_t ss = (size_t)L.slots * n;
+    for (uint64_t w = t; w; w &= w - 1) {
+        const int k = __ffsll((long long)w) - 1;
+        if (k >= L.slots) break;
+        for (int arr = 0; arr < 2; ++arr) {
+            double* h = arr == 0 ? L.shear : L.rolling;
+            if (!h) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                double* p = h + (size_t)c * ss + (size_t)k * n + i;
+                if (to_dw) {
+                    const double v = *p;
+                    const float hi = __double2float_rn(v);
+                    const float lo = __double2float_rn(v - (double)hi);
+                    *reinterpret_cast<DW*>(p) = DW{hi, lo};
+                } else {
+                    const DW v = *reinterpret_cast<const DW*>(p);
+                    *p = (double)v.hi + (double)v.lo;
+                }
+            }
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int tmps_mixed_history(const tmps_nlist* nl, int32_t to_dw, void* stream) {
+    if (!nl || nl->n < 0 || nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
+    if (nl->n == 0 || !nl->touch || !nl->shear) return TMPS_OK;
+    k_history_form<<<grid_for(nl->n, 256), 256, 0, (cudaStream_t)stream>>>(*nl, to_dw ? 1 : 0);
+    note_launches(1);
+    return cudaPeekAtLastError() == cudaSuccess ? TMPS_OK : TMPS_ERR_CUDA;
+}
 
 int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed) {
     return a_blocks(n, mixed != 0) + contact_blocks(n, style, mixed != 0);

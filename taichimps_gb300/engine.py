@@ -74,6 +74,7 @@ class FusedEngine:
         self.cull = bool(cull)
         self._graph = None
         self._graph_key = None
+        self._hist_dw = False
         self.graph_replays = 0
         self.graph_kernel_launches = 0
 
@@ -175,6 +176,17 @@ class FusedEngine:
         rc = L.tmps_fused_bounds(atoms, sim.history.cstruct(nl), sim.domain.dbox, self._eng.data_ptr(),
                                  sim.pair_style.params, 1 if self.cull else 0, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_bounds")
+        self._history_form(True)
+
+    def _history_form(self, dw: bool) -> None:
+        """The mixed form keeps the contact histories as FP32 double words while it runs, and
+        hands them back as doubles (before a rebuild carries them over, and at the end)."""
+        if not self.mixed or self._hist_dw == dw:
+            return
+        sim = self.sim
+        rc = _device.lib().tmps_mixed_history(sim.history.cstruct(sim.neighbor), 1 if dw else 0, _device.stream())
+        _lib.check(rc, "tmps_mixed_history")
+        self._hist_dw = dw
 
     def _launch_step(self, L, st, atoms, nl_struct, params) -> None:
         dbox, eng = self.sim.domain.dbox, self._eng.data_ptr()
@@ -295,6 +307,7 @@ class FusedEngine:
         nl.current_step = s
         if self.mixed:
             _lib.check(L.tmps_mixed_unpack(self.atoms(), sim.domain.dbox, st), "tmps_mixed_unpack")
+        self._history_form(False)
         sim.domain.mark_device_authoritative()
         sim.domain.pull()
         sim.history.save_state(atom, nl)
@@ -326,6 +339,7 @@ class FusedEngine:
         _lib.check(L.tmps_fused_settle(atoms, sim.domain.dbox, self._eng.data_ptr(), st), "tmps_fused_settle")
         if self.mixed:
             _lib.check(L.tmps_mixed_unpack(atoms, sim.domain.dbox, st), "tmps_mixed_unpack")
+        self._history_form(False)
         sim.domain.mark_device_authoritative()
         e = self._engine_state()
         sim.timestep = int(e.step)
