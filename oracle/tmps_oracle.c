@@ -202,7 +202,7 @@ void or_build_grid(const or_box_t* b, const int32_t g[3], const double cs[3], in
         cell_start[ci + 1] += 1;
     }
     for (int c = 0; c < ncell; ++c) cell_start[c + 1] += cell_start[c];
-    int32_t* fill = (int32_t*)calloc((size_t)ncell + 1, sizeof(int32_t));
+    int32_t* fill = (int32_t*)calloc((size_t)(ncell > 0 ? ncell : 0) + 1, sizeof(int32_t));
     for (int i = 0; i < n; ++i) {
         int c = cell_of[i];
         cell_particles[cell_start[c] + fill[c]++] = i;
