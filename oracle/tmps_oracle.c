@@ -41,7 +41,7 @@ typedef struct {
 } or_box_t;
 
 typedef struct {
-    /* legacy gran/* styles (hooke.py:29-50, hooke_history.py:86-106) */
+    /* legacy gran styles (hooke.py:29-50, hooke_history.py:86-106) */
     double kn, kt, gamman, gammat, xmu;
     int32_t limit_damping;
     /* pair granular (granular.py:122-205): model ids and derived coefficients */
