@@ -400,6 +400,7 @@ def run_ensemble(args):
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     launches_batch = 3 * eng.chunk * (eng.graph_replays - r0)
+    shape = {"groups_per_warp_a_c": list(eng.launch_shape), "tuning_us_per_launch": eng.tuning}
     del eng, batch
     torch.cuda.empty_cache()
     looped = [ensemble_instance(G, args.seed, k, prec) for k in range(m)]
@@ -426,7 +427,7 @@ def run_ensemble(args):
                                      "how": "Simulation.run of each instance in turn (its own fused step, CUDA "
                                             "graphs), same steps"},
             "speedup_vs_looped": t_loop / t_batch, "batched_seconds": t_batch,
-            "gpu_launches_batched": launches_batch}
+            "gpu_launches_batched": launches_batch, "launch_shape": shape}
 
 
 # ----------------------------------------------------------------- main

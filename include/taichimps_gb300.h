@@ -192,7 +192,7 @@ typedef struct tmps_engine {
     int32_t servo;           /* a deform/pressure fix is present */
     int32_t mixed;           /* 1: split FP64 positions + FP32 contact arithmetic */
     int32_t single_bin[3];   /* periodic dimension with one bin (FP32 image in C) */
-    int32_t nblocks;         /* C's grid size, = number of virial partials */
+    int32_t nblocks;         /* virial partials: blocks of A + blocks of C */
     double dt, gamma_lin, gamma_ang, trigger_sq;
     double lo0[3], h0[3];    /* box origin and bin size at the last build (mixed) */
     float dlo32[4], dh32[4]; /* lo - lo0, h - h0 (mixed skin check) */
@@ -225,8 +225,9 @@ typedef struct tmps_engine {
  * independent system -- its own atoms, list, pair coefficients, box, servo,
  * fused-step engine and scratch, exactly what the single-instance calls take --
  * and the range of blocks it owns in each batched grid.  Its grids are the
- * ones a single-instance launch would use (tmps_batch_blocks), so a batched
- * step and a single-instance step of the same instance are interchangeable. */
+ * ones a single-instance launch of the same launch shape uses
+ * (tmps_fused_shape), so a batched step and a single-instance step of the
+ * same instance and shape are interchangeable. */
 typedef struct tmps_instance {
     tmps_atoms a;
     tmps_nlist nl;
@@ -396,25 +397,40 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
 /* Launch A (see tmps_engine).  `scratch` is C's: A reads the flag words of
  * the last C (an unflagged atom's force and torque are exact zeros and are
  * not loaded) and writes the first virial partials, the kinetic term
- * sum m v v of every atom at mid-step velocity. */
-int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* scratch, void* stream);
+ * sum m v v of every atom at mid-step velocity.  a_blocks: A's grid from
+ * tmps_fused_shape, or <= 0 for the default. */
+int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32_t a_blocks, void* scratch,
+                 void* stream);
 
 /* Launch C: per 32-atom group a bound check (tmps_fused_bounds), a screen of
  * the atoms the bounds leave (finishes contact-free ones, flags the rest) and
  * the contact law over the flagged ones.  `scratch` (tmps_fused_scratch_bytes(n),
  * caller memory: flag words, per-group and per-atom gaps, then the
- * d_eng->nblocks = tmps_fused_blocks(n) virial partial sums). */
+ * d_eng->nblocks virial partial sums, A's blocks then C's).  c_blocks: C's
+ * grid from tmps_fused_shape, or <= 0 for the default; d_eng->nblocks must be
+ * A's blocks + C's blocks of the same shape. */
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
-                 const tmps_pair_params* p, void* scratch, void* stream);
+                 const tmps_pair_params* p, int32_t c_blocks, void* scratch, void* stream);
 
 /* Launch S: rebuild decision, virial total (from C's scratch), servo. */
 int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const void* scratch,
                      int32_t* d_status, void* stream);
 
 /* Number of virial partial sums A and C write for n atoms with this pair
- * style (tmps_pair_params.style) in this form (mixed 0/1): one per block of
- * one resident wave of A and of C. */
+ * style (tmps_pair_params.style) in this form (mixed 0/1) under the default
+ * launch shape: one per block of A and of C, at most one resident wave each. */
 int32_t tmps_fused_blocks(int32_t n, int32_t style, int32_t mixed);
+
+/* Launch shape: the grids of A and C for n atoms when each warp takes
+ * a_groups_per_warp (A) or c_groups_per_warp (C) 32-atom groups: one block of
+ * A per 256 x a_groups_per_warp atoms, one block of C per 128 x
+ * c_groups_per_warp atoms, never more than the default grid (<= 0: the
+ * default, the grids tmps_fused_blocks counts).  No reference counterpart
+ * (launch geometry).  The virial is summed per block, so the shape fixes the
+ * summation order: results depend on it at rounding level only, and two runs
+ * with the same shape are bit-identical. */
+int tmps_fused_shape(int32_t n, int32_t style, int32_t mixed, int32_t a_groups_per_warp, int32_t c_groups_per_warp,
+                     int32_t* a_blocks, int32_t* c_blocks);
 
 /* Scratch bytes tmps_fused_c / tmps_fused_servo need (same arguments). */
 int64_t tmps_fused_scratch_bytes(int32_t n, int32_t style, int32_t mixed);
@@ -437,7 +453,9 @@ int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void
  * instance.  All instances share the arithmetic form (mixed) and the pair
  * style. */
 
-/* Blocks one instance of n atoms owns in the A and C grids. */
+/* Blocks one instance of n atoms owns in the A and C grids under the default
+ * launch shape (tmps_fused_shape with both counts 0).  An instance may
+ * own any grid tmps_fused_shape gives; its engine's nblocks must match. */
 int tmps_batch_blocks(int32_t n, int32_t style, int32_t mixed, int32_t* a_blocks, int32_t* c_blocks);
 
 int tmps_batch_a(const tmps_instance* d_inst, const int32_t* d_block_inst, int32_t nblocks, int32_t mixed,

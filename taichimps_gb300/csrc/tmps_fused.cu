@@ -461,6 +461,7 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
     const int64_t s = E->step + 1;
     if (rebuild_due(E, s)) return;  // S marks the step aborted; the host rebuilds
     const int nb = E->nblocks;      // partials are component-major, [6][nb]
+    part += nb - nblk;              // C's blocks follow A's
     constexpr bool kHist = STYLE == STYLE_HOOKE_HISTORY || STYLE == STYLE_HERTZ_HISTORY || STYLE == STYLE_GRANULAR;
     const bool hist = kHist && (STYLE != STYLE_GRANULAR || P.tangential_id >= 2 || P.rolling_id != 0);
     const bool roll = STYLE == STYLE_GRANULAR && P.rolling_id != 0;
@@ -1295,19 +1296,25 @@ __device__ __forceinline__ void s_body(tmps_box* b, tmps_servo* sv, tmps_engine*
     const bool servo_now = se.servo && ((ssv.step_count + 1) % ssv.nevery == 0);
     if (servo_now) {
         const double* part = reinterpret_cast<const double*>(scratch + se.part_off);
-        const int nb = se.nblocks, c = warp >> 2, q = warp & 3;
+        const int nb = se.nblocks;
+        // kWarpsS virtual warps, four per component; a block of fewer warps
+        // runs several in turn, with the same arithmetic each
         if (se.mixed) {
-            const float2* row = reinterpret_cast<const float2*>(part) + (size_t)c * nb;
-            float2 acc = sum_component(row, nb, q, lane, make_float2(0.0f, 0.0f), [](float2 x, float2 y) {
-                dw_add2(x.x, x.y, y.x, y.y);
-                return x;
-            });
+            for (int vw = warp; vw < kWarpsS; vw += (int)(blockDim.x >> 5)) {
+                const int c = vw >> 2, q = vw & 3;
+                const float2* row = reinterpret_cast<const float2*>(part) + (size_t)c * nb;
+                float2 acc = sum_component(row, nb, q, lane, make_float2(0.0f, 0.0f), [](float2 x, float2 y) {
+                    dw_add2(x.x, x.y, y.x, y.y);
+                    return x;
+                });
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float bh = __shfl_down_sync(0xffffffffu, acc.x, o), bl = __shfl_down_sync(0xffffffffu, acc.y, o);
-                dw_add2(acc.x, acc.y, bh, bl);
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float bh = __shfl_down_sync(0xffffffffu, acc.x, o),
+                                bl = __shfl_down_sync(0xffffffffu, acc.y, o);
+                    dw_add2(acc.x, acc.y, bh, bl);
+                }
+                if (lane == 0) wsumf[vw] = acc;
             }
-            if (lane == 0) wsumf[warp] = acc;
             __syncthreads();
             if (threadIdx.x < 6) {
                 float h = 0.0f, l = 0.0f;
@@ -1316,11 +1323,14 @@ __device__ __forceinline__ void s_body(tmps_box* b, tmps_servo* sv, tmps_engine*
                 tot[threadIdx.x] = (double)h + (double)l;
             }
         } else {
-            const double* row = part + (size_t)c * nb;
-            double t = sum_component(row, nb, q, lane, 0.0, [](double x, double y) { return x + y; });
+            for (int vw = warp; vw < kWarpsS; vw += (int)(blockDim.x >> 5)) {
+                const int c = vw >> 2, q = vw & 3;
+                const double* row = part + (size_t)c * nb;
+                double t = sum_component(row, nb, q, lane, 0.0, [](double x, double y) { return x + y; });
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-            if (lane == 0) wsum[warp] = t;
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+                if (lane == 0) wsum[vw] = t;
+            }
             __syncthreads();
             if (threadIdx.x < 6)
                 tot[threadIdx.x] = ((wsum[4 * threadIdx.x] + wsum[4 * threadIdx.x + 1]) + wsum[4 * threadIdx.x + 2]) +
@@ -1400,14 +1410,17 @@ __global__ void __launch_bounds__(kBlockC, 2)
     const tmps_instance& I = stage_instance(si, inst, block_inst[blockIdx.x]);
     char* sc = static_cast<char*>(I.scratch);
     const int n = I.a.n;
-    // C's partials follow the instance's A blocks in its [6][nblocks] layout
-    double* part = reinterpret_cast<double*>(sc + lay_part(n)) + I.a_blocks;
+    double* part = reinterpret_cast<double*>(sc + lay_part(n));
     cf_body<STYLE, MIXED>(I.a, I.nl, I.p, I.box, I.eng, reinterpret_cast<uint32_t*>(sc),
                           reinterpret_cast<const float*>(sc + lay_gap(n)), reinterpret_cast<const float*>(sc + lay_agap(n)),
                           part, (int)blockIdx.x - I.c_first, I.c_blocks);
 }
 
-__global__ void __launch_bounds__(kBlockS) kb_s(const tmps_instance* __restrict__ inst, int32_t* status) {
+// S of a batch: one block of six warps per instance (the derived quantities
+// take one warp per kind, the virial sum runs the 24 virtual warps of the
+// single-instance S four at a time), so many instances fit in one wave.
+constexpr int kBlockSB = 192;
+__global__ void __launch_bounds__(kBlockSB) kb_s(const tmps_instance* __restrict__ inst, int32_t* status) {
     const tmps_instance& I = inst[blockIdx.x];
     s_body(I.box, I.servo, I.eng, static_cast<const char*>(I.scratch), status);
 }
@@ -1644,6 +1657,27 @@ int contact_blocks(int n, int style, bool mixed) {
     const int b = grid_for(n, kBlockC);
     return b < contact_wave(style, mixed) ? b : contact_wave(style, mixed);
 }
+// Grids under a launch shape of g 32-atom groups per warp: one block per
+// 256 g atoms for A (g passes of its grid-stride loop), one per 128 g atoms
+// for C (g groups per warp, screened kLive at a time), never more blocks than
+// the default grid (g <= 0).  Both loops cover every atom for any grid; many
+// small systems in one batched launch want g > 1, so that each block's fixed
+// latency (descriptor, engine record, partial sums) is paid for more atoms
+// and a warp of C keeps several groups in flight instead of one group per
+// block wave.  The virial partials are per block, so the shape fixes the
+// order of the virial sum (results depend on it at rounding level only).
+int a_blocks_shaped(int n, bool mixed, int g) {
+    const int d = a_blocks(n, mixed);
+    if (g <= 0) return d;
+    const int b = grid_for(n, kBlockA * g);
+    return b < d ? b : d;
+}
+int contact_blocks_shaped(int n, int style, bool mixed, int g) {
+    const int d = contact_blocks(n, style, mixed);
+    if (g <= 0) return d;
+    const int b = grid_for(n, kBlockC * g);
+    return b < d ? b : d;
+}
 // The scratch regions (lay_*): the first three depend on n alone, so A finds
 // the flag words at the base and S finds the partials through
 // tmps_engine.part_off.
@@ -1728,39 +1762,45 @@ int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream) 
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
-int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, void* scratch, void* stream) {
+int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32_t a_blocks_, void* scratch,
+                 void* stream) {
     if (!a || !d_box || !d_eng || !scratch || a->n < 0) return TMPS_ERR_BAD_ARG;
     if (!a->pos32 && (!a->rinv || !a->x0)) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
     const int n = a->n;
     const bool mixed = a->pos32 != nullptr;
+    const int gdef = a_blocks(n, mixed);
+    if (a_blocks_ > gdef) return TMPS_ERR_BAD_ARG;  // the scratch holds the default grid's partials
+    const int g = a_blocks_ > 0 ? a_blocks_ : gdef;
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t* flags = (const uint32_t*)scratch;
     double* part = (double*)((char*)scratch + part_offset(n));  // A's partials come first
     if (mixed) {
         if (!mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-        launch_pdl(k_a32, a_blocks(n, true), kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
+        launch_pdl(k_a32, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     } else {
-        launch_pdl(k_a64, a_blocks(n, false), kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
+        launch_pdl(k_a64, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     }
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
-                 const tmps_pair_params* p, void* scratch, void* stream) {
+                 const tmps_pair_params* p, int32_t c_blocks, void* scratch, void* stream) {
     if (!a || !nl || !d_box || !d_eng || !p || !scratch || a->n < 0 || nl->n != a->n) return TMPS_ERR_BAD_ARG;
     if (!a->pos32 && !a->rinv) return TMPS_ERR_BAD_ARG;
     if (p->style < 0 || p->style > 4 || nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
     if (p->style == 4 && p->rolling_id != 0 && !nl->rolling) return TMPS_ERR_BAD_ARG;
     const int n = a->n;
     const bool mixed = a->pos32 != nullptr;
-    const int g2 = contact_blocks(n, p->style, mixed);
+    const int g2def = contact_blocks(n, p->style, mixed);
+    if (c_blocks > g2def) return TMPS_ERR_BAD_ARG;  // the scratch holds the default grid's partials
+    const int g2 = c_blocks > 0 ? c_blocks : g2def;
     uint32_t* flags = (uint32_t*)scratch;
     const float* gap = (const float*)((char*)scratch + gap_offset(n));
     const float* agap = (const float*)((char*)scratch + atom_gap_offset(n));
     // partials are component-major, [6][nblocks]; C's blocks follow A's
-    double* part2 = (double*)((char*)scratch + part_offset(n)) + (size_t)a_blocks(n, mixed);
+    double* part2 = (double*)((char*)scratch + part_offset(n));
     cudaStream_t s = (cudaStream_t)stream;
     if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
 #define TMPS_LAUNCH_C(ST)                                                                                    \
@@ -1823,9 +1863,14 @@ int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void
 }
 
 int tmps_batch_blocks(int32_t n, int32_t style, int32_t mixed, int32_t* a_b, int32_t* c_b) {
+    return tmps_fused_shape(n, style, mixed, 0, 0, a_b, c_b);
+}
+
+int tmps_fused_shape(int32_t n, int32_t style, int32_t mixed, int32_t a_groups_per_warp, int32_t c_groups_per_warp,
+                     int32_t* a_b, int32_t* c_b) {
     if (n < 0 || style < 0 || style > 4 || !a_b || !c_b) return TMPS_ERR_BAD_ARG;
-    *a_b = n > 0 ? a_blocks(n, mixed != 0) : 0;
-    *c_b = n > 0 ? contact_blocks(n, style, mixed != 0) : 0;
+    *a_b = n > 0 ? a_blocks_shaped(n, mixed != 0, a_groups_per_warp) : 0;
+    *c_b = n > 0 ? contact_blocks_shaped(n, style, mixed != 0, c_groups_per_warp) : 0;
     return TMPS_OK;
 }
 
@@ -1863,7 +1908,7 @@ int tmps_batch_c(const tmps_instance* d_inst, const int32_t* d_block_inst, int32
 int tmps_batch_servo(const tmps_instance* d_inst, int32_t ninst, int32_t* d_status, void* stream) {
     if (!d_inst || ninst < 0 || !d_status) return TMPS_ERR_BAD_ARG;
     if (ninst == 0) return TMPS_OK;
-    launch_pdl(kb_s, ninst, kBlockS, (cudaStream_t)stream, d_inst, d_status);
+    launch_pdl(kb_s, ninst, kBlockSB, (cudaStream_t)stream, d_inst, d_status);
     note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }

@@ -51,7 +51,7 @@ class FusedEngine:
     LAUNCHES_PER_STEP = 3
 
     def __init__(self, sim, precision: str = "fp64", chunk: int = 64, graphs: bool = True,
-                 cull: bool = True) -> None:
+                 cull: bool = True, launch_shape: tuple[int, int] | None = None) -> None:
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.sim = sim
@@ -72,6 +72,10 @@ class FusedEngine:
         # C skips 32-atom groups whose gap bound rules out any contact (exact;
         # off screens every group, with bit-identical results)
         self.cull = bool(cull)
+        # launch shape (tmps_fused_shape): 32-atom groups per warp of A and of C, 0 = the default grid;
+        # it fixes the order of the virial sum, so equal shapes give bit-identical runs
+        shape = getattr(sim, "launch_shape", (0, 0)) if launch_shape is None else launch_shape
+        self.launch_shape = (int(shape[0]), int(shape[1]))
         self._graph = None
         self._graph_key = None
         self._hist_dw = False
@@ -87,7 +91,7 @@ class FusedEngine:
         f32 = dict(dtype=torch.float32, device=self.dev)
         self.rinv = None if self.mixed else torch.zeros((2, n), **f64)
         style, mixed = int(self.sim.pair_style.params.style), 1 if self.mixed else 0
-        self.nblocks = int(_device.lib().tmps_fused_blocks(n, style, mixed))
+        self._shape(n)
         self.part = torch.zeros(int(_device.lib().tmps_fused_scratch_bytes(n, style, mixed)), dtype=torch.uint8,
                                 device=self.dev)
         if self.mixed:
@@ -102,6 +106,26 @@ class FusedEngine:
             self.o0 = torch.zeros((3, n), **f32)
             self.cell32 = torch.zeros(n, dtype=torch.int32, device=self.dev)
         self._n = n
+
+    def _shape(self, n: int) -> None:
+        """Grids of A and C for n atoms under this engine's launch shape; nblocks = virial partials."""
+        a_b, c_b = ctypes.c_int32(), ctypes.c_int32()
+        style, mixed = int(self.sim.pair_style.params.style), 1 if self.mixed else 0
+        _lib.check(_device.lib().tmps_fused_shape(n, style, mixed, self.launch_shape[0], self.launch_shape[1],
+                                                  ctypes.byref(a_b), ctypes.byref(c_b)), "tmps_fused_shape")
+        self.a_blocks, self.c_blocks = a_b.value, c_b.value
+        self.nblocks = self.a_blocks + self.c_blocks
+
+    def set_launch_shape(self, shape: tuple[int, int]) -> None:
+        """Change the launch shape between steps (the scratch holds any shape's partials)."""
+        self.launch_shape = (int(shape[0]), int(shape[1]))
+        if self._n < 0:
+            return
+        self._shape(self._n)
+        e = self._engine_state()
+        e.nblocks = self.nblocks
+        _device.push_struct(self._eng, e)
+        self._graph = None
 
     def atoms(self) -> _lib.Atoms:
         s = self.sim.atom.cstruct()
@@ -191,10 +215,10 @@ class FusedEngine:
     def _launch_step(self, L, st, atoms, nl_struct, params) -> None:
         dbox, eng = self.sim.domain.dbox, self._eng.data_ptr()
         with _device.timed("fused_a"):
-            rc = L.tmps_fused_a(atoms, dbox, eng, self.part.data_ptr(), st)
+            rc = L.tmps_fused_a(atoms, dbox, eng, self.a_blocks, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_a")
         with _device.timed("fused_c"):
-            rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.part.data_ptr(), st)
+            rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.c_blocks, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_c")
         with _device.timed("fused_s"):
             rc = L.tmps_fused_servo(dbox, self._servo_ptr(), eng, self.part.data_ptr(), self.status.data_ptr(), st)
@@ -325,8 +349,8 @@ class FusedEngine:
         atoms = self.atoms()
         nl_struct = sim.history.cstruct(nl)
         dbox, eng = sim.domain.dbox, self._eng.data_ptr()
-        _lib.check(L.tmps_fused_c(atoms, nl_struct, dbox, eng, sim.pair_style.params, self.part.data_ptr(), st),
-                   "tmps_fused_c")
+        _lib.check(L.tmps_fused_c(atoms, nl_struct, dbox, eng, sim.pair_style.params, self.c_blocks,
+                                  self.part.data_ptr(), st), "tmps_fused_c")
         _lib.check(L.tmps_fused_servo(dbox, self._servo_ptr(), eng, self.part.data_ptr(), self.status.data_ptr(),
                                       st), "tmps_fused_servo")
 

