@@ -217,7 +217,9 @@ typedef struct tmps_engine {
      * (tmps_fused_pressure_log): step s writes plog[(s % plog_len) * 6 + k]. */
     double* plog;            /* device address of a pinned host array, or NULL */
     int32_t plog_len;
-    int32_t pad5_;
+    int32_t order_ready;     /* 1: C walks the groups in the ascending gap order
+                              * tmps_fused_bounds left in the scratch (set by S
+                              * after the first step that follows the bounds) */
     int64_t stop_step;       /* fused launches do nothing once step >= stop_step (batched runs) */
 } tmps_engine;
 
@@ -248,6 +250,11 @@ const char* tmps_version(void);
 /* Kernels launched by this library since it was loaded (all entry points);
  * no reference counterpart. */
 long long tmps_launch_count(void);
+
+/* The CUDA runtime's last error on this host thread, by name and text
+ * (left set; an entry point that returned TMPS_ERR_CUDA left it there);
+ * no reference counterpart. */
+const char* tmps_last_cuda_error(void);
 
 /* Copies a host box into device memory (Domain._sync, domain.py:235-254). */
 int tmps_box_set(tmps_box* d_box, const tmps_box* h_box, void* stream);

@@ -3,11 +3,33 @@
 from __future__ import annotations
 
 import ctypes
+import gc
 
 import numpy as np
 import torch
 
 from . import _lib
+
+
+def capture_graph(launch) -> torch.cuda.CUDAGraph:
+    """Captures what `launch()` enqueues on the current stream into a CUDA graph (on a side
+    stream).  Python's cyclic garbage collector is held off during the capture: a collection
+    inside it could destroy an unreferenced graph of an earlier run, a call CUDA does not
+    permit while a stream is capturing (the capture would be invalidated)."""
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    enabled = gc.isenabled()
+    gc.disable()
+    try:
+        with torch.cuda.graph(g, stream=side):
+            launch()
+    finally:
+        if enabled:
+            gc.enable()
+    torch.cuda.current_stream().wait_stream(side)
+    return g
 
 
 # Optional per-launch CUDA-event timing, keyed by kernel name; None when off.

@@ -105,7 +105,7 @@ class Engine(ctypes.Structure):
         ("prd_ref", c_f64 * 3), ("part_off", ctypes.c_int64),
         ("shift_bound", ctypes.c_float), ("maxd2_bits", ctypes.c_uint32), ("cull", c_i32),
         ("cull_tol", ctypes.c_float),
-        ("plog", ctypes.c_void_p), ("plog_len", c_i32), ("pad5_", c_i32),
+        ("plog", ctypes.c_void_p), ("plog_len", c_i32), ("order_ready", c_i32),
         ("stop_step", ctypes.c_int64),
     ]
 
@@ -181,6 +181,7 @@ STATUS_NLIST_OVERFLOW, STATUS_NONFINITE, STATUS_BOX_NONPOSITIVE, STATUS_CELL_OVE
 _SIGS = {
     "tmps_version": (ctypes.c_char_p, []),
     "tmps_launch_count": (ctypes.c_longlong, []),
+    "tmps_last_cuda_error": (ctypes.c_char_p, []),
     "tmps_box_set": (c_i32, [c_vp, ctypes.POINTER(Box), c_vp]),
     "tmps_verlet_initial": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),
     "tmps_verlet_final": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),
@@ -275,6 +276,8 @@ def check(rc: int, what: str) -> None:
     if rc != TMPS_OK:
         kind = {TMPS_ERR_BAD_ARG: "bad argument", TMPS_ERR_CUDA: "CUDA launch failure",
                 TMPS_ERR_TOO_LARGE: "size beyond the fixed scratch"}.get(rc, str(rc))
+        if rc == TMPS_ERR_CUDA and _lib is not None:
+            kind += f" ({_lib.tmps_last_cuda_error().decode()})"
         raise TmpsError(f"{what} failed: {kind}")
 
 

@@ -122,12 +122,22 @@ __device__ __forceinline__ void pdl_enter() {
 }
 
 // Scratch layout of one instance: [flag words, one per 32-atom group + 1]
-// [per-group gaps][per-atom gaps][virial partials, component-major [6][blocks
-// of A and C]], each region on a 256-byte boundary.
+// [per-group gaps][per-atom gaps][groups in ascending gap order][their gaps]
+// [sort keys, a power of two of them][virial partials, component-major
+// [6][blocks of A and C]], each region on a 256-byte boundary.
 __host__ __device__ inline size_t lay_round256(size_t b) { return (b + 255) & ~size_t(255); }
-__host__ __device__ inline size_t lay_gap(int n) { return lay_round256((size_t)((n + 31) / 32 + 1) * sizeof(uint32_t)); }
-__host__ __device__ inline size_t lay_agap(int n) { return lay_gap(n) + lay_round256((size_t)((n + 31) / 32) * sizeof(float)); }
-__host__ __device__ inline size_t lay_part(int n) { return lay_agap(n) + lay_round256((size_t)n * sizeof(float)); }
+__host__ __device__ inline int lay_groups(int n) { return (n + 31) / 32; }
+__host__ __device__ inline int lay_npad(int n) {
+    int p = 2;
+    while (p < lay_groups(n)) p <<= 1;
+    return p;
+}
+__host__ __device__ inline size_t lay_gap(int n) { return lay_round256((size_t)(lay_groups(n) + 1) * sizeof(uint32_t)); }
+__host__ __device__ inline size_t lay_agap(int n) { return lay_gap(n) + lay_round256((size_t)lay_groups(n) * sizeof(float)); }
+__host__ __device__ inline size_t lay_order(int n) { return lay_agap(n) + lay_round256((size_t)n * sizeof(float)); }
+__host__ __device__ inline size_t lay_sgap(int n) { return lay_order(n) + lay_round256((size_t)lay_groups(n) * sizeof(int32_t)); }
+__host__ __device__ inline size_t lay_keys(int n) { return lay_sgap(n) + lay_round256((size_t)lay_groups(n) * sizeof(float)); }
+__host__ __device__ inline size_t lay_part(int n) { return lay_keys(n) + lay_round256((size_t)lay_npad(n) * sizeof(uint64_t)); }
 
 __device__ __forceinline__ bool rebuild_due(const tmps_engine* __restrict__ e, int64_t s) {
     const int64_t since = s - e->last_build_step;
@@ -414,7 +424,72 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
         E->shift_bound = 0.0f;
         for (int c = 0; c < 3; ++c) E->prd_ref[c] = B->prd[c];
         E->cull = (cull && !single) ? 1 : 0;
+        E->order_ready = 0;  // the first pass after the bounds visits every group
     }
+}
+
+// Groups in ascending order of their gap bound, for C's ordered pass.  Key:
+// the gap's bits made to order as unsigned (a NaN first), then the group.
+// Deterministic: a bitonic sort of distinct keys.
+__global__ void __launch_bounds__(256) k_gap_keys(const float* __restrict__ gap, int ng, int npad,
+                                                  uint64_t* __restrict__ keys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    if (i >= ng) {
+        keys[i] = ~0ull;
+        return;
+    }
+    const uint32_t u = __float_as_uint(gap[i]);
+    uint32_t k;
+    if ((u & 0x7fffffffu) > 0x7f800000u) k = 0u;  // NaN: culls nothing, so first
+    else k = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    keys[i] = ((uint64_t)k << 32) | (uint32_t)i;
+}
+
+__global__ void __launch_bounds__(256) k_bitonic_global(uint64_t* __restrict__ keys, int npad, int j, int k) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    const int l = i ^ j;
+    if (l <= i) return;
+    const uint64_t a = keys[i], b = keys[l];
+    if ((a > b) == ((i & k) == 0)) {
+        keys[i] = b;
+        keys[l] = a;
+    }
+}
+
+// Stages k_lo..k_hi of the bitonic sort inside chunks of `chunk` keys (the
+// first stage from j = j_first), one block of chunk / 2 threads per chunk.
+constexpr int kSortChunk = 2048;
+__global__ void __launch_bounds__(kSortChunk / 2) k_bitonic_shared(uint64_t* __restrict__ keys, int chunk, int k_lo,
+                                                                 int k_hi, int j_first) {
+    __shared__ uint64_t sk[kSortChunk];
+    const int c0 = blockIdx.x * chunk;
+    for (int t = threadIdx.x; t < chunk; t += blockDim.x) sk[t] = keys[c0 + t];
+    __syncthreads();
+    for (int k = k_lo; k <= k_hi; k <<= 1) {
+        for (int j = (k == k_lo ? j_first : k >> 1); j > 0; j >>= 1) {
+            const int t = threadIdx.x;
+            const int i = 2 * t - (t & (j - 1));  // lower element of the pair
+            const int l = i + j;
+            const uint64_t a = sk[i], b = sk[l];
+            if ((a > b) == (((c0 + i) & k) == 0)) {
+                sk[i] = b;
+                sk[l] = a;
+            }
+            __syncthreads();
+        }
+    }
+    for (int t = threadIdx.x; t < chunk; t += blockDim.x) keys[c0 + t] = sk[t];
+}
+
+__global__ void __launch_bounds__(256) k_gap_order(const uint64_t* __restrict__ keys, const float* __restrict__ gap,
+                                                   int ng, int32_t* __restrict__ order, float* __restrict__ sgap) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ng) return;
+    const int g = (int)(uint32_t)keys[p];
+    order[p] = g;
+    sgap[p] = gap[g];
 }
 
 // C: the contact forces of one step.  Per warp, 32 groups strided over the
@@ -449,7 +524,8 @@ template <int STYLE, bool MIXED>
 __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L, const tmps_pair_params& P,
                                         const tmps_box* __restrict__ B, tmps_engine* __restrict__ E,
                                         uint32_t* __restrict__ flags, const float* __restrict__ gap,
-                                        const float* __restrict__ agap, double* __restrict__ part, const int bid,
+                                        const float* __restrict__ agap, const int32_t* __restrict__ order,
+                                        const float* __restrict__ sgap, double* __restrict__ part, const int bid,
                                         const int nblk) {
     using T = typename std::conditional<MIXED, float, double>::type;
     __shared__ double smem[6 * (kBlockC / 32)];
@@ -940,21 +1016,35 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
     };
     if (lane < kLive) cwords[wib][lane] = 0u;
     __syncwarp();
+    // Ordered pass: after the first pass that follows the bounds (which
+    // visits every group, clears the flags of those it rules out and their
+    // stale forces), thr only grows until the next bounds, so a group ruled
+    // out stays out with its flags clear, and the live groups are a prefix of
+    // the ascending gap order.  Walking that order instead of the group
+    // index gives every warp the same number of live groups (+-1).
+    const bool ordered = cull && E->order_ready != 0;
     int ncand = 0;  // atoms waiting in croster (warp-uniform)
     for (int base = gw; base < ngroups; base += 32 * nwarps) {
-        const int mygrp = base + lane * nwarps;
+        const int k = base + lane * nwarps;
+        int mygrp = k;
         uint32_t myold = 0u;
         bool live = false;
-        if (mygrp < ngroups) {
-            myold = flags[mygrp];
-            live = !(cull && gap[mygrp] > thr);
-            if (!live && myold != 0u) {
-                // ruled out now, flagged last step: clear the stale forces
-                for (uint32_t w = myold; w; w &= w - 1) zero_force<MIXED>(A, (mygrp << 5) + __ffs(w) - 1);
-                flags[mygrp] = 0u;
+        if (k < ngroups) {
+            if (ordered) {
+                mygrp = order[k];
+                live = !(sgap[k] > thr);
+            } else {
+                myold = flags[mygrp];
+                live = !(cull && gap[mygrp] > thr);
+                if (!live && myold != 0u) {
+                    // ruled out now, flagged last step: clear the stale forces
+                    for (uint32_t w = myold; w; w &= w - 1) zero_force<MIXED>(A, (mygrp << 5) + __ffs(w) - 1);
+                    flags[mygrp] = 0u;
+                }
             }
         }
         uint32_t pending = __ballot_sync(0xffffffffu, live);
+        if (ordered && pending == 0u) break;  // no later position of this warp is live
         while (pending) {
             // up to kLive live groups at once
             int gq[kLive];
@@ -967,17 +1057,19 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                 if (pending) {
                     const int src = __ffs(pending) - 1;
                     pending &= pending - 1;
-                    gq[u] = base + src * nwarps;
+                    gq[u] = __shfl_sync(0xffffffffu, mygrp, src);
                     oq[u] = __shfl_sync(0xffffffffu, myold, src);
                     nq = u + 1;
                 }
             }
-            // the atoms' own bounds, all issued at once
+            // the atoms' own bounds (and, in the ordered pass, the groups'
+            // flag words), all issued at once
             float ag[kLive];
 #pragma unroll
             for (int u = 0; u < kLive; ++u) {
                 const int i = (gq[u] << 5) + lane;
                 ag[u] = (u < nq && i < n) ? agap[i] : 0.0f;
+                if (ordered && u < nq) oq[u] = flags[gq[u]];
             }
             int near_total = 0;
 #pragma unroll
@@ -1056,7 +1148,9 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
     k_cf(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
          tmps_engine* __restrict__ E, uint32_t* __restrict__ flags, const float* __restrict__ gap,
          const float* __restrict__ agap, double* __restrict__ part) {
-    cf_body<STYLE, MIXED>(A, L, P, B, E, flags, gap, agap, part, blockIdx.x, gridDim.x);
+    const char* sc = reinterpret_cast<const char*>(flags);  // the scratch base
+    cf_body<STYLE, MIXED>(A, L, P, B, E, flags, gap, agap, reinterpret_cast<const int32_t*>(sc + lay_order(A.n)),
+                          reinterpret_cast<const float*>(sc + lay_sgap(A.n)), part, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------- S
@@ -1341,6 +1435,7 @@ __device__ __forceinline__ void s_body(tmps_box* b, tmps_servo* sv, tmps_engine*
     if (warp == 0) {
         if (lane == 0) {
             se.step = s;
+            se.order_ready = se.cull;  // C has had its first pass since the bounds
             sb.remap_pending = 0;
             if (se.servo) {
                 ssv.step_count += 1;
@@ -1413,7 +1508,9 @@ __global__ void __launch_bounds__(kBlockC, 2)
     double* part = reinterpret_cast<double*>(sc + lay_part(n));
     cf_body<STYLE, MIXED>(I.a, I.nl, I.p, I.box, I.eng, reinterpret_cast<uint32_t*>(sc),
                           reinterpret_cast<const float*>(sc + lay_gap(n)), reinterpret_cast<const float*>(sc + lay_agap(n)),
-                          part, (int)blockIdx.x - I.c_first, I.c_blocks);
+                          reinterpret_cast<const int32_t*>(sc + lay_order(n)),
+                          reinterpret_cast<const float*>(sc + lay_sgap(n)), part, (int)blockIdx.x - I.c_first,
+                          I.c_blocks);
 }
 
 // S of a batch: one block of six warps per instance (the derived quantities
@@ -1838,9 +1935,30 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
     float* gap = (float*)((char*)scratch + gap_offset(n));
     float* agap = (float*)((char*)scratch + atom_gap_offset(n));
     const int g = n > 0 ? grid_for(n, kBlockA) : 1;
-    k_bounds<<<g, kBlockA, 0, (cudaStream_t)stream>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, cull ? 1 : 0, flags,
-                                                       gap, agap);
+    cudaStream_t st = (cudaStream_t)stream;
+    k_bounds<<<g, kBlockA, 0, st>>>(*a, *nl, d_box, d_eng, has_hist ? 1 : 0, cull ? 1 : 0, flags, gap, agap);
     note_launches(1);
+    if (cull && n > 0) {
+        // the groups in ascending gap order (C's ordered pass)
+        const int ng = lay_groups(n), npad = lay_npad(n);
+        uint64_t* keys = (uint64_t*)((char*)scratch + lay_keys(n));
+        const int bt = npad < 256 ? npad : 256;
+        k_gap_keys<<<grid_for(npad, bt), bt, 0, st>>>(gap, ng, npad, keys);
+        const int chunk = npad < kSortChunk ? npad : kSortChunk;
+        k_bitonic_shared<<<npad / chunk, chunk / 2, 0, st>>>(keys, chunk, 2, chunk, 1);
+        int launches = 2;
+        for (int k = 2 * chunk; k <= npad; k <<= 1) {
+            for (int j = k >> 1; j >= chunk; j >>= 1) {
+                k_bitonic_global<<<grid_for(npad, bt), bt, 0, st>>>(keys, npad, j, k);
+                ++launches;
+            }
+            k_bitonic_shared<<<npad / chunk, chunk / 2, 0, st>>>(keys, chunk, k, k, chunk / 2);
+            ++launches;
+        }
+        k_gap_order<<<grid_for(ng, 256), 256, 0, st>>>(keys, gap, ng, (int32_t*)((char*)scratch + lay_order(n)),
+                                                       (float*)((char*)scratch + lay_sgap(n)));
+        note_launches(launches + 1);
+    }
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 

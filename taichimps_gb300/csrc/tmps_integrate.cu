@@ -322,6 +322,13 @@ const char* tmps_version(void) { return "taichimps_gb300 0.1 (sm_103a)"; }
 
 long long tmps_launch_count(void) { return tmps::g_launches.load(std::memory_order_relaxed); }
 
+const char* tmps_last_cuda_error(void) {
+    static thread_local char buf[256];
+    const cudaError_t e = cudaPeekAtLastError();
+    snprintf(buf, sizeof(buf), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+    return buf;
+}
+
 int tmps_box_set(tmps_box* d_box, const tmps_box* h_box, void* stream) {
     if (!d_box || !h_box) return TMPS_ERR_BAD_ARG;
     cudaError_t e = cudaMemcpyAsync(d_box, h_box, sizeof(tmps_box), cudaMemcpyHostToDevice,

@@ -275,16 +275,13 @@ class FusedEngine:
                sim.neighbor.nbr.data_ptr())
         if self._graph is None or self._graph_key != key:
             self._graph = None
-            torch.cuda.synchronize()
-            g = torch.cuda.CUDAGraph()
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.graph(g, stream=side):
+
+            def chunk():
                 st = _device.stream()
                 for _ in range(self.chunk):
                     self._launch_step(L, st, atoms, nl_struct, params)
-            torch.cuda.current_stream().wait_stream(side)
-            self._graph, self._graph_key = g, key
+
+            self._graph, self._graph_key = _device.capture_graph(chunk), key
         self._graph.replay()
         self.graph_replays += 1
         self.graph_kernel_launches += self.chunk * self.LAUNCHES_PER_STEP
@@ -356,6 +353,9 @@ class FusedEngine:
 
     def finish(self) -> None:
         """Settle pending updates and hand the state back to the per-hook path."""
+        # the captured graph goes now, not whenever the engine is collected (which may be
+        # during a later capture)
+        self._graph = self._graph_key = None
         sim = self.sim
         L = _device.lib()
         st = _device.stream()

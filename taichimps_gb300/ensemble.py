@@ -110,16 +110,12 @@ class BatchedEngine:
                 self._launch_step(L, st)
             return
         if self._graph is None:
-            torch.cuda.synchronize()
-            g = torch.cuda.CUDAGraph()
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.graph(g, stream=side):
+            def chunk():
                 st = _device.stream()
                 for _ in range(self.chunk):
                     self._launch_step(L, st)
-            torch.cuda.current_stream().wait_stream(side)
-            self._graph = g
+
+            self._graph = _device.capture_graph(chunk)
         self._graph.replay()
         self.graph_replays += 1
 
