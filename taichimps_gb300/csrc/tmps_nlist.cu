@@ -159,14 +159,17 @@ __global__ void __launch_bounds__(kBlock) k_permute(tmps_atoms src, tmps_atoms d
 // multiply-add contraction can move a pair across the cut.
 //
 // With `off32` (and every periodic dimension at least 3 cells wide) each
-// candidate first meets an FP32 prefilter on cell-local offsets: a pair
-// within the cut lies in adjacent cells, so its separation is exactly
+// candidate first meets an FP32 test on cell-local offsets: a pair within
+// the cut lies in adjacent cells, so its separation is exactly
 // (o_i - o_j) - offset * h, which FP32 carries to ~1e-6 of (h + |o|).  A
-// candidate is dropped only when its FP32 distance exceeds the cut by more
-// than ten times that error bound; every other candidate gets the exact FP64
-// test, so the list is the same pair set the FP64 test alone gives, at a
-// fraction of the FP64 work (this part's FP64 pipe is ~70x narrower than its
-// FP32 pipe, and the exact test divides).
+// candidate is dropped when its FP32 distance exceeds the cut by more than
+// ten times that error bound, and taken when it falls short of the cut by
+// as much (the cut is at most one cell, under a third of the box, so the
+// minimum image the FP64 test would pick is the stencil's image); only the
+// candidates in that narrow band get the exact FP64 test.  The list is the
+// pair set the FP64 test alone gives, at a sliver of the FP64 work (this
+// part's FP64 pipe is ~70x narrower than its FP32 pipe, and the exact test
+// divides).
 __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* __restrict__ b,
                                                   double skin, const int32_t* __restrict__ cell_of,
                                                   const int32_t* __restrict__ rank,
@@ -212,14 +215,26 @@ __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* 
                 const float fx = (float)ox * h32[0], fy = (float)oy * h32[1], fz = (float)oz * h32[2];
                 for (int q = beg; q < end; ++q) {
                     if (q == p) continue;
+                    bool inside = false;
                     if (pre) {
                         const float4 oj = off32[q];
                         const float dx = (oi.x - oj.x) - fx, dy = (oi.y - oj.y) - fy, dz = (oi.z - oj.z) - fz;
                         const float rq = (dx * dx + dy * dy) + dz * dz;
                         const float mj = fmaxf(fmaxf(fabsf(oj.x), fabsf(oj.y)), fabsf(oj.z));
                         const float cut = (oi.w + oj.w) + skin32;
-                        const float lim = cut + 1e-5f * (((hsum + mi) + mj) + cut);
+                        const float slack = 1e-5f * (((hsum + mi) + mj) + cut);
+                        const float lim = cut + slack, near = cut - slack;
                         if (!(rq < lim * lim) && rq == rq) continue;  // out of reach (a NaN goes on to the exact test)
+                        inside = near > 0.0f && rq < near * near;     // within reach beyond doubt
+                    }
+                    if (inside) {
+                        if (count < nl.slots) {
+                            nl.nbr[(size_t)count * n + p] = q | (code << kNbrIndexBits);
+                            ++count;
+                        } else {
+                            overflow = true;
+                        }
+                        continue;
                     }
                     const double4 xj = ld4(a.xr, q);
                     double d[3] = {__dsub_rn(xi.x, xj.x), __dsub_rn(xi.y, xj.y), __dsub_rn(xi.z, xj.z)};
