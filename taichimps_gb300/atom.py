@@ -66,7 +66,11 @@ class FieldView:
         vals = self._internal().detach()
         ordered = torch.empty(vals.shape, dtype=vals.dtype, device=vals.device)
         ordered[a.buffers.uid.long()] = vals
-        host = ordered.cpu().numpy().astype(self._dtype, copy=False)
+        # through page-locked memory: a direct DMA at link speed instead of a staged copy
+        staged = torch.empty(vals.shape, dtype=vals.dtype, pin_memory=True)
+        staged.copy_(ordered, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        host = staged.numpy().astype(self._dtype, copy=False)
         if a.nlocal == a.max_atoms:
             return host
         out = np.zeros(shape, dtype=self._dtype)

@@ -386,12 +386,16 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
         iprd[c] = B->inv_prd[c];
         single = single || (per[c] == 1 && B->g[c] == 1);
     }
+    // The bound only has to be a lower bound: the separation is formed in FP64
+    // (its image as the reference picks it), the distance and gap in FP32, and
+    // the gap is then lowered by well over the FP32 error (a few ulps of r and
+    // of the radii): a bound a little low only culls a little less.
     for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += nwarps) {
         const int i = (g << 5) + lane;
-        double gmin = 1e300;
+        float gmin = 3e38f;
         if (i < n) {
             const double xi[3] = {A.x0[i], A.x0[n + i], A.x0[2 * n + i]};
-            const double ri = A.xr[4 * (size_t)i + 3];
+            const float ri = (float)A.xr[4 * (size_t)i + 3];
             const int nn = L.nnb[i];
             for (int k = 0; k < nn; ++k) {
                 const int j = L.nbr[(size_t)k * n + i] & kNbrIndexMask;
@@ -399,17 +403,19 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
 #pragma unroll
                 for (int c = 0; c < 3; ++c)
                     if (per[c] == 1) d[c] -= rint(d[c] * iprd[c]) * prd[c];
-                const double r = sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
-                const double gp = r - (ri + A.xr[4 * (size_t)j + 3]);
-                gmin = gp == gp ? fmin(gmin, gp) : -1e300;  // a NaN pair pins the group
+                const float f0 = (float)d[0], f1 = (float)d[1], f2 = (float)d[2];
+                const float r = sqrtf((f0 * f0 + f1 * f1) + f2 * f2);
+                const float rs = ri + (float)A.xr[4 * (size_t)j + 3];
+                const float gp = (r - rs) - 1e-6f * (r + rs);
+                gmin = gp == gp ? fminf(gmin, gp) : -3e38f;  // a NaN pair pins the group
             }
-            if ((hist && L.touch[i] != 0ull) || single) gmin = -1e300;
-            agap[i] = __double2float_rd(gmin);
+            if ((hist && L.touch[i] != 0ull) || single) gmin = -3e38f;
+            agap[i] = gmin;
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) gmin = fmin(gmin, __shfl_down_sync(0xffffffffu, gmin, o));
+        for (int o = 16; o > 0; o >>= 1) gmin = fminf(gmin, __shfl_down_sync(0xffffffffu, gmin, o));
         if (lane == 0) {
-            gap[g] = __double2float_rd(gmin);
+            gap[g] = gmin;
             // bits of existing atoms only: a set bit makes C clear that atom's force
             const int rem = n - (g << 5);
             flags[g] = rem >= 32 ? 0xffffffffu : (1u << rem) - 1u;
