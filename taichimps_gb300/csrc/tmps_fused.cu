@@ -1383,23 +1383,25 @@ __device__ __forceinline__ void s_body(tmps_box* b, tmps_servo* sv, tmps_engine*
     __shared__ ServoNew snew;
     copy_words(&sb, b);
     copy_words(&ssv, sv);
-    pdl_enter();
-    copy_words(&se, e);
+    // run constants of the engine record (only the host changes them, between
+    // launches), so the partial sums can be fetched with this step's words
+    const int nb = e->nblocks;
+    const int64_t part_off = e->part_off;
+    const bool mixed = e->mixed != 0, servo = e->servo != 0;
     __syncthreads();
-    if (se.aborted || se.step >= se.stop_step) return;
-    const int64_t s = se.step + 1;
-    if (rebuild_due(&se, s)) {
-        if (threadIdx.x == 0) e->aborted = 1;
-        return;
-    }
+    const bool servo_now = servo && ((ssv.step_count + 1) % ssv.nevery == 0);
+    pdl_enter();
+    // this step's engine words (A and C write some) and the virial partials in
+    // flight together; one word per thread (the batched S has 192 threads)
+    constexpr int kEngineWords = (int)(sizeof(tmps_engine) / 4);
+    static_assert(kEngineWords <= 192, "one engine word per thread of the batched S");
+    const uint32_t ew = (int)threadIdx.x < kEngineWords ? reinterpret_cast<const uint32_t*>(e)[threadIdx.x] : 0u;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const bool servo_now = se.servo && ((ssv.step_count + 1) % ssv.nevery == 0);
     if (servo_now) {
-        const double* part = reinterpret_cast<const double*>(scratch + se.part_off);
-        const int nb = se.nblocks;
+        const double* part = reinterpret_cast<const double*>(scratch + part_off);
         // kWarpsS virtual warps, four per component; a block of fewer warps
         // runs several in turn, with the same arithmetic each
-        if (se.mixed) {
+        if (mixed) {
             for (int vw = warp; vw < kWarpsS; vw += (int)(blockDim.x >> 5)) {
                 const int c = vw >> 2, q = vw & 3;
                 const float2* row = reinterpret_cast<const float2*>(part) + (size_t)c * nb;
@@ -1415,13 +1417,6 @@ __device__ __forceinline__ void s_body(tmps_box* b, tmps_servo* sv, tmps_engine*
                 }
                 if (lane == 0) wsumf[vw] = acc;
             }
-            __syncthreads();
-            if (threadIdx.x < 6) {
-                float h = 0.0f, l = 0.0f;
-#pragma unroll
-                for (int w = 0; w < 4; ++w) dw_add2(h, l, wsumf[4 * threadIdx.x + w].x, wsumf[4 * threadIdx.x + w].y);
-                tot[threadIdx.x] = (double)h + (double)l;
-            }
         } else {
             for (int vw = warp; vw < kWarpsS; vw += (int)(blockDim.x >> 5)) {
                 const int c = vw >> 2, q = vw & 3;
@@ -1431,10 +1426,27 @@ __device__ __forceinline__ void s_body(tmps_box* b, tmps_servo* sv, tmps_engine*
                 for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
                 if (lane == 0) wsum[vw] = t;
             }
-            __syncthreads();
-            if (threadIdx.x < 6)
+        }
+    }
+    if ((int)threadIdx.x < kEngineWords) reinterpret_cast<uint32_t*>(&se)[threadIdx.x] = ew;
+    __syncthreads();
+    if (se.aborted || se.step >= se.stop_step) return;
+    const int64_t s = se.step + 1;
+    if (rebuild_due(&se, s)) {
+        if (threadIdx.x == 0) e->aborted = 1;
+        return;
+    }
+    if (servo_now) {
+        if (threadIdx.x < 6) {
+            if (mixed) {
+                float h = 0.0f, l = 0.0f;
+#pragma unroll
+                for (int w = 0; w < 4; ++w) dw_add2(h, l, wsumf[4 * threadIdx.x + w].x, wsumf[4 * threadIdx.x + w].y);
+                tot[threadIdx.x] = (double)h + (double)l;
+            } else {
                 tot[threadIdx.x] = ((wsum[4 * threadIdx.x] + wsum[4 * threadIdx.x + 1]) + wsum[4 * threadIdx.x + 2]) +
                                    wsum[4 * threadIdx.x + 3];
+            }
         }
         __syncthreads();
     }
