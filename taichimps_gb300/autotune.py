@@ -45,9 +45,10 @@ def _moved(ptr: int, src: torch.Tensor, dst: torch.Tensor) -> int:
 
 
 class _Trial:
-    """One instance's descriptor with every output of A and C pointing at a copy."""
+    """One instance's descriptor with every output of A and C pointing at a copy (its engine
+    record at `rec`, a row of the batch's table of record copies)."""
 
-    def __init__(self, eng) -> None:
+    def __init__(self, eng, rec: torch.Tensor) -> None:
         sim = eng.sim
         self.eng = eng
         d = eng.instance(0, eng.a_blocks, 0, eng.c_blocks)
@@ -75,15 +76,9 @@ class _Trial:
         if d.nl.rolling:
             d.nl.rolling = redirect(d.nl.rolling, h.rolling)
         d.scratch = redirect(d.scratch, eng.part)
-        self.rec = eng._eng.clone()
-        self.keep.append(self.rec)
-        d.eng = self.rec.data_ptr()
+        rec.copy_(eng._eng)
+        d.eng = rec.data_ptr()
         self.d = d
-
-    def set_blocks(self, nblocks: int) -> None:
-        rec = _device.pull_struct(self.rec, _lib.Engine)
-        rec.nblocks = nblocks
-        _device.push_struct(self.rec, rec)
 
 
 def _time(launch, reps: int) -> float:
@@ -105,7 +100,12 @@ def tune_launch_shape(batched, candidates=CANDIDATES, reps: int = 8) -> dict:
     st = _device.stream()
     mixed = 1 if batched.mixed else 0
     size = ctypes.sizeof(_lib.Instance)
-    trials = [_Trial(e) for e in batched.engines]
+    esize = ctypes.sizeof(_lib.Engine)
+    # every instance's engine record copy, one row each, rows 16-byte aligned
+    stride = (esize + 15) // 16 * 16
+    recs = torch.zeros((len(batched.engines), stride), dtype=torch.uint8, device=batched.dev)
+    trials = [_Trial(e, recs[i, :esize]) for i, e in enumerate(batched.engines)]
+    nb_word = _lib.Engine.nblocks.offset // 4
     a_us, c_us = {}, {}
     a_b, c_b = ctypes.c_int32(), ctypes.c_int32()
     tables = {}
@@ -127,8 +127,8 @@ def tune_launch_shape(batched, candidates=CANDIDATES, reps: int = 8) -> dict:
 
     def shape(g):
         d_inst, d_a, d_c, nblocks = tables[g]
-        for t, nb in zip(trials, nblocks):
-            t.set_blocks(nb)  # the partial layout of this shape
+        # the partial layout of this shape, in every record copy at once
+        recs.view(torch.int32)[:, nb_word] = torch.tensor(nblocks, dtype=torch.int32).to(batched.dev)
         return d_inst, d_a, d_c
 
     # C first: its trials move no atom, so A's trials (which do, in the copies) cannot trip the
@@ -141,7 +141,7 @@ def tune_launch_shape(batched, candidates=CANDIDATES, reps: int = 8) -> dict:
         d_inst, d_a, _ = shape(g)
         a_us[g] = _time(lambda: _lib.check(L.tmps_batch_a(d_inst.data_ptr(), d_a.data_ptr(), d_a.numel(), mixed,
                                                           st), "tmps_batch_a"), reps)
-    del trials
+    del trials, recs
     best_a = min(a_us, key=lambda k: (a_us[k], k))
     best_c = min(c_us, key=lambda k: (c_us[k], k))
     return {"launch_shape": (best_a, best_c), "a_us": a_us, "c_us": c_us}
