@@ -499,9 +499,12 @@ __global__ void __launch_bounds__(256) k_gap_order(const uint64_t* __restrict__ 
 }
 
 // C: the contact forces of one step.  Per warp, 32 groups strided over the
-// system (warp w owns groups w, w + nwarps, ...; warps numbered across blocks
-// first, so neighbouring groups -- atoms are in Morton order -- go to
-// different SMs):
+// system (warp w owns positions w, w + nwarps, ...; warps numbered across
+// blocks first).  The first pass after the bounds takes the groups in index
+// order (neighbouring groups -- atoms are in Morton order -- go to different
+// SMs); every later pass takes them in ascending order of their gap bound, in
+// which the live groups are a prefix, so each warp gets the same number of
+// live groups and stops at its first ruled-out position:
 //  1. bound check, one group per lane: a group whose smallest gap at the
 //     reference positions (tmps_fused_bounds) exceeds 2 max|x - x0| + the
 //     change of the periodic image shifts + a rounding slack cannot touch
@@ -524,8 +527,8 @@ __global__ void __launch_bounds__(256) k_gap_order(const uint64_t* __restrict__ 
 // torque are written as zeros only when it was flagged the step before, so
 // every unflagged atom holds an exact zero, which A relies on to skip
 // loading them.  None of the skipping changes a result.  The per-block
-// virial partials depend only on the flag words and the grid, not on
-// scheduling; the kinetic term of an unflagged atom is A's.
+// virial partials depend only on the flag words, the group order and the
+// grid, not on scheduling; the kinetic term of an unflagged atom is A's.
 template <int STYLE, bool MIXED>
 __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L, const tmps_pair_params& P,
                                         const tmps_box* __restrict__ B, tmps_engine* __restrict__ E,
