@@ -22,6 +22,7 @@ Two precisions:
 from __future__ import annotations
 
 import ctypes
+import weakref
 
 import numpy as np
 import torch
@@ -54,7 +55,10 @@ class FusedEngine:
                  cull: bool = True, launch_shape: tuple[int, int] | None = None) -> None:
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
-        self.sim = sim
+        # the Simulation keeps its last engine (Simulation.last_engine); the engine refers back
+        # weakly, so a finished run's device memory goes with the Simulation instead of waiting
+        # for the cycle collector
+        self._sim = weakref.ref(sim)
         self.precision = precision
         self.mixed = precision == "mixed"
         self.chunk = int(chunk)
@@ -81,6 +85,13 @@ class FusedEngine:
         self._hist_dw = False
         self.graph_replays = 0
         self.graph_kernel_launches = 0
+
+    @property
+    def sim(self):
+        sim = self._sim()
+        if sim is None:
+            raise RuntimeError("the Simulation of this fused engine no longer exists")
+        return sim
 
     # ------------------------------------------------------------ storage
 
