@@ -4,19 +4,22 @@ The fused step engine behind ``Simulation.run``.
 One step of Simulation._sub_step_inner (simulation.py:205-247) with fix
 nve/sphere, optionally damping/cundall and deform/pressure, becomes three
 kernels (tmps_fused_a, tmps_fused_c, tmps_fused_servo) that decide on the
-device whether the step needs a neighbor rebuild.  Steps are queued in chunks (replayed as CUDA graphs) with one host
-synchronisation per chunk.  When a step finds it needs a rebuild, every later
-launch of the chunk does nothing; the host then rebuilds exactly as the
-reference does at that step (save history, wrap, build, restore history),
-finishes the step, and carries on.
+device whether the step needs a neighbor rebuild.  Steps are queued in
+chunks (replayed as CUDA graphs) with one host synchronisation per chunk.
+When a step finds it needs a rebuild, every later launch of the chunk does
+nothing; the host then rebuilds exactly as the reference does at that step
+(save history, wrap, build, restore history), finishes the step, and
+carries on.
 
 Two precisions:
   "fp64"  every operation FP64 (the plain FP64 form);
   "mixed" FP32 contact arithmetic and per-atom force accumulation;
           positions (offsets from each atom's cell origin), velocities and
           angular velocities as double-word FP32 (hi + lo, ~48 bits) updated
-          with error-free transforms; FP64 shear history; virial partials as
-          double words, their totals -- what the servo reads -- in FP64.
+          with error-free transforms; the contact histories as double words
+          too while the run lasts (doubles before a rebuild carries them over
+          and at the end); virial partials as double words, their totals --
+          what the servo reads -- in FP64.
 """
 
 from __future__ import annotations
