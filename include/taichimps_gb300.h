@@ -303,19 +303,24 @@ int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_bo
 
 /* No counterpart in the reference: tmps_nlist_build for callers that cannot
  * allocate device memory at all -- a host whose device memory all belongs to
- * its own fixed arena, code running while a CUDA graph is captured (no
- * cudaMalloc allowed there), or a foreign-language host that can only pass
- * the arrays it registered.  Same arguments and results as tmps_nlist_build
- * minus the workspace: the scratch is one static device array built into the
- * library (about 6.6 MB, held by every GPU that loads the library until the
- * process exits), so it takes at most TMPS_NOALLOC_MAX_ATOMS atoms and
- * TMPS_NOALLOC_MAX_CELLS grid cells (the reference's own cell cap) and returns
- * TMPS_ERR_TOO_LARGE beyond that.  It calls no allocator.  The first call on
- * a device looks up the scratch's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture.  Every call shares the one
- * scratch (the counters are cleared at the start of each call): calls whose
- * work overlaps on the GPU -- other streams, other host threads -- race; order
- * them on one stream. */
+ * its own fixed arena, a host whose step loop must not enter the CUDA
+ * allocator (an allocation can synchronise the device and stall the loop),
+ * or a foreign-language host that can only pass the arrays it registered.
+ * Same arguments and results as tmps_nlist_build minus the workspace: the
+ * scratch is one static device array built into the library (about 6.6 MB,
+ * held by every GPU that loads the library until the process exits), so it
+ * takes at most TMPS_NOALLOC_MAX_ATOMS atoms and TMPS_NOALLOC_MAX_CELLS grid
+ * cells (the reference's own cell cap) and returns TMPS_ERR_TOO_LARGE beyond
+ * that.  It calls no allocator.  It has no room for the FP32 copy of the
+ * positions that lets tmps_nlist_build settle most candidate pairs in FP32,
+ * so every candidate goes to the exact FP64 test: the same pair set, more
+ * slowly.  The first call on a device looks up the scratch's device address
+ * (cudaGetSymbolAddress) and keeps it for the life of the process, so make
+ * that first call before any stream capture, and do not use the library
+ * across a cudaDeviceReset (the kept address belongs to the old context).
+ * Every call shares the one scratch (the counters are cleared at the start of
+ * each call): calls whose work overlaps on the GPU -- other streams, other
+ * host threads -- race; order them on one stream. */
 int tmps_nlist_build_noalloc(const tmps_atoms* src, const tmps_atoms* dst, const tmps_box* d_box,
                              int32_t ncell, double skin, const int32_t* cell_rank, int32_t* order,
                              int32_t* cell_of, const tmps_nlist* nl, int32_t* d_status, void* stream);

@@ -1,8 +1,8 @@
 """
 tmps_nlist_build_noalloc: the neighbor build for callers that cannot allocate
-device memory (a fixed device arena owned by the host, code running inside a
-CUDA graph capture, a foreign-language host that only passes registered
-arrays).  Its scratch is built into the library, so this checks, through the
+device memory (a fixed device arena owned by the host, a step loop that must
+not enter the CUDA allocator, a foreign-language host that only passes
+registered arrays).  Its scratch is built into the library, so this checks, through the
 C ABI, that it gives exactly what tmps_nlist_build gives with a caller-provided
 workspace, on two calls in a row (the second reuses the scratch the first
 left behind), and that it refuses sizes beyond its fixed limits.
