@@ -27,10 +27,29 @@ struct StyleTraits {
     static constexpr bool legacy_history = STYLE == STYLE_HOOKE_HISTORY || STYLE == STYLE_HERTZ_HISTORY;
 };
 
+// Division and square root of the law.  The FP64 form keeps IEEE-rounded
+// operations (its results follow the reference to 1e-12).  The mixed form's
+// law is FP32 arithmetic whose every operation already rounds at 2^-24, so
+// it uses the hardware's approximate reciprocal and reciprocal square root
+// (errors of a few ulp, the same order): a tenth of the instructions of the
+// IEEE sequences.
+template <typename T>
+TMPS_DEV T ldiv(T a, T b) { return a / b; }
+template <>
+TMPS_DEV float ldiv<float>(float a, float b) { return __fdividef(a, b); }
+template <typename T>
+TMPS_DEV T lsqrt(T a) { return sqrt(a); }
+template <>
+TMPS_DEV float lsqrt<float>(float a) {
+    // a * rsqrt(a); IEEE sqrtf for zero and for tiny arguments, whose reciprocal
+    // square root would overflow
+    return a >= 1e-30f ? a * rsqrtf(a) : sqrtf(a);
+}
+
 template <typename T>
 TMPS_DEV T dot3(const T* a, const T* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
 template <typename T>
-TMPS_DEV T norm3(const T* a) { return sqrt(dot3(a, a)); }
+TMPS_DEV T norm3(const T* a) { return lsqrt(dot3(a, a)); }
 template <typename T>
 TMPS_DEV void cross3(const T* a, const T* b, T* o) {
     o[0] = a[1] * b[2] - a[2] * b[1];
@@ -112,8 +131,29 @@ struct PairOut {
 // the overlap).  `sh` and `rl` (canonical sense) are read and written only by
 // history styles and by the rolling model; the caller passes zeros when the
 // slot held no live contact (the reference's partner != jtag reset).
-template <typename T, int STYLE, typename H = double>
-TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, const PairIn<T>& in,
+// The pair coefficients in FP32, for the mixed form's law: read from double
+// fields, every coefficient of every contact would be an FP64 -> FP32
+// conversion, which this part runs on its narrow FP64 pipe.  Same field names
+// as tmps_pair_params, so the law reads either.
+struct PairParams32 {
+    int32_t style, normal_id, damping_id, tangential_id, limit_damping, rolling_id;
+    float kn, kt, gamman, gammat, xmu, damp, xt, mu, k_roll, gamma_roll, mu_roll;
+};
+
+TMPS_DEV void params32(const tmps_pair_params& P, PairParams32& q) {
+    q.style = P.style;
+    q.normal_id = P.normal_id;
+    q.damping_id = P.damping_id;
+    q.tangential_id = P.tangential_id;
+    q.limit_damping = P.limit_damping;
+    q.rolling_id = P.rolling_id;
+    q.kn = (float)P.kn; q.kt = (float)P.kt; q.gamman = (float)P.gamman; q.gammat = (float)P.gammat;
+    q.xmu = (float)P.xmu; q.damp = (float)P.damp; q.xt = (float)P.xt; q.mu = (float)P.mu;
+    q.k_roll = (float)P.k_roll; q.gamma_roll = (float)P.gamma_roll; q.mu_roll = (float)P.mu_roll;
+}
+
+template <typename T, int STYLE, typename H = double, typename PP = tmps_pair_params>
+TMPS_DEV void contact_law(const PP& P, T dt, int shearupdate, const PairIn<T>& in,
                           H* sh, H* rl, PairOut<T>& out) {
     using HS = Hist<H>;
     using S = StyleTraits<STYLE>;
@@ -123,12 +163,12 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
         const T delta = in.delta;
         T polyhertz = T(1);
         if constexpr (S::hertz) {
-            const T reff = (in.ra * in.rb) / (in.ra + in.rb);
-            polyhertz = sqrt(reff * delta);
+            const T reff = ldiv(in.ra * in.rb, in.ra + in.rb);
+            polyhertz = lsqrt(reff * delta);
         }
-        const T meff = (in.ma * in.mb) / (in.ma + in.mb);
-        const T rsqinv = T(1) / in.rsq;
-        const T rinv = T(1) / r;
+        const T meff = ldiv(in.ma * in.mb, in.ma + in.mb);
+        const T rsqinv = ldiv(T(1), in.rsq);
+        const T rinv = ldiv(T(1), r);
         T vrel_t[3], vt[3], wr[3], cr[3], vtr[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) vrel_t[k] = in.va[k] - in.vb[k];
@@ -151,7 +191,7 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             const T fn = T(P.xmu) * fabs(ccel * r);
             const T fsd = (meff * T(P.gammat)) * vrel;
             T ft = T(0);
-            if (vrel > T(1e-16)) ft = (fn < fsd ? fn : fsd) / vrel;
+            if (vrel > T(1e-16)) ft = ldiv(fn < fsd ? fn : fsd, vrel);
 #pragma unroll
             for (int k = 0; k < 3; ++k) fs[k] = (-ft) * vtr[k];
         } else {
@@ -182,10 +222,10 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             const T fn = T(P.xmu) * fabs(ccel * r);
             if (fsmag > fn) {
                 if (shrmag != T(0)) {
-                    const T ratio = fn / fsmag;
+                    const T ratio = ldiv(fn, fsmag);
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        const T dc = (geff * vtr[k]) / T(P.kt);
+                        const T dc = ldiv(geff * vtr[k], T(P.kt));
                         HS::rescale(sh[k], ratio, dc);
                         fs[k] = ratio * fs[k];
                     }
@@ -204,14 +244,14 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
         out.arm_b = -in.rb;
     } else {
         const T r = in.r;
-        const T rinv = T(1) / r;
+        const T rinv = ldiv(T(1), r);
         T nv[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) nv[k] = in.d[k] * rinv;
         const T delta = in.delta;
-        const T reff = (in.ra * in.rb) / (in.ra + in.rb);
-        const T meff = (in.ma * in.mb) / (in.ma + in.mb);
-        const T a = sqrt(delta * reff);
+        const T reff = ldiv(in.ra * in.rb, in.ra + in.rb);
+        const T meff = ldiv(in.ma * in.mb, in.ma + in.mb);
+        const T a = lsqrt(delta * reff);
         T vr[3], vt[3], wr[3], cr[3], vtr[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) vr[k] = in.va[k] - in.vb[k];
@@ -234,10 +274,10 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             case 5: {
                 T arg = T(0);
                 if (delta > T(0)) {
-                    const T q = (meff * fne) / delta;
+                    const T q = ldiv(meff * fne, delta);
                     arg = q > T(0) ? q : T(0);
                 }
-                dpf = T(P.damp) * sqrt(arg);
+                dpf = T(P.damp) * lsqrt(arg);
                 break;
             }
             default: break;
@@ -251,7 +291,7 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             T ft = T(0);
             if (vrel != T(0)) {
                 const T q = damp_t * vrel;
-                ft = (fscrit < q ? fscrit : q) / vrel;
+                ft = ldiv(fscrit < q ? fscrit : q, vrel);
             }
 #pragma unroll
             for (int k = 0; k < 3; ++k) fs[k] = (-ft) * vtr[k];
@@ -272,7 +312,7 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
                     for (int k = 0; k < 3; ++k) o[k] = hf[k] - rsht * nv[k];
                     const T prjmag = norm3(o);
                     T scale = T(0);
-                    if (prjmag > T(0)) scale = shrmag / prjmag;
+                    if (prjmag > T(0)) scale = ldiv(shrmag, prjmag);
 #pragma unroll
                     for (int k = 0; k < 3; ++k) HS::set(sh[k], o[k] * scale);
                 }
@@ -290,11 +330,11 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             const T magfs = norm3(fs);
             if (magfs > fscrit) {
                 if (norm3(hf) != T(0)) {
-                    const T sc = fscrit / magfs;
+                    const T sc = ldiv(fscrit, magfs);
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         fs[k] = fs[k] * sc;
-                        HS::set(sh[k], (-(fs[k] - fdamp[k])) / keff);
+                        HS::set(sh[k], ldiv(-(fs[k] - fdamp[k]), keff));
                     }
                 } else {
                     fs[0] = fs[1] = fs[2] = T(0);
@@ -328,8 +368,8 @@ TMPS_DEV void contact_law(const tmps_pair_params& P, T dt, int shearupdate, cons
             if (tr_mag > tr_max && tr_mag > T(1e-12)) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    out.troll[k] = (-tr_max) * (h[k] / tr_mag);
-                    HS::set(rl[k], (tr_max / T(P.k_roll)) * (h[k] / tr_mag));
+                    out.troll[k] = (-tr_max) * ldiv(h[k], tr_mag);
+                    HS::set(rl[k], ldiv(tr_max, T(P.k_roll)) * ldiv(h[k], tr_mag));
                 }
             }
         }

@@ -212,8 +212,9 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
         const double d0 = __dsub_rn(x.x, __ldcs(a.x0 + i)), d1 = __dsub_rn(x.y, __ldcs(a.x0 + n + i)),
                      d2 = __dsub_rn(x.z, __ldcs(a.x0 + 2 * n + i));
         const double q = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
-        hit = hit || q > e->trigger_sq;
-        dd = fmaxf(dd, __double2float_ru(q));
+        // a non-finite displacement forces the rebuild, whose binning reports the position
+        hit = hit || !(q <= e->trigger_sq);
+        dd = q == q ? fmaxf(dd, __double2float_ru(q)) : __int_as_float(0x7fffffff);
         const double kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
                                (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
 #pragma unroll
@@ -306,8 +307,8 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
         const float d1 = ((p.y - __ldcs(a.o0_32 + n + i)) + pl.y) + (float)cell_y(c) * e->dh32[1] + e->dlo32[1];
         const float d2 = ((p.z - __ldcs(a.o0_32 + 2 * n + i)) + pl.z) + (float)cell_z(c) * e->dh32[2] + e->dlo32[2];
         const float q = (d0 * d0 + d1 * d1) + d2 * d2;
-        hit = hit || q > e->trigger32;
-        dd = fmaxf(dd, q);
+        hit = hit || !(q <= e->trigger32);  // NaN included (see a64_body)
+        dd = q == q ? fmaxf(dd, q) : __int_as_float(0x7fffffff);
         // kinetic term from the high words (vel32.w = m)
         const float kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
                               (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
@@ -511,24 +512,64 @@ __global__ void __launch_bounds__(256) k_gap_order(const uint64_t* __restrict__ 
 //     (triangle inequality; both running maxima only grow, so it has had no
 //     contact since the reference and its history is clear): its atoms are
 //     finished with no row read;
-//  2. screen: the atoms of up to kLive live groups whose own gap bound does
-//     not rule contact out are screened together, one per lane -- is any
-//     neighbor within reach of contact? (the contact test itself in FP64; a
-//     conservative FP32 version in the mixed form) -- reading their rows
-//     four entries (and partners) at a time.  Their ballot words are the
-//     group's new flag words; an atom not flagged gets its history cleared;
-//  3. contact: the flagged atoms, in group then atom order, in rounds of up
-//     to 32: the (atom, neighbor slot) entries of a round are laid across the
-//     lanes, 32 per pass, so a round costs the latency of one contact, not of
-//     its longest row.  Each atom's force, torque and virial are summed by the
-//     atom's own lane over its entries in slot order -- the order of a
-//     one-thread-per-atom loop.
+//  2. rosters: the atoms of up to kLive live groups whose own gap bound does
+//     not rule contact out, in group then atom order, 32 at a time.  A
+//     roster's state words go to shared memory (CfWarp), then
+//  3. near test: its (atom, slot) entries laid across the lanes, two passes
+//     of 32 at once -- is the partner within reach of contact? (the contact
+//     test itself in FP64; a conservative FP32 version in the mixed form).
+//     Near entries join a ring of queued contacts in shared memory;
+//  4. contact law: 32 queued contacts at a time, one per lane, so the law
+//     runs with full lanes however the contacts fall over the rows; each
+//     contact's force, torque and virial go to shared memory and the first
+//     lane of each atom's run of contacts adds them to the atom's sums in
+//     slot order -- the order of a one-thread-per-atom loop, whatever the
+//     batching (so culling changes no bit of a force);
+//  5. finish, one lane per roster atom: an atom with a near entry is flagged
+//     (its bit in the group's new flag word), gets Cundall damping, its force
+//     and torque written and its virial and kinetic terms summed; every
+//     roster atom's touch mask is rewritten if it changed (cleared when it
+//     has no near entry).
 // The flag words double as "force may be nonzero": an atom's force and
 // torque are written as zeros only when it was flagged the step before, so
 // every unflagged atom holds an exact zero, which A relies on to skip
 // loading them.  None of the skipping changes a result.  The per-block
 // virial partials depend only on the flag words, the group order and the
 // grid, not on scheduling; the kinetic term of an unflagged atom is A's.
+constexpr int kRing = 128;  // queued contacts per warp: < 32 waiting + 64 from one near-test step
+
+template <bool MIXED>
+struct CfWarp;
+
+// mixed form: FP32 state words; a queued entry keeps the partner's high
+// position word the near test loaded
+template <>
+struct CfWarp<true> {
+    float4 p[32], pl[32], v[32], w[32];  // pos32, pos32lo, vel32, om32 of the roster atoms
+    float4 red[3][32];                   // one contact per lane: f.xyz t.x | t.yz V0 V1 | V2..V5
+    float4 acc[3][32];                   // per roster atom, the same packing
+    float4 qp[kRing];                    // queued: partner pos32
+    uint64_t touch[32], ntouch[32];      // touch mask at entry / of this step's contacts
+    int32_t start[33], idx[32], cell[32], qe[kRing];
+    uint32_t near[32], qak[kRing];       // queued: roster atom | slot << 5
+};
+
+template <>
+struct CfWarp<false> {
+    double4 p[32], v[32], w[32];  // xr, vm, om of the roster atoms
+    double2 red[6][32];           // f.xy | f.z t.x | t.yz | V0 V1 | V2 V3 | V4 V5
+    double2 acc[6][32];
+    uint64_t touch[32], ntouch[32];
+    int32_t start[33], idx[32], qe[kRing];
+    uint32_t near[32], qak[kRing];
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
 template <int STYLE, bool MIXED>
 __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L, const tmps_pair_params& P,
                                         const tmps_box* __restrict__ B, tmps_engine* __restrict__ E,
@@ -537,10 +578,14 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                                         const float* __restrict__ sgap, double* __restrict__ part, const int bid,
                                         const int nblk) {
     using T = typename std::conditional<MIXED, float, double>::type;
+    // histories: doubles in the FP64 form, FP32 double words in the mixed form
+    using HT = typename std::conditional<MIXED, DW, double>::type;
     __shared__ double smem[6 * (kBlockC / 32)];
-    __shared__ uint8_t owner[kBlockC / 32][32];
-    __shared__ int32_t croster[kBlockC / 32][32];
     __shared__ uint32_t cwords[kBlockC / 32][kLive];
+    // the kLive groups of the batch in hand: group, old and near words (warp-uniform)
+    __shared__ int32_t bgrp[kBlockC / 32][kLive];
+    __shared__ uint32_t bold[kBlockC / 32][kLive], bnear[kBlockC / 32][kLive];
+    __shared__ CfWarp<MIXED> cwarp[kBlockC / 32];
     pdl_enter();
     if (E->aborted || E->step >= E->stop_step) return;
     const int64_t s = E->step + 1;
@@ -582,9 +627,24 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
         hrate[0] = (T)B->h_rate[0]; hrate[1] = (T)B->h_rate[1]; hrate[2] = (T)B->h_rate[2];
         hshear[0] = (T)B->h_rate[3]; hshear[1] = (T)B->h_rate[4]; hshear[2] = (T)B->h_rate[5];
     }
+    // mixed form: the 27 stencil offsets (ox, oy, oz) in {-1, 0, 1} times the
+    // cell edge, both words (exact products), by the code a list entry carries
+    __shared__ float4 soff[MIXED ? 27 : 1], sofl[MIXED ? 27 : 1];
+    __shared__ PairParams32 sP;  // the mixed law's coefficients, converted once per block
+    if constexpr (MIXED) {
+        if (threadIdx.x == 32) params32(P, sP);
+        if (threadIdx.x < 27) {
+            const int code = threadIdx.x;
+            const float ox = (float)(code % 3 - 1), oy = (float)((code / 3) % 3 - 1), oz = (float)(code / 9 - 1);
+            soff[code] = make_float4(ox * hh[0], oy * hh[1], oz * hh[2], 0.0f);
+            sofl[code] = make_float4(ox * hlo[0], oy * hlo[1], oz * hlo[2], 0.0f);
+        }
+        __syncthreads();
+    }
     double Vd[6] = {0, 0, 0, 0, 0, 0};
     float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};  // mixed: per-thread double words
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    CfWarp<MIXED>& W = cwarp[wib];
     const int ngroups = (n + 31) >> 5;
     const int nwarps = (nblk * blockDim.x) >> 5;
     const size_t ss = (size_t)L.slots * n;
@@ -597,373 +657,445 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
         const float md = sqrtf(__uint_as_float(E->maxd2_bits));
         thr = ((2.0f * md) * 1.0001f + E->shift_bound) + E->cull_tol;
     }
-    constexpr int kChunk = 4;  // row entries (and their partners) loaded at once
-    const int kfirst = L.slots < kChunk ? L.slots : kChunk;
-    // screen one atom: is any neighbor within reach of contact?
-    auto screen_atom = [&](int i) -> bool {
-        const int nn = L.nnb[i];
-        int e[kChunk];
-#pragma unroll
-        for (int u = 0; u < kChunk; ++u) e[u] = u < kfirst ? L.nbr[(size_t)u * n + i] : 0;
-        bool cand = false;
-        if constexpr (MIXED) {
-            const float4 pi = ld4f(A.pos32, i);
-            for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
-                if (k0 > 0) {
-#pragma unroll
-                    for (int u = 0; u < kChunk; ++u)
-                        if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
+
+    // 4. the contact law for `cnt` (<= 32) queued contacts from ring position
+    // qhead, one per lane, and their in-order reduction onto the roster atoms
+    auto law = [&](int cnt, int qhead) {
+        __syncwarp();
+        const bool live = lane < cnt;
+        const int slot = (qhead + lane) & (kRing - 1);
+        int a = 32 + lane, k = 0, e = 0;  // a >= 32: no roster atom (a run of its own)
+        if (live) {
+            const uint32_t ak = W.qak[slot];
+            a = (int)(ak & 31u);
+            k = (int)(ak >> 5);
+            e = W.qe[slot];
+        }
+        bool contact = false;
+        T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
+        if (live) {
+            const int ia = W.idx[a];
+            const int j = e & kNbrIndexMask;
+            const bool lo = ia < j;
+            const bool was = ((W.touch[a] >> k) & 1ull) != 0;
+            const size_t so = (size_t)k * n + ia;
+            // every load of the contact at once: one round trip
+            T xi[3], xj[3], ri, rj;
+            int32_t ci = 0, cj = 0;
+            float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
+            T vi[3], wi[3], mi, vj[3], wj[3], mj;
+            HT shr[3] = {}, rlr[3] = {};
+            if constexpr (MIXED) {
+                const float4 pi = W.p[a], pj = W.qp[slot];
+                il = W.pl[a];
+                jl = ld4f(A.pos32lo, j);
+                const float4 v = W.v[a], w = W.w[a];
+                const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
+                if (vremap) {
+                    ci = W.cell[a];
+                    cj = A.cell32[j];
                 }
-                float4 pj[kChunk];
+                xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+                xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+            } else {
+                const double4 pi = W.p[a], pj = ld4(A.xr, j);
+                const double4 v = W.v[a], w = W.w[a];
+                const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
+                xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+                xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+                vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+                wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+            }
+            if (hist && was) {
+                const HT* hs = reinterpret_cast<const HT*>(L.shear);
+                shr[0] = hs[so];
+                shr[1] = hs[ss + so];
+                shr[2] = hs[2 * ss + so];
+                if (roll) {
+                    const HT* hr = reinterpret_cast<const HT*>(L.rolling);
+                    rlr[0] = hr[so];
+                    rlr[1] = hr[ss + so];
+                    rlr[2] = hr[2 * ss + so];
+                }
+            }
+            // separation x_i - x_j
+            T d[3];
+            T nimg[3] = {0, 0, 0};
+            const int code = (unsigned)e >> kNbrIndexBits;
+            float offh[3] = {0.f, 0.f, 0.f}, offl[3] = {0.f, 0.f, 0.f};
+            if constexpr (MIXED) {
+                const float4 so = soff[code], sl = sofl[code];
+                offh[0] = so.x; offh[1] = so.y; offh[2] = so.z;
+                offl[0] = sl.x; offl[1] = sl.y; offl[2] = sl.z;
+                // offsets are relative to each atom's own cell: j's cell is
+                // the stencil offset (ox, oy, oz) away from i's, so
+                // x_i - x_j = (o_i - o_j) - offset * h
 #pragma unroll
-                for (int u = 0; u < kChunk; ++u)
-                    if (k0 + u < nn) pj[u] = ld4f(A.pos32, e[u] & kNbrIndexMask);
+                for (int c = 0; c < 3; ++c) {
+                    d[c] = (xi[c] - xj[c]) - offh[c];
+                    if (single[c]) {
+                        nimg[c] = rintf(d[c] * iprd[c]);
+                        d[c] -= nimg[c] * prd[c];
+                    }
+                }
+                if (vremap) {  // image count for the partner velocity shift
+                    const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+                    const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
+                                       cell_z(ci) + off[2] - cell_z(cj)};
 #pragma unroll
-                for (int u = 0; u < kChunk; ++u) {
-                    if (k0 + u < nn) {
-                        const int code = (unsigned)e[u] >> kNbrIndexBits;
-                        const float off[3] = {(float)(code % 3 - 1), (float)((code / 3) % 3 - 1),
-                                              (float)(code / 9 - 1)};
+                    for (int c = 0; c < 3; ++c)
+                        if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / gdim[c]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    d[c] = xi[c] - xj[c];
+                    if (per[c] == 1) {
+                        nimg[c] = rint(d[c] * iprd[c]);
+                        d[c] -= nimg[c] * prd[c];
+                    }
+                }
+            }
+            PairIn<T> in;
+            const T sg = lo ? T(1) : T(-1);
+            in.ra = lo ? ri : rj;
+            in.rb = lo ? rj : ri;
+            bool near;
+            if constexpr (MIXED) {
+                // separation, |d|^2, |d| and the overlap from the high and
+                // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
+                // FP32 difference of two unit-size numbers keeps 2^-24)
+                const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
+                float dh[3], dl[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float s1, e1, s2, e2;
+                    two_sum(xi[c], -xj[c], s1, e1);
+                    two_sum(s1, -offh[c], s2, e2);
+                    const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), offl[c]), __fadd_rn(e1, e2));
+                    two_sum(s2, low, dh[c], dl[c]);
+                    if (single[c]) {
+                        const float ni = rintf(dh[c] * iprd[c]);
+                        float s3, e3;
+                        two_sum(dh[c], -ni * prd[c], s3, e3);
+                        two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * prdlo[c]), e3), dh[c], dl[c]);
+                    }
+                    dh[c] = sg * dh[c];
+                    dl[c] = sg * dl[c];
+                }
+                // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
+                float pp[3], pe[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    pp[c] = __fmul_rn(dh[c], dh[c]);
+                    pe[c] = __fmaf_rn(dh[c], dh[c], -pp[c]);
+                }
+                float t1, te1, rh, re;
+                two_sum(pp[0], pp[1], t1, te1);
+                two_sum(t1, pp[2], rh, re);
+                const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]),
+                                                                        __fmul_rn(dh[1], dl[1])),
+                                                             __fmul_rn(dh[2], dl[2])));
+                const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])),
+                                            cross);
+                float rsh, rsl;
+                two_sum(rh, rl0, rsh, rsl);
+                // r_hi need not be the rounded root: the residual rsh - r_hi^2 (one FMA,
+                // within an ulp of exact for an r_hi a few ulp off) corrects it in r_lo
+                const float r_hi = lsqrt(rsh);
+                const float res = __fmaf_rn(-r_hi, r_hi, rsh);
+                const float r_lo = __fdividef(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
+                // ra + rb, both words
+                const float4 al = lo ? il : jl, bl = lo ? jl : il;
+                float sh_, se_;
+                two_sum(in.ra, in.rb, sh_, se_);
+                const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
+                const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
+                near = delta > 0.0f && rsh > 1e-28f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
+                in.rsq = rsh;
+                in.r = r_hi;
+                in.delta = delta;
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
+                in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
+                const T radsum = in.ra + in.rb;
+                near = in.rsq < radsum * radsum && in.rsq > T(1e-28);
+                if (near) {
+                    in.r = sqrt(in.rsq);
+                    in.delta = radsum - in.r;
+                }
+            }
+            if (near) {
+                contact = true;
+                T dv[3] = {0, 0, 0};
+                if (vremap) {
+                    // image count of x_a - x_b, then n . h_rate for partner b
+                    T na[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
+                    dv[0] = (na[0] * hrate[0] + na[1] * hshear[2]) + na[2] * hshear[1];
+                    dv[1] = na[1] * hrate[1] + na[2] * hshear[0];
+                    dv[2] = na[2] * hrate[2];
+                }
+                in.ma = lo ? mi : mj;
+                in.mb = lo ? mj : mi;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    in.va[c] = lo ? vi[c] : vj[c];
+                    in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
+                    in.wa[c] = lo ? wi[c] : wj[c];
+                    in.wb[c] = lo ? wj[c] : wi[c];
+                }
+                HT sh[3] = {}, rl[3] = {};
+                if (hist && was) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        sh[c] = hsign(shr[c], lo);
+                        rl[c] = hsign(rlr[c], lo);
+                    }
+                }
+                PairOut<T> out;
+                if constexpr (MIXED) contact_law<T, STYLE>(sP, dt, 1, in, sh, rl, out);
+                else contact_law<T, STYLE>(P, dt, 1, in, sh, rl, out);
+                if (hist) {
+                    HT* hs = reinterpret_cast<HT*>(L.shear);
+                    hs[so] = hsign(sh[0], lo);
+                    hs[ss + so] = hsign(sh[1], lo);
+                    hs[2 * ss + so] = hsign(sh[2], lo);
+                    if (roll) {
+                        HT* hr = reinterpret_cast<HT*>(L.rolling);
+                        hr[so] = hsign(rl[0], lo);
+                        hr[ss + so] = hsign(rl[1], lo);
+                        hr[2 * ss + so] = hsign(rl[2], lo);
+                    }
+                }
+                const T arm = lo ? out.arm_a : out.arm_b;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    fc[c] = sg * out.f[c];
+                    tc[c] = arm * out.tor[c] + sg * out.troll[c];
+                }
+                vc[0] = T(0.5) * (in.d[0] * out.f[0]);
+                vc[1] = T(0.5) * (in.d[1] * out.f[1]);
+                vc[2] = T(0.5) * (in.d[2] * out.f[2]);
+                vc[3] = T(0.5) * (in.d[0] * out.f[1]);
+                vc[4] = T(0.5) * (in.d[0] * out.f[2]);
+                vc[5] = T(0.5) * (in.d[1] * out.f[2]);
+            }
+        }
+        if (contact) atomicOr(reinterpret_cast<unsigned long long*>(&W.ntouch[a]), 1ull << k);
+        if constexpr (MIXED) {
+            W.red[0][lane] = make_float4(fc[0], fc[1], fc[2], tc[0]);
+            W.red[1][lane] = make_float4(tc[1], tc[2], vc[0], vc[1]);
+            W.red[2][lane] = make_float4(vc[2], vc[3], vc[4], vc[5]);
+        } else {
+            W.red[0][lane] = make_double2(fc[0], fc[1]);
+            W.red[1][lane] = make_double2(fc[2], tc[0]);
+            W.red[2][lane] = make_double2(tc[1], tc[2]);
+            W.red[3][lane] = make_double2(vc[0], vc[1]);
+            W.red[4][lane] = make_double2(vc[2], vc[3]);
+            W.red[5][lane] = make_double2(vc[4], vc[5]);
+        }
+        // each roster atom's contacts form one run of lanes; its first lane
+        // adds them to the atom's sums in slot order
+        const int ap = __shfl_up_sync(0xffffffffu, a, 1), an = __shfl_down_sync(0xffffffffu, a, 1);
+        const uint32_t ends = __ballot_sync(0xffffffffu, lane == 31 || an != a);
+        __syncwarp();
+        if (live && (lane == 0 || ap != a)) {
+            const int last = __ffs(ends & ~lanemask_lt()) - 1;
+            if constexpr (MIXED) {
+                float4 s0 = W.acc[0][a], s1 = W.acc[1][a], s2 = W.acc[2][a];
+                for (int t = lane; t <= last; ++t) {
+                    const float4 r0 = W.red[0][t], r1 = W.red[1][t], r2 = W.red[2][t];
+                    s0.x += r0.x; s0.y += r0.y; s0.z += r0.z; s0.w += r0.w;
+                    s1.x += r1.x; s1.y += r1.y; s1.z += r1.z; s1.w += r1.w;
+                    s2.x += r2.x; s2.y += r2.y; s2.z += r2.z; s2.w += r2.w;
+                }
+                W.acc[0][a] = s0; W.acc[1][a] = s1; W.acc[2][a] = s2;
+            } else {
+                double2 sacc[6];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) sacc[c] = W.acc[c][a];
+                for (int t = lane; t <= last; ++t) {
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) {
+                        const double2 r = W.red[c][t];
+                        sacc[c].x += r.x;
+                        sacc[c].y += r.y;
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 6; ++c) W.acc[c][a] = sacc[c];
+            }
+        }
+        __syncwarp();
+    };
+
+    // 2-5: one roster of `count` atoms; this lane's atom is i (group word uq, bit)
+    auto roster = [&](int count, int i, int uq, int bit) {
+        __syncwarp();
+        const bool mine = lane < count;
+        const int nn = mine ? L.nnb[i] : 0;
+        const uint64_t touch = (hist && mine) ? L.touch[i] : 0ull;
+        if (mine) {
+            if constexpr (MIXED) {
+                W.p[lane] = ld4f(A.pos32, i);
+                W.pl[lane] = ld4f(A.pos32lo, i);
+                W.v[lane] = ld4f(A.vel32, i);
+                W.w[lane] = ld4f(A.om32, i);
+                if (vremap) W.cell[lane] = A.cell32[i];
+            } else {
+                W.p[lane] = ld4(A.xr, i);
+                W.v[lane] = ld4(A.vm, i);
+                W.w[lane] = ld4(A.om, i);
+            }
+        }
+        W.idx[lane] = i;
+        W.touch[lane] = touch;
+        W.ntouch[lane] = 0ull;
+        W.near[lane] = 0u;
+        if constexpr (MIXED) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) W.acc[c][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) W.acc[c][lane] = make_double2(0.0, 0.0);
+        }
+        int incl = nn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        W.start[lane] = incl - nn;  // atoms past `count` start at `total`: the search never picks them
+        if (lane == 0) W.start[32] = total;
+        __syncwarp();
+        int qhead = 0, qtail = 0, p0 = 0;  // ring positions and next entry (warp-uniform)
+        while (true) {
+            const int pending = qtail - qhead;
+            if (pending >= 32 || (p0 >= total && pending > 0)) {
+                const int cnt = pending < 32 ? pending : 32;
+                law(cnt, qhead);
+                qhead += cnt;
+                continue;
+            }
+            if (p0 >= total) break;
+            // 3. near test of entries p0 .. p0 + 63, two per lane, all loads in flight together
+            int ea[2], aa[2], ka[2];
+            bool va[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int idx = p0 + 32 * u + lane;
+                va[u] = idx < total;
+                int a = 0;
+                if (va[u]) {
+#pragma unroll
+                    for (int st = 16; st > 0; st >>= 1)
+                        if (W.start[a + st] <= idx) a += st;
+                }
+                aa[u] = a;
+                ka[u] = idx - W.start[a];
+                ea[u] = va[u] ? L.nbr[(size_t)ka[u] * n + W.idx[a]] : 0;
+            }
+            p0 += 64;
+            if constexpr (MIXED) {
+                float4 pj[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+                    if (va[u]) pj[u] = ld4f(A.pos32, ea[u] & kNbrIndexMask);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    bool nr = false;
+                    if (va[u]) {
+                        const float4 pi = W.p[aa[u]];
+                        const float4 so = soff[(unsigned)ea[u] >> kNbrIndexBits];
                         const float xi[3] = {pi.x, pi.y, pi.z}, xj[3] = {pj[u].x, pj[u].y, pj[u].z};
+                        const float oh[3] = {so.x, so.y, so.z};
                         float d[3];
 #pragma unroll
                         for (int c = 0; c < 3; ++c) {
-                            d[c] = (xi[c] - xj[c]) - off[c] * hh[c];
+                            d[c] = (xi[c] - xj[c]) - oh[c];
                             if (single[c]) d[c] -= rintf(d[c] * iprd[c]) * prd[c];
                         }
                         const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
                         const float rs = (pi.w + pj[u].w) * 1.00001f;
-                        cand = cand || rq < rs * rs;
+                        nr = rq < rs * rs;
                     }
+                    const uint32_t bal = __ballot_sync(0xffffffffu, nr);
+                    if (nr) {
+                        const int q = (qtail + __popc(bal & lanemask_lt())) & (kRing - 1);
+                        W.qe[q] = ea[u];
+                        W.qak[q] = (uint32_t)aa[u] | ((uint32_t)ka[u] << 5);
+                        W.qp[q] = pj[u];
+                        W.near[aa[u]] = 1u;
+                    }
+                    qtail += __popc(bal);
                 }
-            }
-        } else {
-            const double4 pi = ld4(A.xr, i);
-            for (int k0 = 0; k0 < nn && !cand; k0 += kChunk) {
-                if (k0 > 0) {
+            } else {
+                double4 pj[2];
 #pragma unroll
-                    for (int u = 0; u < kChunk; ++u)
-                        if (k0 + u < nn) e[u] = L.nbr[(size_t)(k0 + u) * n + i];
-                }
-                double4 pj[kChunk];
+                for (int u = 0; u < 2; ++u)
+                    if (va[u]) pj[u] = ld4(A.xr, ea[u] & kNbrIndexMask);
 #pragma unroll
-                for (int u = 0; u < kChunk; ++u)
-                    if (k0 + u < nn) pj[u] = ld4(A.xr, e[u] & kNbrIndexMask);
-#pragma unroll
-                for (int u = 0; u < kChunk; ++u) {
-                    if (k0 + u < nn) {
+                for (int u = 0; u < 2; ++u) {
+                    bool nr = false;
+                    if (va[u]) {
+                        const double4 pi = W.p[aa[u]];
                         double d[3] = {pi.x - pj[u].x, pi.y - pj[u].y, pi.z - pj[u].z};
 #pragma unroll
                         for (int c = 0; c < 3; ++c)
                             if (per[c] == 1) d[c] -= rint(d[c] * iprd[c]) * prd[c];
                         const double rsq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
                         const double radsum = pi.w + pj[u].w;
-                        cand = cand || (rsq < radsum * radsum && rsq > 1e-28);
+                        nr = rsq < radsum * radsum && rsq > 1e-28;
                     }
+                    const uint32_t bal = __ballot_sync(0xffffffffu, nr);
+                    if (nr) {
+                        const int q = (qtail + __popc(bal & lanemask_lt())) & (kRing - 1);
+                        W.qe[q] = ea[u];
+                        W.qak[q] = (uint32_t)aa[u] | ((uint32_t)ka[u] << 5);
+                        W.near[aa[u]] = 1u;
+                    }
+                    qtail += __popc(bal);
                 }
             }
+            __syncwarp();
         }
-        return cand;
-    };
-    // contact forces of the `count` atoms in croster[wib]
-    auto contact_round = [&](int count) {
-        const bool mine = lane < count;
-        const int i = mine ? croster[wib][lane] : 0;
+        // 5. finish the roster atoms
         __syncwarp();
-            const int nn = mine ? L.nnb[i] : 0;
-            const uint64_t touch = (hist && mine) ? L.touch[i] : 0ull;
-            // the row atom's own velocities (Cundall, kinetic term), issued with its row length
-            T rv[3] = {0, 0, 0}, rw[3] = {0, 0, 0}, rm = 0;
-            if (mine) {
+        if (mine) {
+            const uint64_t nt = W.ntouch[lane];
+            if (hist && nt != touch) L.touch[i] = nt;
+            if (W.near[lane]) {
+                atomicOr(&cwords[wib][uq], 1u << bit);
+                T F[3], Tq[3], V[6], vi[3], wi[3], mi;
                 if constexpr (MIXED) {
-                    const float4 v = ld4f(A.vel32, i), w = ld4f(A.om32, i);
-                    rv[0] = v.x; rv[1] = v.y; rv[2] = v.z; rm = v.w;
-                    rw[0] = w.x; rw[1] = w.y; rw[2] = w.z;
+                    const float4 s0 = W.acc[0][lane], s1 = W.acc[1][lane], s2 = W.acc[2][lane];
+                    F[0] = s0.x; F[1] = s0.y; F[2] = s0.z; Tq[0] = s0.w;
+                    Tq[1] = s1.x; Tq[2] = s1.y; V[0] = s1.z; V[1] = s1.w;
+                    V[2] = s2.x; V[3] = s2.y; V[4] = s2.z; V[5] = s2.w;
+                    const float4 v = W.v[lane], w = W.w[lane];
+                    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                    wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
                 } else {
-                    const double4 v = ld4(A.vm, i), w = ld4(A.om, i);
-                    rv[0] = v.x; rv[1] = v.y; rv[2] = v.z; rm = v.w;
-                    rw[0] = w.x; rw[1] = w.y; rw[2] = w.z;
+                    const double2 s0 = W.acc[0][lane], s1 = W.acc[1][lane], s2 = W.acc[2][lane],
+                                  s3 = W.acc[3][lane], s4 = W.acc[4][lane], s5 = W.acc[5][lane];
+                    F[0] = s0.x; F[1] = s0.y; F[2] = s1.x; Tq[0] = s1.y; Tq[1] = s2.x; Tq[2] = s2.y;
+                    V[0] = s3.x; V[1] = s3.y; V[2] = s4.x; V[3] = s4.y; V[4] = s5.x; V[5] = s5.y;
+                    const double4 v = W.v[lane], w = W.w[lane];
+                    vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+                    wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
                 }
-            }
-            int incl = nn;
-    #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            const int start = incl - nn;
-            const int total = __shfl_sync(0xffffffffu, incl, 31);
-            T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
-            uint64_t newtouch = 0ull;
-            for (int p0 = 0; p0 < total; p0 += 32) {
-                if (mine) {
-                    const int k0 = max(start, p0), k1 = min(start + nn, p0 + 32);
-                    for (int k = k0; k < k1; ++k) owner[wib][k - p0] = (uint8_t)lane;
-                }
-                __syncwarp();
-                const bool live = p0 + lane < total;
-                const int ol = live ? owner[wib][lane] : 0;
-                const int ost = __shfl_sync(0xffffffffu, start, ol);
-                const int ia = __shfl_sync(0xffffffffu, i, ol);  // the entry's row atom
-                const uint32_t tlo = __shfl_sync(0xffffffffu, (uint32_t)touch, ol);
-                const uint32_t thi = __shfl_sync(0xffffffffu, (uint32_t)(touch >> 32), ol);
-                bool contact = false;
-                T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
-                if (live) {
-                    const int k = p0 + lane - ost;      // the entry's slot in its row
-                    const int e = L.nbr[(size_t)k * n + ia];
-                    const int j = e & kNbrIndexMask;
-                    const bool lo = ia < j;
-                    const bool was = k < 32 ? ((tlo >> k) & 1u) : ((thi >> (k - 32)) & 1u);
-                    const size_t so = (size_t)k * n + ia;
-                    // every load of the entry at once, whether or not it turns out to touch:
-                    // one round trip after the row entry instead of three
-                    T xi[3], xj[3], ri, rj;
-                    int32_t ci = 0, cj = 0;
-                    float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
-                    T vi[3], wi[3], mi, vj[3], wj[3], mj;
-                    // histories: doubles in the FP64 form, FP32 double words in the mixed form
-                    using HT = typename std::conditional<MIXED, DW, double>::type;
-                    HT shr[3] = {}, rlr[3] = {};
-                    if constexpr (MIXED) {
-                        const float4 pi = ld4f(A.pos32, ia), pj = ld4f(A.pos32, j);
-                        il = ld4f(A.pos32lo, ia);
-                        jl = ld4f(A.pos32lo, j);
-                        const float4 v = ld4f(A.vel32, ia), w = ld4f(A.om32, ia);
-                        const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
-                        if (vremap) {
-                            ci = A.cell32[ia];
-                            cj = A.cell32[j];
-                        }
-                        xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
-                        xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
-                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-                    } else {
-                        const double4 pi = ld4(A.xr, ia), pj = ld4(A.xr, j);
-                        const double4 v = ld4(A.vm, ia), w = ld4(A.om, ia);
-                        const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
-                        xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
-                        xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
-                        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                        wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                        vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                        wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-                    }
-                    if (hist && was) {
-                        const HT* hs = reinterpret_cast<const HT*>(L.shear);
-                        shr[0] = hs[so];
-                        shr[1] = hs[ss + so];
-                        shr[2] = hs[2 * ss + so];
-                        if (roll) {
-                            const HT* hr = reinterpret_cast<const HT*>(L.rolling);
-                            rlr[0] = hr[so];
-                            rlr[1] = hr[ss + so];
-                            rlr[2] = hr[2 * ss + so];
-                        }
-                    }
-                    // separation x_i - x_j
-                    T d[3];
-                    T nimg[3] = {0, 0, 0};
-                    const int code = (unsigned)e >> kNbrIndexBits;
-                    const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
-                    if constexpr (MIXED) {
-                        // offsets are relative to each atom's own cell: j's cell is
-                        // the stencil offset (ox, oy, oz) away from i's, so
-                        // x_i - x_j = (o_i - o_j) - offset * h
-    #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            d[c] = (xi[c] - xj[c]) - (float)off[c] * hh[c];
-                            if (single[c]) {
-                                nimg[c] = rintf(d[c] * iprd[c]);
-                                d[c] -= nimg[c] * prd[c];
-                            }
-                        }
-                        if (vremap) {  // image count for the partner velocity shift
-                            const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
-                                               cell_z(ci) + off[2] - cell_z(cj)};
-    #pragma unroll
-                            for (int c = 0; c < 3; ++c)
-                                if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / gdim[c]);
-                        }
-                    } else {
-    #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            d[c] = xi[c] - xj[c];
-                            if (per[c] == 1) {
-                                nimg[c] = rint(d[c] * iprd[c]);
-                                d[c] -= nimg[c] * prd[c];
-                            }
-                        }
-                    }
-                    PairIn<T> in;
-                    const T sg = lo ? T(1) : T(-1);
-                    in.ra = lo ? ri : rj;
-                    in.rb = lo ? rj : ri;
-                    bool near;
-                    if constexpr (MIXED) {
-                        // FP32 screen, with room for the FP32 rounding of the words
-                        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-                        const float rs = (ri + rj) * 1.00001f;
-                        near = rq < rs * rs;
-                        if (near) {
-                            // separation, |d|^2, |d| and the overlap from the high and
-                            // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
-                            // FP32 difference of two unit-size numbers keeps 2^-24)
-                            const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
-                            float dh[3], dl[3];
-    #pragma unroll
-                            for (int c = 0; c < 3; ++c) {
-                                float s1, e1, s2, e2;
-                                two_sum(xi[c], -xj[c], s1, e1);
-                                two_sum(s1, -(float)off[c] * hh[c], s2, e2);
-                                const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), (float)off[c] * hlo[c]),
-                                                            __fadd_rn(e1, e2));
-                                two_sum(s2, low, dh[c], dl[c]);
-                                if (single[c]) {
-                                    const float ni = rintf(dh[c] * iprd[c]);
-                                    float s3, e3;
-                                    two_sum(dh[c], -ni * prd[c], s3, e3);
-                                    two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * prdlo[c]), e3), dh[c], dl[c]);
-                                }
-                                dh[c] = sg * dh[c];
-                                dl[c] = sg * dl[c];
-                            }
-                            // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
-                            float pp[3], pe[3];
-    #pragma unroll
-                            for (int c = 0; c < 3; ++c) {
-                                pp[c] = __fmul_rn(dh[c], dh[c]);
-                                pe[c] = __fmaf_rn(dh[c], dh[c], -pp[c]);
-                            }
-                            float t1, te1, rh, re;
-                            two_sum(pp[0], pp[1], t1, te1);
-                            two_sum(t1, pp[2], rh, re);
-                            const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]),
-                                                                                    __fmul_rn(dh[1], dl[1])),
-                                                                         __fmul_rn(dh[2], dl[2])));
-                            const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])),
-                                                        cross);
-                            float rsh, rsl;
-                            two_sum(rh, rl0, rsh, rsl);
-                            const float r_hi = __fsqrt_rn(rsh);
-                            const float res = __fmaf_rn(-r_hi, r_hi, rsh);  // exact
-                            const float r_lo = __fdiv_rn(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
-                            // ra + rb, both words
-                            const float4 al = lo ? il : jl, bl = lo ? jl : il;
-                            float sh_, se_;
-                            two_sum(in.ra, in.rb, sh_, se_);
-                            const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
-                            const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
-                            near = delta > 0.0f && rsh > 1e-28f;
-    #pragma unroll
-                            for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
-                            in.rsq = rsh;
-                            in.r = r_hi;
-                            in.delta = delta;
-                        }
-                    } else {
-    #pragma unroll
-                        for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
-                        in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
-                        const T radsum = in.ra + in.rb;
-                        near = in.rsq < radsum * radsum && in.rsq > T(1e-28);
-                        if (near) {
-                            in.r = sqrt(in.rsq);
-                            in.delta = radsum - in.r;
-                        }
-                    }
-                    if (near) {
-                        contact = true;
-                        T dv[3] = {0, 0, 0};
-                        if (vremap) {
-                            // image count of x_a - x_b, then n . h_rate for partner b
-                            T na[3];
-    #pragma unroll
-                            for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
-                            dv[0] = (na[0] * hrate[0] + na[1] * hshear[2]) + na[2] * hshear[1];
-                            dv[1] = na[1] * hrate[1] + na[2] * hshear[0];
-                            dv[2] = na[2] * hrate[2];
-                        }
-                        in.ma = lo ? mi : mj;
-                        in.mb = lo ? mj : mi;
-    #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            in.va[c] = lo ? vi[c] : vj[c];
-                            in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
-                            in.wa[c] = lo ? wi[c] : wj[c];
-                            in.wb[c] = lo ? wj[c] : wi[c];
-                        }
-                        HT sh[3] = {}, rl[3] = {};
-                        if (hist && was) {
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) {
-                                sh[c] = hsign(shr[c], lo);
-                                rl[c] = hsign(rlr[c], lo);
-                            }
-                        }
-                        PairOut<T> out;
-                        contact_law<T, STYLE>(P, dt, 1, in, sh, rl, out);
-                        if (hist) {
-                            HT* hs = reinterpret_cast<HT*>(L.shear);
-                            hs[so] = hsign(sh[0], lo);
-                            hs[ss + so] = hsign(sh[1], lo);
-                            hs[2 * ss + so] = hsign(sh[2], lo);
-                            if (roll) {
-                                HT* hr = reinterpret_cast<HT*>(L.rolling);
-                                hr[so] = hsign(rl[0], lo);
-                                hr[ss + so] = hsign(rl[1], lo);
-                                hr[2 * ss + so] = hsign(rl[2], lo);
-                            }
-                        }
-                        const T arm = lo ? out.arm_a : out.arm_b;
-    #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            fc[c] = sg * out.f[c];
-                            tc[c] = arm * out.tor[c] + sg * out.troll[c];
-                        }
-                        vc[0] = T(0.5) * (in.d[0] * out.f[0]);
-                        vc[1] = T(0.5) * (in.d[1] * out.f[1]);
-                        vc[2] = T(0.5) * (in.d[2] * out.f[2]);
-                        vc[3] = T(0.5) * (in.d[0] * out.f[1]);
-                        vc[4] = T(0.5) * (in.d[0] * out.f[2]);
-                        vc[5] = T(0.5) * (in.d[1] * out.f[2]);
-                    }
-                }
-                // each row atom's lane takes its contacts in slot order
-                uint32_t cm = __ballot_sync(0xffffffffu, contact);
-                while (cm) {
-                    const int q = __ffs(cm) - 1;
-                    cm &= cm - 1;
-                    const int oq = owner[wib][q];
-                    T gf[3], gt[3], gv[6];
-    #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        gf[c] = __shfl_sync(0xffffffffu, fc[c], q);
-                        gt[c] = __shfl_sync(0xffffffffu, tc[c], q);
-                    }
-    #pragma unroll
-                    for (int c = 0; c < 6; ++c) gv[c] = __shfl_sync(0xffffffffu, vc[c], q);
-                    if (lane == oq) {
-    #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            F[c] += gf[c];
-                            Tq[c] += gt[c];
-                        }
-    #pragma unroll
-                        for (int c = 0; c < 6; ++c) V[c] += gv[c];
-                        newtouch |= 1ull << (p0 + q - start);
-                    }
-                }
-                __syncwarp();
-            }
-            if (mine) {
-                if (hist && newtouch != touch) L.touch[i] = newtouch;
-                const T* vi = rv;
-                const T* wi = rw;
-                const T mi = rm;
                 if (E->cundall) {  // FixDampingCundall.post_force_kernel
                     T gl, ga;
                     if constexpr (MIXED) {
@@ -973,7 +1105,7 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                         gl = E->gamma_lin;
                         ga = E->gamma_ang;
                     }
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         const T sf = F[c] * vi[c] >= T(0) ? T(1) : T(-1);
                         F[c] *= T(1) - gl * sf;
@@ -982,13 +1114,13 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                     }
                 }
                 if constexpr (MIXED) {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         A.f32[c * n + i] = F[c];
                         A.torque32[c * n + i] = Tq[c];
                     }
                 } else {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         A.f[c * n + i] = F[c];
                         A.torque[c * n + i] = Tq[c];
@@ -1000,29 +1132,29 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                 // (the same products from the same words, so a zero force adds an
                 // exact zero)
                 T im;
-                if constexpr (MIXED) im = 1.0f / mi;
+                if constexpr (MIXED) im = __fdividef(1.0f, mi);
                 else im = A.rinv[i];
                 const T hdt = T(0.5) * dt;
                 T vf[3];
-    #pragma unroll
+#pragma unroll
                 for (int c = 0; c < 3; ++c) vf[c] = vi[c] + hdt * (F[c] * im);
                 const T kin[6] = {(mi * vf[0]) * vf[0], (mi * vf[1]) * vf[1], (mi * vf[2]) * vf[2],
                                   (mi * vf[0]) * vf[1], (mi * vf[0]) * vf[2], (mi * vf[1]) * vf[2]};
                 const T kh[6] = {(mi * vi[0]) * vi[0], (mi * vi[1]) * vi[1], (mi * vi[2]) * vi[2],
                                  (mi * vi[0]) * vi[1], (mi * vi[0]) * vi[2], (mi * vi[1]) * vi[2]};
                 if constexpr (MIXED) {
-    #pragma unroll
-                    for (int c = 0; c < 6; ++c) {
-                        dw_add(Vh[c], Vl[c], V[c]);
-                        dw_add(Vh[c], Vl[c], kin[c]);
-                        dw_add(Vh[c], Vl[c], -kh[c]);
-                    }
+                    // kin - kh is exact where the force changed v little (Sterbenz); elsewhere
+                    // kh is the smaller term and the difference rounds once, as kin did
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) dw_add(Vh[c], Vl[c], V[c] + (kin[c] - kh[c]));
                 } else {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 6; ++c) Vd[c] += (V[c] + kin[c]) - kh[c];
                 }
             }
+        }
     };
+
     if (lane < kLive) cwords[wib][lane] = 0u;
     __syncwarp();
     // Ordered pass: after the first pass that follows the bounds (which
@@ -1032,7 +1164,6 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
     // the ascending gap order.  Walking that order instead of the group
     // index gives every warp the same number of live groups (+-1).
     const bool ordered = cull && E->order_ready != 0;
-    int ncand = 0;  // atoms waiting in croster (warp-uniform)
     for (int base = gw; base < ngroups; base += 32 * nwarps) {
         const int k = base + lane * nwarps;
         int mygrp = k;
@@ -1087,55 +1218,49 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                 nw[u] = __ballot_sync(0xffffffffu, u < nq && i < n && !(cull && ag[u] > thr));
                 near_total += __popc(nw[u]);
             }
-            // screen the near atoms, 32 at a time, in group then atom order
+            // park the batch in shared memory while its rosters run (registers go to the law)
+            if (lane < kLive) {
+#pragma unroll
+                for (int u = 0; u < kLive; ++u) {
+                    if (u == lane) {
+                        bgrp[wib][u] = gq[u];
+                        bold[wib][u] = oq[u];
+                        bnear[wib][u] = nw[u];
+                    }
+                }
+            }
+            __syncwarp();
+            // the near atoms, 32 at a time, in group then atom order: one roster each
             for (int r0 = 0; r0 < near_total; r0 += 32) {
                 const int idx = r0 + lane;
                 int uq = -1, bit = 0, acc = 0, g = 0;
-#pragma unroll
-                for (int u = 0; u < kLive; ++u) {
-                    const int c = __popc(nw[u]);
+                for (int u = 0; u < nq; ++u) {
+                    const uint32_t w = bnear[wib][u];
+                    const int c = __popc(w);
                     if (uq < 0 && idx < acc + c) {
                         uq = u;
-                        bit = nth_bit(nw[u], idx - acc);
-                        g = gq[u];
+                        bit = nth_bit(w, idx - acc);
+                        g = bgrp[wib][u];
                     }
                     acc += c;
                 }
-                bool cand = false;
-                int i = 0;
-                if (uq >= 0) {
-                    i = (g << 5) + bit;
-                    cand = screen_atom(i);
-                    if (cand) atomicOr(&cwords[wib][uq], 1u << bit);
-                    else if (hist && L.touch[i] != 0ull) L.touch[i] = 0ull;
-                }
-                // flagged atoms join the contact roster
-                const uint32_t cm = __ballot_sync(0xffffffffu, cand);
-                if (ncand + __popc(cm) > 32) {
-                    contact_round(ncand);
-                    ncand = 0;
-                }
-                if (cand) croster[wib][ncand + __popc(cm & ((1u << lane) - 1u))] = i;
-                ncand += __popc(cm);
-                __syncwarp();
+                const int count = near_total - r0 < 32 ? near_total - r0 : 32;
+                roster(count, uq >= 0 ? (g << 5) + bit : 0, uq < 0 ? 0 : uq, bit);
             }
             __syncwarp();
             // new flag words; stale forces of atoms no longer flagged
-#pragma unroll
-            for (int u = 0; u < kLive; ++u) {
-                if (u < nq) {
-                    const uint32_t w = cwords[wib][u];
-                    const int i = (gq[u] << 5) + lane;
-                    if (lane == 0 && w != oq[u]) flags[gq[u]] = w;
-                    if (i < n && ((oq[u] >> lane) & 1u) && !((w >> lane) & 1u)) zero_force<MIXED>(A, i);
-                }
+            for (int u = 0; u < nq; ++u) {
+                const uint32_t w = cwords[wib][u], old = bold[wib][u];
+                const int g = bgrp[wib][u];
+                const int i = (g << 5) + lane;
+                if (lane == 0 && w != old) flags[g] = w;
+                if (i < n && ((old >> lane) & 1u) && !((w >> lane) & 1u)) zero_force<MIXED>(A, i);
             }
             __syncwarp();
             if (lane < kLive) cwords[wib][lane] = 0u;
             __syncwarp();
         }
     }
-    if (ncand > 0) contact_round(ncand);
     if constexpr (MIXED) {
         block_sum_dw<6, kBlockC>(Vh, Vl, reinterpret_cast<float2*>(smem));
         if (threadIdx.x == 0) {
@@ -1153,7 +1278,7 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
 }
 
 template <int STYLE, bool MIXED>
-__global__ void __launch_bounds__(kBlockC, MIXED ? 3 : 2)
+__global__ void __launch_bounds__(kBlockC, MIXED ? 4 : 3)
     k_cf(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
          tmps_engine* __restrict__ E, uint32_t* __restrict__ flags, const float* __restrict__ gap,
          const float* __restrict__ agap, double* __restrict__ part) {
@@ -1520,7 +1645,7 @@ __global__ void __launch_bounds__(kBlockA, 4) kb_a32(const tmps_instance* __rest
 }
 
 template <int STYLE, bool MIXED>
-__global__ void __launch_bounds__(kBlockC, 2)
+__global__ void __launch_bounds__(kBlockC, MIXED ? 4 : 3)
     kb_cf(const tmps_instance* __restrict__ inst, const int32_t* __restrict__ block_inst) {
     __shared__ tmps_instance si;
     const tmps_instance& I = stage_instance(si, inst, block_inst[blockIdx.x]);

@@ -79,7 +79,9 @@ __global__ void __launch_bounds__(kBlock) k_cundall(tmps_atoms a, double gl, dou
 
 // NeighborList.check_displacement (neighbor.py:242-245): stamp the flag when
 // |x - x0|^2 > trigger.  Exact FP64 (no contraction) so the decision matches
-// the reference for the same positions.
+// the reference for the same positions.  A non-finite displacement stamps it
+// too (the reference's test lets a NaN through): the rebuild that follows
+// bins the atom and reports TMPS_STATUS_NONFINITE.
 __global__ void __launch_bounds__(kBlock) k_skin_check(tmps_atoms a, double trig, int32_t stamp,
                                                         int32_t* flag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -91,7 +93,7 @@ __global__ void __launch_bounds__(kBlock) k_skin_check(tmps_atoms a, double trig
         double d1 = __dsub_rn(x.y, a.x0[n + i]);
         double d2 = __dsub_rn(x.z, a.x0[2 * n + i]);
         double s = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
-        hit = s > trig;
+        hit = !(s <= trig);
     }
     // one store per warp that saw a crossing; nothing at all in the common case
     if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) *flag = stamp;

@@ -347,3 +347,42 @@ def test_launch_shape_changes_rounding_only(gpu, oracle, precision):
         assert rel_err(g["f"], o["f"]) < MIXED_F
         assert rel_err(g["v"], o["v"]) < MIXED_V
         np.testing.assert_allclose(sim.domain.prd, osim.domain.prd, rtol=1e-9)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_neighbor_delay_every_check(gpu, oracle, precision):
+    """neigh_modify delay 5 every 3 check yes through the fused step: a rebuild only once 5 steps have
+    passed since the last one, only on every third step, and only when an atom moved more than half the
+    skin (NeighborList.decide, neighbor.py:371-403).  The rebuild steps match the oracle's step by step
+    (runs of 7 steps continuing one another), and so does the state."""
+    rng = np.random.default_rng(57)
+    x, r = dense_packing(rng, 343, 7.0, 0.5, 0.56)
+    v = rng.normal(scale=0.8, size=x.shape)
+    w = rng.normal(scale=2.0, size=x.shape)
+    sim, osim = make_twin(oracle, x, r, 2.5, [0.0] * 3, [7.0] * 3, v=v, w=w, pair="hertz/history", dt=5e-5,
+                          skin=0.004, cundall=(0.7, 0.7))
+    sim.precision = precision
+    for nl in (sim.neighbor, osim.neighbor):
+        nl.delay, nl.every, nl.check = 5, 3, True
+    builds, obuilds = [], []
+    for seg in range(9):
+        sim.run(7)
+        if seg == 0:
+            osim.run(7)
+        else:  # the oracle's step() continues a run without the setup pass (run 7 pre no)
+            for _ in range(7):
+                osim.step()
+        sim.run_pre = False
+        builds.append((sim.neighbor.build_count, sim.neighbor.last_build_step))
+        obuilds.append((osim.neighbor.build_count, osim.neighbor.last_build_step))
+    assert builds == obuilds, (builds, obuilds)
+    # rebuilds happened, all at steps that the delay and every rules allow
+    assert builds[-1][0] >= 4
+    assert all(b[1] % 3 == 0 for b in builds)
+    g, o = gpu_state(sim), oracle_state(osim)
+    if precision == "fp64":
+        for k in ("x", "v", "omega", "f", "torque"):
+            assert rel_err(g[k], o[k]) < 1e-10, (k, rel_err(g[k], o[k]))
+    else:
+        assert rel_err(g["v"], o["v"]) < MIXED_V, rel_err(g["v"], o["v"])
+        assert rel_err(g["f"], o["f"]) < MIXED_F, rel_err(g["f"], o["f"])
