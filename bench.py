@@ -68,9 +68,12 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="config2", choices=["config2", "ensemble", "adjoint", "triaxial"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "dense", "ensemble", "adjoint", "triaxial"],
                     help="config2: the 1M-sphere servo run (default); ensemble: the batched-instances run")
     ap.add_argument("--instances", type=int, default=512, help="ensemble: number of instances")
+    ap.add_argument("--no-dense", action="store_true", help="skip the contact-dense 1M-sphere line")
+    ap.add_argument("--dense-reps", type=int, nargs=3, default=[4, 4, 4],
+                    help="dense: copies of the compressed 15,625-sphere cell along x, y, z")
     return ap.parse_args()
 
 
@@ -114,10 +117,17 @@ class ClockSampler:
 # ----------------------------------------------------------------- GPU arm
 
 
+def box_of(p):
+    """Lower and upper corners of a packing's periodic box (`L` a cube edge or three edges, `lo` optional)."""
+    L = np.broadcast_to(np.asarray(p["L"], dtype=np.float64), (3,))
+    lo = np.asarray(p.get("lo", np.zeros(3)), dtype=np.float64)
+    return [float(a) for a in lo], [float(a) for a in lo + L]
+
+
 def make_sim(G, p, n, precision, host=None):
     """The config-2 system; `host` (optional) holds x, v as pinned float64 tensors to upload from."""
-    L = p["L"]
-    dom = G.Domain(boxlo=[0.0] * 3, boxhi=[L] * 3, boundary=("p", "p", "p"))
+    lo, hi = box_of(p)
+    dom = G.Domain(boxlo=lo, boxhi=hi, boundary=("p", "p", "p"))
     atom = G.AtomSystem(max_atoms=n)
     if host is not None:
         atom.add_particles(x=host["x"], radius=host["radius"], density=p["density"], v=host["v"])
@@ -281,7 +291,7 @@ def run_e2e(args, p, precision):
         times.append(time.perf_counter() - t0)
     dt = statistics.median(times)
     assert np.isfinite(x).all() and np.isfinite(v).all() and np.isfinite(pressures).all()
-    up = n * (3 * 8 + 8 + 3 * 8 + 2 * 8)        # positions, radius, velocities; mass and inertia
+    up = n * (3 * 8 + 8 + 3 * 8)                # positions, radius, velocities (mass and inertia are formed on the device)
     down = n * 2 * 3 * 8 + K * 48               # final x, v; per step the pressure tensor
     return {"value": n * K / dt, "unit": UNIT, "h2d_bytes_per_step": up / K, "d2h_bytes_per_step": down / K,
             "seconds": dt, "precision": precision,
@@ -294,8 +304,8 @@ def run_e2e(args, p, precision):
 
 def oracle_sim(O, p, nthreads):
     O.set_threads(nthreads)
-    L = p["L"]
-    dom = O.OracleDomain.make([0.0] * 3, [L] * 3)
+    lo, hi = box_of(p)
+    dom = O.OracleDomain.make(lo, hi)
     at = O.OracleAtoms(x=p["x"], radius=p["radius"], density=p["density"], v=p["v"])
     nl = O.OracleNeighbor(dom, skin=SKIN, max_neighbors=32)
     hist = O.OracleHistory(32)
@@ -428,6 +438,78 @@ def run_ensemble(args):
                                             "graphs), same steps"},
             "speedup_vs_looped": t_loop / t_batch, "batched_seconds": t_batch,
             "gpu_launches_batched": launches_batch, "launch_shape": shape}
+
+
+# ----------------------------------------------------------------- dense state
+
+DENSE_WORKLOAD = ("1M-sphere contact-dense servo run: a 15,625-sphere cell compressed to p = 1 "
+                  "(packing.dense_cell) tiled 4x4x4, at rest; the config-2 physics (gran/hertz/history kn=2e5 "
+                  "kt=2/7kn gn=50 gt=25 xmu=0.5, nve/sphere, damping/cundall 0.7 0.7, deform/pressure x/y/z "
+                  "pressure 1.0 pgain 1e-3 couple xyz max/rate 1e-4 remap x, dt 5e-5, skin 0.1)")
+DENSE_TRAFFIC_FILE = ROOT / "profiles" / "ncu_traffic_dense_1M.json"
+
+
+def contact_bytes(precision: str, n_nb: float, n_c: float) -> float:
+    """Algorithmic bytes per atom of one contact-kernel launch: S + 4 n_nb + 52 n_c, S the atom's own
+    state read once and its force and torque written once (84 mixed, 140 FP64), 4 per neighbor-list
+    entry, 4 (partner) + 48 (shear read and written) per touching entry."""
+    return (84.0 if precision == "mixed" else 140.0) + 4.0 * n_nb + 52.0 * n_c
+
+
+def dense_traffic(kernel: str, precision: str):
+    if not DENSE_TRAFFIC_FILE.exists():
+        return None
+    d = json.loads(DENSE_TRAFFIC_FILE.read_text())
+    k = d.get("kernels", {}).get(f"{kernel}/{precision}")
+    if not k:
+        return None
+    return {"bytes": k["dram_bytes_read"] + k["dram_bytes_write"], "source": f"ncu: {d.get('command', '')}",
+            "n_atoms": d.get("n_atoms")}
+
+
+def run_dense(args, rank, world, forms):
+    """The contact kernel where contacts exist: the same physics on the tiled compressed packing, W warm-up
+    and K timed steps per form, the contact kernel's time against its algorithmic bytes at the measured
+    neighbor and contact counts.  The FP64 form is the reference for the mixed form's pressure here."""
+    import torch
+    from taichimps_gb300.packing import dense_config2
+    p = dense_config2(reps=tuple(args.dense_reps))
+    p["density"] = 2.5
+    runs = {}
+    for prec in forms:
+        runs[prec] = run_gpu_arm(args, p, prec, rank, world)
+        del runs[prec]["sim"]
+        torch.cuda.empty_cache()
+    if rank != 0:
+        return None
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6806.5)
+    scal = lambda t: (t[0] + t[1] + t[2]) / 3.0
+    out = {"workload": DENSE_WORKLOAD, "n_atoms": runs[forms[0]]["n"], "steps": args.steps, "warmup": args.warmup,
+           "forms": {}}
+    for prec, r in runs.items():
+        n = r["n"]
+        kb = contact_bytes(prec, r["n_nb"], r["n_c"])
+        c_ms = r["kern_ms"].get("fused_c")
+        ach = kb * n / (c_ms * 1e-3) / 1e9 if c_ms else None
+        tr = dense_traffic(KERNEL_NAMES[("fused_c", prec)], prec)
+        out["forms"][prec] = {
+            "value": world * n * args.steps / (r["ms"] * 1e-3), "ms_per_step": r["ms"] / args.steps,
+            "kernel_ms": r["kern_ms"], "neighbors_per_atom": r["n_nb"], "contacts_per_atom": r["n_c"],
+            "flagged_atoms_frac": r["flagged"], "rebuilds_in_timed_steps": r["rebuilds_timed"],
+            "mean_pressure": scal(r["pressure"]), "pressure": list(map(float, r["pressure"])),
+            "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "contact_kernel": {"kernel": KERNEL_NAMES[("fused_c", prec)], "bound": "hbm", "achieved": ach,
+                               "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None,
+                               "bytes_per_atom": kb, "algorithmic_bytes_per_launch": kb * n,
+                               "bytes_formula": "S + 4 n_nb + 52 n_c, S = 84 mixed / 140 FP64",
+                               "kernel_ms": c_ms, "traffic": tr["bytes"] if tr else None,
+                               "traffic_source": tr["source"] if tr else None}}
+    if len(runs) == 2:
+        m, f = out["forms"]["mixed"], out["forms"]["fp64"]
+        out["speedup_mixed_vs_fp64"] = m["value"] / f["value"]
+        out["mixed_mean_pressure_rel_err_vs_fp64"] = rel(m["mean_pressure"], f["mean_pressure"])
+    return out
 
 
 # ----------------------------------------------------------------- main
@@ -632,6 +714,21 @@ def main():
         torch.cuda.set_device(local)
         print(json.dumps(run_ensemble(args)), flush=True)
         return
+    if args.workload == "dense":
+        if args.impl != "ours":
+            print(json.dumps({"impl": args.impl, "unavailable": "the dense line is part of the default run"}))
+            return
+        import torch
+        torch.cuda.set_device(local)
+        if world > 1:
+            torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+        forms = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
+        out = run_dense(args, rank, world, forms)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
     if args.impl == "reference":
         out = reference_arm(args, rank, world)
         if out is not None:
@@ -669,6 +766,7 @@ def main():
     c_achieved = c_bytes * n / (kern["fused_c"] * 1e-3) / 1e9 if kern.get("fused_c") else None
     c_traffic = ncu_traffic("fused_c", head)
     e2e = None if args.no_e2e else run_e2e(args, p, head)
+    dense = None if args.no_dense else run_dense(args, rank, world, forms)
     cpu = None
     p_oracle = None
     if not args.no_cpu:
@@ -720,6 +818,7 @@ def main():
         "pressure_compared_after_steps": r["steps_run"],
         "forms": forms_out,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r["launches"], "clocks": r["clocks"],
+        "dense": dense,
     }
     print(json.dumps(out), flush=True)
     if world > 1:

@@ -217,3 +217,63 @@ def compress_packing(n: int, seed: int, dmin: float = 0.8, dmax: float = 1.2, de
     vol_s = float(np.sum((4.0 / 3.0) * np.pi * p["radius"] ** 3))
     return {"x": state["x"], "radius": p["radius"], "lo": lo, "L": hi - lo, "pressure": tensor,
             "phi": vol_s / float(np.prod(hi - lo)), "density": density}
+
+
+def tile_packing(cell: dict, reps=(4, 4, 4)) -> dict:
+    """A periodic packing repeated reps[0] x reps[1] x reps[2] times in a box that many cells wide.
+
+    A packing in a periodic box is also a packing of any whole number of
+    copies of that box: every sphere keeps the neighbours it had through the
+    cell's periodic images, so the tiled system starts with the cell's contact
+    network (and pressure) in every copy.  Copies are laid out x fastest, then
+    y, then z; positions are cell positions (wrapped into the cell) plus the
+    copy's offset.  Returns dict(x, radius, lo, L, density, phi)."""
+    lo = np.asarray(cell["lo"], dtype=np.float64)
+    L = np.asarray(cell["L"], dtype=np.float64)
+    x = lo + np.mod(np.asarray(cell["x"], dtype=np.float64) - lo, L)
+    r = np.asarray(cell["radius"], dtype=np.float64)
+    xs, rs = [], []
+    for kz in range(reps[2]):
+        for ky in range(reps[1]):
+            for kx in range(reps[0]):
+                xs.append(x + L * np.array([kx, ky, kz], dtype=np.float64))
+                rs.append(r)
+    Lt = L * np.array(reps, dtype=np.float64)
+    out = {"x": np.concatenate(xs), "radius": np.concatenate(rs), "lo": lo.copy(), "L": Lt,
+           "density": float(cell.get("density", 2.5))}
+    out["phi"] = float(np.sum((4.0 / 3.0) * np.pi * out["radius"] ** 3) / np.prod(Lt))
+    return out
+
+
+# The contact-dense counterpart of the 1M-sphere servo run: a 15,625-sphere
+# cell compressed to p = 1 with the run's own contact law, tiled 4 x 4 x 4.
+DENSE_CELL_FILE = "dense_cell_hertz2e5_15625.npz"
+DENSE_CELL_ARGS = dict(n=15625, seed=11, kn=2.0e5, dt=2.5e-4, max_rate=0.005, cycles=100, relax_cycles=10,
+                       cycle_steps=2000, precision="mixed")
+
+
+def dense_cell(path=None, regenerate: bool = False) -> dict:
+    """The compressed cell of the dense 1M-sphere workload: gran/hertz/history kn 2e5 (kt 2/7 kn, gamman
+    50, gammat 25, xmu 0.5), d ~ U[0.8, 1.2], density 2.5, 15,625 spheres compressed by compress_packing
+    with DENSE_CELL_ARGS.  Read from the package's data file (written by this function on a GPU run with
+    regenerate=True, so every run of the workload starts from the same bits)."""
+    from pathlib import Path
+    f = Path(path) if path is not None else Path(__file__).resolve().parent / "data" / DENSE_CELL_FILE
+    if f.exists() and not regenerate:
+        z = np.load(f)
+        return {"x": z["x"], "radius": z["radius"], "lo": z["lo"], "L": z["L"], "pressure": z["pressure"],
+                "phi": float(z["phi"]), "density": float(z["density"])}
+    a = dict(DENSE_CELL_ARGS)
+    cell = compress_packing(a.pop("n"), **a)
+    f.parent.mkdir(parents=True, exist_ok=True)
+    np.savez(f, x=cell["x"], radius=cell["radius"], lo=cell["lo"], L=cell["L"], pressure=cell["pressure"],
+             phi=cell["phi"], density=cell["density"])
+    return cell
+
+
+def dense_config2(reps=(4, 4, 4), path=None) -> dict:
+    """The dense workload's packing: the compressed cell tiled `reps` times (4 x 4 x 4 = 1,000,000
+    spheres), at rest; dict(x, radius, L (three edges), lo, v, density, phi)."""
+    t = tile_packing(dense_cell(path), reps)
+    t["v"] = np.zeros_like(t["x"])
+    return t
