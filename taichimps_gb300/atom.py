@@ -179,13 +179,15 @@ class AtomSystem:
 
     # ---------------------------------------------------------- particles
 
-    def add_particles(self, x, radius, density, v=None, omega=None, tag=None, atom_type=1) -> None:
+    def add_particles(self, x, radius, density, v=None, omega=None, tag=None, atom_type=1, rmass=None) -> None:
         """Append particles; rmass = 4/3 pi r^3 density (atom.py:55-145).  Arrays may be numpy or
-        torch tensors; a pinned host tensor or a CUDA tensor is uploaded without a host copy."""
+        torch tensors; a pinned host tensor or a CUDA tensor is uploaded without a host copy.
+        `rmass` (not in the reference): the masses as given, for a system read back from a restart
+        file, which stores them -- recomputing them from a density would round differently."""
         tens = {k: a for k, a in (("x", x), ("v", v), ("omega", omega)) if isinstance(a, torch.Tensor)}
         if isinstance(radius, torch.Tensor):
             radius = radius.detach().cpu().numpy()
-        if tens and self.nlocal == 0 and all(t.dtype == torch.float64 and t.dim() == 2 and t.shape[1] == 3
+        if tens and rmass is None and self.nlocal == 0 and all(t.dtype == torch.float64 and t.dim() == 2 and t.shape[1] == 3
                                               for t in tens.values()):
             self._add_first_tensors(tens, radius, density, tag, atom_type)
             return
@@ -207,6 +209,9 @@ class AtomSystem:
         types = (np.full(n_new, int(atom_type), dtype=np.int32) if np.isscalar(atom_type)
                  else np.asarray(atom_type, dtype=np.int32))
         mass, inertia = _sphere_mass(rad, dens)
+        if rmass is not None:
+            mass = np.broadcast_to(np.asarray(rmass, dtype=np.float64), rad.shape).copy()
+            inertia = ((0.4 * mass) * rad) * rad
         start = self.nlocal
         tags = (np.arange(start + 1, start + n_new + 1, dtype=np.int32) if tag is None
                 else np.asarray(tag, dtype=np.int32))

@@ -192,6 +192,17 @@ class ContactHistory:
                 out[uid[p]].append((int(tag[q]), sh[:, k, p].copy()))
         return out
 
+    def both_sided_contacts(self, nlist):
+        """Every touching contact under both of its atoms, as flat arrays (row atom's insertion index,
+        partner tag, values): values are the shear in the row atom's i->j sense, followed by the
+        rolling displacement when a rolling model keeps one (3 or 6 per contact).  Rows ascend, each
+        row's contacts in slot order -- FixNeighHistory's per-atom records, for write_restart."""
+        pp, kk, qq, uid, tag, sh = self._touching_slots(nlist)
+        vals = sh[:, kk, pp].T
+        if self.rolling is not None:
+            vals = np.concatenate([vals, self.rolling.cpu().numpy()[:, kk, pp].T], axis=1)
+        return uid[pp].astype(np.int64), tag[qq].astype(np.int32), np.ascontiguousarray(vals)
+
     def contacts_by_tag(self, nlist) -> dict[tuple[int, int], np.ndarray]:
         """{(tag_i, tag_j): shear in the i->j sense} for every touching slot (both sides)."""
         pp, kk, qq, uid, tag, sh = self._touching_slots(nlist)
@@ -206,21 +217,38 @@ class ContactHistory:
         the reference's half list does, and its other copy is set to the exact negative."""
         n = min(len(partner_tags), self.max_atoms)
         us, ts, vs = [], [], []
+        width = 3
         for i in range(n):
             t = np.asarray(partner_tags[i], dtype=np.int64).reshape(-1)
             m = len(t)
-            if m > self.max_neighbors:
-                raise ValueError(f"atom {i} has {m} stored contacts but the history only "
-                                 f"has {self.max_neighbors} slots per atom")
-            w = np.zeros((m, 3))
-            if m:
-                v = np.asarray(values[i], dtype=np.float64).reshape(m, -1)
-                w[:, :min(3, v.shape[1])] = v[:, :3]
+            v = np.asarray(values[i], dtype=np.float64).reshape(m, -1) if m else np.zeros((0, 3))
+            width = max(width, v.shape[1])
             us.append(np.full(m, i, dtype=np.int64))
             ts.append(t)
-            vs.append(w)
+            vs.append(v)
+        width = 6 if width >= 6 else 3
+        vs = [np.pad(v[:, :width], ((0, 0), (0, max(0, width - v.shape[1])))) for v in vs]
         cat = lambda a, shape: np.concatenate(a) if a else np.zeros(shape)
-        self._restart = (cat(us, 0).astype(np.int64), cat(ts, 0).astype(np.int64), cat(vs, (0, 3)))
+        self.load_restart_arrays(cat(us, 0), cat(ts, 0), cat(vs, (0, width)))
+
+    def load_restart_arrays(self, rows, partner_tags, values) -> None:
+        """load_restart from flat arrays, one entry per stored contact: the atom's position in the
+        add_particles order, the partner's tag and the values (shear, then the rolling displacement when
+        there are six).  RestartData.neigh_history() gives these arrays for a whole file at once."""
+        rows = np.asarray(rows, dtype=np.int64).reshape(-1)
+        tags = np.asarray(partner_tags, dtype=np.int64).reshape(-1)
+        vals = np.asarray(values, dtype=np.float64).reshape(len(rows), -1) if len(rows) else np.zeros((0, 3))
+        keep = rows < self.max_atoms
+        rows, tags, vals = rows[keep], tags[keep], vals[keep]
+        if len(rows):
+            per = np.bincount(rows)
+            if per.max() > self.max_neighbors:
+                i = int(np.argmax(per))
+                raise ValueError(f"atom {i} has {int(per[i])} stored contacts but the history only "
+                                 f"has {self.max_neighbors} slots per atom")
+        if vals.shape[1] >= 6:
+            self.enable_rolling()  # the records carry a rolling displacement: keep it
+        self._restart = (rows, tags, vals)
         self.setup_pending = True
 
     def _apply_restart(self, atom, nlist) -> None:
@@ -257,7 +285,12 @@ class ContactHistory:
         sh = np.zeros((3, S, n))
         np.bitwise_or.at(touch, po, np.left_shift(np.uint64(1), ko.astype(np.uint64)))
         np.bitwise_or.at(touch, qo, np.left_shift(np.uint64(1), km.astype(np.uint64)))
-        sh[:, ko, po] = val.T
-        sh[:, km, qo] = -val.T
+        sh[:, ko, po] = val[:, :3].T
+        sh[:, km, qo] = -val[:, :3].T
         self.touch.copy_(torch.from_numpy(touch.view(np.int64)))
         self.shear.copy_(torch.from_numpy(sh))
+        if self.rolling is not None and val.shape[1] >= 6:
+            rl = np.zeros((3, S, n))
+            rl[:, ko, po] = val[:, 3:6].T
+            rl[:, km, qo] = -val[:, 3:6].T
+            self.rolling.copy_(torch.from_numpy(rl))

@@ -70,8 +70,26 @@ class Simulation:
     def add_dump(self, dump, freq: int = 100) -> None:
         raise NotImplementedError("dump output is outside the GB300 contact path")
 
-    def set_restart(self, every: int, path, writer) -> None:
-        raise NotImplementedError("restart output is outside the GB300 contact path")
+    def set_restart(self, every: int, path, writer=None) -> None:
+        """Periodic restart output, `restart N file` (simulation.py:86-90): run() writes one every `every`
+        steps through writer(path with the step for a `*`, step).  With no writer, the file is a LAMMPS
+        restart of this system written by taichimps_gb300.restart.write_restart (atoms, box, pair style
+        and the contact history)."""
+        self.restart_every = int(every)
+        self.restart_file = None if path is None else str(path)
+        self.restart_writer = writer
+
+    def write_restart_now(self) -> None:
+        """Write one periodic restart file for the current step (simulation.py:92-98)."""
+        if not self.restart_file:
+            return
+        path = self.restart_file.replace("*", str(self.timestep))
+        if self.restart_writer is not None:
+            self.restart_writer(path, self.timestep)
+            return
+        from .restart import write_restart
+        write_restart(path, self.atom, self.domain, timestep=self.timestep, dt=self.dt, history=self.history,
+                      pair=self.pair_style, nlist=self.neighbor if self.neighbor.has_built else None)
 
     def set_pair_style(self, pair: GranularPair) -> None:
         self.pair_style = pair
@@ -167,17 +185,30 @@ class Simulation:
         if self.precision == "mixed" and not (self.fused and fusable(self)):
             raise NotImplementedError("the mixed form runs through the fused step: fix nve/sphere with "
                                       "optional damping/cundall and deform/pressure")
-        if self.fused and steps > 0 and fusable(self) and self.atom.nlocal > 0:
-            eng = FusedEngine(self, self.precision)
-            self.last_engine = eng
-            eng.begin()
-            try:
-                eng.run(steps)
-            finally:
-                eng.finish()
-        else:
-            for _ in range(steps):
-                self._sub_step_inner()
+        # with periodic restart output the run stops at each multiple of restart_every to write one
+        # (the next segment continues without a setup pass, as `run N pre no` would)
+        remaining = int(steps)
+        while True:
+            seg = remaining
+            if self.restart_every > 0:
+                seg = min(seg, self.restart_every - self.timestep % self.restart_every)
+            if self.fused and seg > 0 and fusable(self) and self.atom.nlocal > 0:
+                eng = FusedEngine(self, self.precision)
+                self.last_engine = eng
+                eng.begin()
+                try:
+                    eng.run(seg)
+                finally:
+                    eng.finish()
+            else:
+                for _ in range(seg):
+                    self._sub_step_inner()
+            remaining -= seg
+            if self.restart_every > 0 and seg > 0 and self.timestep % self.restart_every == 0:
+                self.check_device_status()
+                self.write_restart_now()
+            if remaining <= 0:
+                break
         self.check_device_status()
         self.domain.pull()
 

@@ -29,6 +29,7 @@ AXES = {"x": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
         "y": {"style": "pressure", "ptarget": 1.0, "pgain": 0.1},
         "z": {"style": "erate", "rate": -1e-3}}
 MAX_RATE = 1e-2
+P_SCALE = 1.0  # the pressure target: the size of the stress components q is a difference of
 BASE = dict(kn=1.0e5, kt=1.0e5 * 2.0 / 7.0, gamman=50.0, gammat=25.0, xmu=0.5)
 TARGET = dict(BASE, kn=1.3e5, xmu=0.4)
 DT = 5e-5
@@ -91,6 +92,7 @@ def _loss_and_grads_adjoint(run, prm, radius, target):
     q = stress_curve(run, ps["kn"], ps["kt"], ps["gamman"], ps["gammat"], ps["xmu"], r)
     L = ((q - target) ** 2).sum()
     L.backward()
+    _loss_and_grads_adjoint.q = q.detach().clone()
     return float(L), {k: float(v.grad) for k, v in ps.items()}, r.grad.detach().clone()
 
 
@@ -110,6 +112,7 @@ def _torch_grads(pk, prm, steps, every, target, pi, pj, v=None):
     qs = q[every - 1::every]
     L = ((qs - target) ** 2).sum()
     L.backward()
+    _torch_grads.q = qs.detach().clone()
     return float(L), {k: float(P[k].grad) for k in prm}, r.grad.detach()
 
 
@@ -133,8 +136,17 @@ def test_adjoint_matches_autograd(pack512):
     r = torch.tensor(pack512["radius"], dtype=torch.float64, device="cuda")
     L_a, g_a, gr_a = _loss_and_grads_adjoint(run, BASE, r, target)
     pi, pj = run.lists[0].pi, run.lists[0].pj
+    q_a = _loss_and_grads_adjoint.q
     L_t, g_t, gr_t = _torch_grads(pack512, BASE, steps, every, target, pi, pj)
-    assert abs(L_a - L_t) <= 1e-10 * abs(L_t), (L_a, L_t)
+    q_t = _torch_grads.q
+    # the two FP64 forwards sum in different orders: q agrees to rounding, which is relative to the
+    # pressures q is a difference of (their scale is the servo's target, 1), not to q itself
+    dq = float((q_a - q_t).abs().max())
+    assert dq <= 1e-11 * P_SCALE, (dq, q_t)
+    # and the loss to first order in that difference: q - target = 0.1 q0 - 0.01 may nearly cancel, so
+    # the loss's relative error is not bounded by q's, its absolute error is
+    bound = 2.0 * float((q_t - target).abs().sum()) * dq + len(q_t) * dq * dq
+    assert abs(L_a - L_t) <= bound * (1.0 + 1e-6) + 1e-300, (L_a, L_t, dq, bound)
     for k in BASE:
         assert abs(g_a[k] - g_t[k]) <= 1e-8 * abs(g_t[k]) + 1e-12, (k, g_a[k], g_t[k])
     scale = gr_t.abs().max()
@@ -179,11 +191,13 @@ def _fd(loss, base, h_list):
     return vals[best], spread[best], vals
 
 
-def test_adjoint_matches_finite_differences(pack2048):
+@pytest.fixture(scope="module")
+def fd2048(pack2048):
     """2,048 spheres, 200 steps, q every 50 steps, checkpoints every 100: the
-    gradients of sum (q - q_target)^2, q_target from kn 1.3e5 and xmu 0.4,
-    against FP64 central differences (relative steps 1e-3 .. 1e-7 for the
-    parameters, absolute 1e-4 .. 1e-8 for radii), within 1e-5 relative."""
+    gradients of sum (q - q_target)^2, q_target from kn 1.3e5 and xmu 0.4, and
+    FP64 central differences of the same loss (relative steps 1e-2 .. 1e-5 for
+    the parameters, 1e-4 .. 1e-7 for radii).  Returns {name: (adjoint,
+    difference estimate, spread of the differences, all differences)}."""
     steps, every = 200, 50
     run = _run(pack2048, steps, every, 100)
     target = run.forward(**TARGET).clone()
@@ -195,13 +209,12 @@ def test_adjoint_matches_finite_differences(pack2048):
         q = run.forward(**prm, radius=radius)
         return float(((q - target) ** 2).sum())
 
-    errs, info = {}, {}
+    out = {}
     steps_rel = [1e-2, 3e-3, 1e-3, 3e-4, 1e-4, 3e-5, 1e-5]
     for k in BASE:
         fd, spread, vals = _fd(lambda v: loss_of(dict(BASE, **{k: v}), r0), BASE[k],
                                [BASE[k] * h for h in steps_rel])
-        errs[k] = abs(g[k] - fd) / abs(fd)
-        info[k] = (g[k], spread, vals)
+        out[k] = (g[k], fd, spread, vals)
     # radii: the largest gradients and a few others
     order = torch.argsort(gr.abs(), descending=True).cpu().numpy()
     for i in list(order[:3]) + list(order[100:1000:300]):
@@ -210,29 +223,49 @@ def test_adjoint_matches_finite_differences(pack2048):
             rr[i] = v
             return loss_of(BASE, rr)
         fd, spread, vals = _fd(lr, float(r0[i]), [float(r0[i]) * h for h in (1e-4, 3e-5, 1e-5, 3e-6, 1e-6, 3e-7, 1e-7)])
-        errs[f"r{i}"] = abs(float(gr[i]) - fd) / abs(fd)
-        info[f"r{i}"] = (float(gr[i]), spread, vals)
-    print("adjoint vs finite differences, relative errors:", {k: f"{v:.2e}" for k, v in errs.items()})
-    for k, (ga, spread, vals) in info.items():
-        print(f"  {k}: adjoint {ga:.10e} fd spread {spread:.1e} fd", " ".join(f"{v:.10e}" for v in vals))
-    for k, e in errs.items():
+        out[f"r{i}"] = (float(gr[i]), fd, spread, vals)
+    print("adjoint vs finite differences, relative errors:",
+          {k: f"{abs(a - fd) / abs(fd):.2e}" for k, (a, fd, _, _) in out.items()})
+    for k, (a, fd, spread, vals) in out.items():
+        print(f"  {k}: adjoint {a:.10e} fd spread {spread:.1e} fd", " ".join(f"{v:.10e}" for v in vals))
+    return out
+
+
+def test_adjoint_matches_finite_differences(fd2048):
+    """kn, kt, gamman, gammat and the radii: the adjoint within 1e-5 relative of the central
+    differences (the gate).  xmu is checked by the two tests below."""
+    for k, (a, fd, spread, vals) in fd2048.items():
         if k == "xmu":
-            # every usable step spans Coulomb stick/slip thresholds of some contacts at this
-            # size (kinks of the loss in xmu), so the differences themselves only converge to
-            # their spread (~1e-4); the adjoint must lie within it.  test_xmu_gradient_small
-            # checks xmu at 1e-5 where the differences do converge; autograd checks it exactly.
-            assert e < max(1e-5, 2.0 * info[k][1]), (k, info[k], e)
-        else:
-            assert e < 1e-5, (k, info[k], e)
+            continue
+        e = abs(a - fd) / abs(fd)
+        assert e < 1e-5, (k, a, spread, vals, e)
+
+
+def test_xmu_misses_the_1e5_gate_at_stick_slip_kinks_but_lies_within_the_differences_spread(fd2048):
+    """xmu on the calibration-sized run does NOT meet the 1e-5 gate, and cannot be checked against it:
+    sliding contacts sit on the Coulomb bound, so every usable difference step moves some of them across
+    it (kinks of the loss in xmu) and the differences converge only to their own spread (~1e-4, far
+    above 1e-5).  What holds, and is asserted: the adjoint lies within twice that spread of the best
+    difference estimate.  The gate itself is met for xmu where the differences converge
+    (test_xmu_gradient_small, gross sliding) and the adjoint equals PyTorch autograd of the same forward
+    to 1e-8 (test_adjoint_matches_autograd)."""
+    a, fd, spread, vals = fd2048["xmu"]
+    e = abs(a - fd) / abs(fd)
+    print(f"xmu at 2048 x 200: adjoint {a:.10e} fd {fd:.10e} relative error {e:.1e} (gate 1e-5), "
+          f"spread of the differences {spread:.1e}")
+    assert spread > 1e-5, "the differences converged: this test's premise no longer holds, use the gate"
+    assert e < 2.0 * spread, (a, vals, e, spread)
 
 
 def test_xmu_gradient_small(pack512):
-    """xmu where the sliding is gross: spheres spun up (omega ~ N(0, 5^2)) so
-    every contact slides each step with a wide margin over the Coulomb bound;
-    no contact crosses the threshold within the finite-difference steps, the
-    differences converge and agree with the adjoint to 1e-5."""
+    """xmu where the sliding is gross: spheres spun up (omega ~ N(0, 50^2)) so
+    that a contact's tangential spring passes the Coulomb bound within its first
+    step (shear per step ~ |omega| r dt = 1.25e-3 against xmu kn delta / kt
+    ~ 9e-4 at the packing's overlaps) and slides from then on with a wide
+    margin; no contact crosses the threshold within the finite-difference
+    steps, the differences converge and agree with the adjoint to 1e-5."""
     steps, every = 50, 10
-    w = np.random.default_rng(11).normal(0.0, 5.0, size=pack512["x"].shape)
+    w = np.random.default_rng(11).normal(0.0, 50.0, size=pack512["x"].shape)
     run = _run(pack512, steps, every, 25, omega=w)
     target = run.forward(**TARGET).clone()
     r0 = torch.tensor(pack512["radius"], dtype=torch.float64, device="cuda")
