@@ -154,20 +154,30 @@ def list_stats(sim):
 def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float, flagged: float) -> float:
     """Bytes per atom a launch must move through HBM.
 
-    fused_a (A), every atom:
-      mixed: reads the six FP32 state words (position, velocity, angular velocity, high and low) 96,
-             offset at the last build 12, packed cell 4; writes the six state words 96          = 208
-      FP64:  reads x, v, omega records 96, 1/m and 1/I 16, x at the last build 24; writes the records 96
-                                                                                                 = 232
+    fused_a (A), every atom: the Verlet stream of the step plus the skin check's reference words.
+      mixed: reads the position, velocity and angular velocity (high and low FP32 words, 72), m, 1/m
+             and 1/I (12), the offset at the last build (12) and the packed cell (4); writes the three
+             vectors, both words (72)                                                             = 172
+      FP64:  reads x, v, omega (72), 1/m and 1/I (16), x at the last build (24); writes x, v, omega (72)
+                                                                                                  = 184
       plus, per flagged atom (`flagged` = fraction), the force and torque: 24 (mixed) / 48 (FP64).
-    fused_c (C): the contact kernel's nominal per-atom bytes, S + 4 n_nb + 52 n_c (own state read once
-      and force written once, S = 84 mixed / 140 FP64; 4 per neighbor index; 4 partner + 48 shear per
-      touching slot).  C's bound check skips most of these bytes (groups that cannot touch read 4 bytes
-      per 32 atoms), so this figure is nominal: it says what a kernel without the check would move."""
+      The records A actually streams are float4 / double4 words whose fourth lanes hold per-build
+      constants (radius, m, I, 1/m, 1/I) for C's gathers, so A reads and writes those too
+      (layout_bytes: 208 mixed / 232 FP64); those extra bytes are not counted here.
+    fused_c (C): the contact kernel's per-atom bytes, S + 4 n_nb + 52 n_c (own state read once and
+      force written once, S = 84 mixed / 140 FP64; 4 per neighbor index; 4 partner + 48 shear per
+      touching slot)."""
     if kernel == "fused_a":
-        return (208.0 + 24.0 * flagged) if precision == "mixed" else (232.0 + 48.0 * flagged)
+        return (172.0 + 24.0 * flagged) if precision == "mixed" else (184.0 + 48.0 * flagged)
     if kernel == "fused_c":
         return (84.0 if precision == "mixed" else 140.0) + 4.0 * n_nb + 52.0 * n_c
+    return 0.0
+
+
+def layout_bytes(kernel: str, precision: str, flagged: float) -> float:
+    """Bytes per atom A's record layout makes it read and write (see algorithmic_bytes)."""
+    if kernel == "fused_a":
+        return (208.0 + 24.0 * flagged) if precision == "mixed" else (232.0 + 48.0 * flagged)
     return 0.0
 
 
@@ -186,6 +196,51 @@ def ncu_traffic(kernel: str, precision: str):
     if not k:
         return None
     return {"bytes": k["dram_bytes_read"] + k["dram_bytes_write"], "source": f"ncu: {d.get('command', '')}"}
+
+
+FP64_COUNTS_FILE = ROOT / "profiles" / "fp64_pipe_config2.json"
+
+
+def fp64_peak_dfma_per_s() -> float:
+    """The FP64 pipe's DFMA rate on this GPU, measured now (tmps_probe_fp64: eight independent DFMA chains
+    per thread, eight blocks of 256 threads per SM; best of five timed launches)."""
+    import torch
+    from taichimps_gb300 import _device
+    L = _device.lib()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    blocks, threads, iters = 8 * sms, 256, 4096
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    st = _device.stream()
+    for _ in range(2):
+        L.tmps_probe_fp64(blocks, threads, iters, out.data_ptr(), st)
+    best = None
+    s = torch.cuda.current_stream()
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        L.tmps_probe_fp64(blocks, threads, iters, out.data_ptr(), st)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return 8.0 * iters * blocks * threads / (best * 1e-3)
+
+
+def fp64_roofline(kernel: str, n: int, kernel_ms, peak: float):
+    """FP64-pipe roofline of an FP64-form kernel: its FP64 instructions per atom (DFMA + DMUL + DADD, from
+    the committed ncu counts, profiles/fp64_pipe_config2.json) x atoms / its CUDA-event time, against the
+    DFMA rate measured by fp64_peak_dfma_per_s."""
+    if not FP64_COUNTS_FILE.exists() or not kernel_ms or not peak:
+        return None
+    d = json.loads(FP64_COUNTS_FILE.read_text())
+    k = d.get("kernels", {}).get(kernel)
+    if not k:
+        return None
+    ach = k["fp64_inst_per_atom"] * n / (kernel_ms * 1e-3)
+    return {"kernel": kernel, "bound": "fp64 pipe", "achieved": ach, "peak": peak, "unit": "FP64 inst/s",
+            "frac": ach / peak, "fp64_inst_per_atom": k["fp64_inst_per_atom"],
+            "pipe_active_pct_ncu": k.get("pipe_active_pct"), "kernel_ms": kernel_ms,
+            "peak_source": "measured now: tmps_probe_fp64 (DFMA)", "counts_source": f"ncu: {d.get('command', '')}"}
 
 
 def max_over_ranks(ms: float, world: int, device: str = "cuda") -> float:
@@ -763,10 +818,10 @@ def main():
     achieved = bytes_atom * n / (kern[dom_name] * 1e-3) / 1e9 if kern.get(dom_name) else None
     traffic = ncu_traffic(dom_name, head)
     c_bytes = algorithmic_bytes("fused_c", head, r["n_nb"], r["n_c"], r["flagged"])
-    c_achieved = c_bytes * n / (kern["fused_c"] * 1e-3) / 1e9 if kern.get("fused_c") else None
     c_traffic = ncu_traffic("fused_c", head)
     e2e = None if args.no_e2e else run_e2e(args, p, head)
     dense = None if args.no_dense else run_dense(args, rank, world, forms)
+    fp64_peak = fp64_peak_dfma_per_s() if "fp64" in runs else None
     cpu = None
     p_oracle = None
     if not args.no_cpu:
@@ -789,7 +844,11 @@ def main():
             "gpu_launches": v["launches"], "rebuilds_in_timed_steps": v["rebuilds_timed"],
             "groups_culled": {"groups": v["cull"][0], "culled_after_timed_steps": v["cull"][1]},
             "flagged_atoms_frac": v["flagged"],
-            "kernel_bytes_per_atom": kb, "kernel_bytes_note": "fused_c: nominal (see algorithmic_bytes)"}
+            "kernel_bytes_per_atom": kb,
+            "kernel_bytes_note": "algorithmic bytes (see algorithmic_bytes); fused_c on this contact-free state "
+                                 "moves far fewer (its bound check), so its GB/s figure is nominal"}
+        if k == "fp64":
+            forms_out[k]["fp64_roofline"] = fp64_roofline("k_a64", n, v["kern_ms"].get("fused_a"), fp64_peak)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": r["ms"] / K, "higher_is_better": True, "scaling": "weak",
@@ -804,14 +863,14 @@ def main():
                      "traffic": traffic["bytes"] if traffic else None,
                      "traffic_source": traffic["source"] if traffic else None,
                      "algorithmic_bytes_per_launch": bytes_atom * n, "bytes_per_atom": bytes_atom,
+                     "layout_bytes_per_atom": layout_bytes(dom_name, head, r["flagged"]),
                      "kernel_ms": kern[dom_name], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
-        # the contact kernel on its own: the nominal bytes of a contact kernel over the full rows
-        # (S + 4 n_nb + 52 n_c per atom, see algorithmic_bytes) per C launch; C's bound check skips
-        # most of them, so this says how fast the contact work is against what it would have to move
-        "contact_kernel": {"kernel": KERNEL_NAMES[("fused_c", head)], "bound": "hbm (nominal bytes)",
-                           "achieved": c_achieved, "peak": peak, "unit": "GB/s",
-                           "frac": (c_achieved / peak) if c_achieved else None,
-                           "nominal_bytes_per_atom": c_bytes, "kernel_ms": kern.get("fused_c"),
+        # the contact kernel on this contact-free state: its bound check rules out most groups, so it
+        # moves a small part of the nominal S + 4 n_nb + 52 n_c bytes per atom (traffic) and its time
+        # is latency; no roofline fraction is claimed here -- the contact-dense line ("dense") carries
+        # the contact kernel's roofline on the bytes it moves
+        "contact_kernel": {"kernel": KERNEL_NAMES[("fused_c", head)], "bound": "latency (contact-free state)",
+                           "frac": None, "nominal_bytes_per_atom": c_bytes, "kernel_ms": kern.get("fused_c"),
                            "traffic": c_traffic["bytes"] if c_traffic else None},
         "speedup_mixed_vs_fp64": (values["mixed"] / values["fp64"]) if len(values) == 2 else None,
         "oracle_mean_pressure": None if p_oracle is None else scal(p_oracle),

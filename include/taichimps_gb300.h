@@ -410,9 +410,12 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
  * the last C (an unflagged atom's force and torque are exact zeros and are
  * not loaded) and writes the first virial partials, the kinetic term
  * sum m v v of every atom at mid-step velocity.  a_blocks: A's grid from
- * tmps_fused_shape, or <= 0 for the default. */
+ * tmps_fused_shape, or <= 0 for the default.  chained != 0 states that the
+ * previous launch on `stream` is tmps_fused_servo of the previous step of
+ * the same system: A (mixed form) then loads the first atom of each thread
+ * before its dependency wait, overlapping that S; pass 0 otherwise. */
 int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32_t a_blocks, void* scratch,
-                 void* stream);
+                 int32_t chained, void* stream);
 
 /* Launch C: per 32-atom group a bound check (tmps_fused_bounds), a screen of
  * the atoms the bounds leave (finishes contact-free ones, flags the rest) and
@@ -454,6 +457,13 @@ int64_t tmps_fused_scratch_bytes(int32_t n, int32_t style, int32_t mixed);
  * every step (deform_pressure.py:1113-1219); this is that read without the
  * round trip. */
 int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void* stream);
+
+/* FP64 pipe probe (no reference counterpart; the FP64 form's roofline
+ * denominator): eight independent DFMA chains of `iters` steps per thread on
+ * a grid of blocks x threads (threads a multiple of 32, at most 256); time it
+ * on `stream` and count 8 x iters x blocks x threads DFMA.  Each thread
+ * writes one double to d_out (blocks x threads slots); nothing is allocated. */
+int tmps_probe_fp64(int32_t blocks, int32_t threads, int32_t iters, double* d_out, void* stream);
 
 /* ---- batched runs ----------------------------------------------------------
  * Many independent systems of uneven size (each with its own box, contact

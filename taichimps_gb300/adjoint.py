@@ -191,8 +191,11 @@ class AdjointRun:
     # ----------------------------------------------------------- forward
 
     def forward(self, kn: float, kt: float, gamman: float, gammat: float, xmu: float,
-                radius: torch.Tensor | None = None) -> torch.Tensor:
-        """Runs `steps` steps; returns q at the sample steps (device tensor)."""
+                radius: torch.Tensor | None = None, track_masks: bool = False) -> torch.Tensor:
+        """Runs `steps` steps; returns q at the sample steps (device tensor).  track_masks: also keep
+        `mask_digest`, an integer fingerprint of every step's per-pair masks (contact on, Coulomb slip,
+        |shear| != 0, damping clamp) and rebuild steps -- two runs with equal digests took the same
+        branch of every piecewise law at every step, so the loss is smooth between them."""
         L = _device.lib()
         sc = _device.stream()
         f64 = dict(dtype=torch.float64, device=self.dev)
@@ -221,6 +224,7 @@ class AdjointRun:
         disp = torch.zeros(1, dtype=torch.int64, device=self.dev)
         trig = 0.25 * self.skin * self.skin
         self.rebuilds = 0
+        digest = torch.zeros((), dtype=torch.int64, device=self.dev)
         for s in range(1, self.steps + 1):
             if (s - 1) % self.checkpoint_every == 0:
                 self.ckpt[s - 1] = ({k: a.clone() for k, a in st.items()}, shear.clone(), li)
@@ -242,9 +246,20 @@ class AdjointRun:
                 self.rebuilds += 1
             _lib.check(L.tmps_adj_finish(self._sys(st, pairs, shear), self.prm, self.servo, tape.cstruct(),
                                          self.rec.data_ptr(), s, _p(self._work(pairs.npairs)), sc), "tmps_adj_finish")
+            if track_masks:
+                digest = self._digest_step(digest, tape.mask[:pairs.npairs], s if s in self.events else 0)
         self.final_state = st
+        self.mask_digest = int(digest.item()) if track_masks else None
         self._fwd = True
         return self.q_samples()
+
+    @staticmethod
+    def _digest_step(digest: torch.Tensor, mask: torch.Tensor, rebuilt: int) -> torch.Tensor:
+        """digest * 1000003 + sum_k mask_k (k + 1) + 7 sum_k mask_k (k + 1)^2 + rebuild step (int64,
+        wrapping): any change of one pair's mask bits changes it."""
+        k = torch.arange(1, mask.numel() + 1, dtype=torch.int64, device=mask.device)
+        m = mask.to(torch.int64)
+        return digest * 1000003 + (m * k).sum() + 7 * (m * k * k).sum() + rebuilt
 
     def records(self) -> np.ndarray:
         """The per-step records as a structured view: q, w, box (host copy)."""

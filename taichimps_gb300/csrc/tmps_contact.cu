@@ -56,13 +56,13 @@ __global__ void __launch_bounds__(kBlock)
         for (int c = 0; c < 3; ++c)
             if (per[c] == 1) {
                 nimg[c] = rint(in.d[c] * iprd[c]);
-                in.d[c] -= nimg[c] * prd[c];
+                in.d[c] = image_sub64(in.d[c], nimg[c], prd[c]);
             }
-        in.rsq = (in.d[0] * in.d[0] + in.d[1] * in.d[1]) + in.d[2] * in.d[2];
+        in.rsq = rsq64(in.d);
         in.ra = xa.w;
         in.rb = xb.w;
         const double radsum = in.ra + in.rb;
-        if (!(in.rsq < radsum * radsum && in.rsq > 1e-28)) continue;
+        if (!(in.rsq < __dmul_rn(radsum, radsum) && in.rsq > 1e-28)) continue;
         in.r = sqrt(in.rsq);
         in.delta = radsum - in.r;
         const double4 vj = ld4(A.vm, j), wj = ld4(A.om, j);

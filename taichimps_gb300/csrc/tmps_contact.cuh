@@ -46,6 +46,16 @@ TMPS_DEV float lsqrt<float>(float a) {
     return a >= 1e-30f ? a * rsqrtf(a) : sqrtf(a);
 }
 
+// The FP64 form's separation component and |d|^2, every operation rounded as
+// the reference writes it (d - n prd, d0 d0 + d1 d1 + d2 d2), with no
+// multiply-add contraction: the overlap radsum - |d| of a near contact cancels
+// about three digits, so a contracted |d|^2 or image shift would move a force
+// by ~1e-13 relative.
+TMPS_DEV double image_sub64(double d, double nimg, double prd) { return __dsub_rn(d, __dmul_rn(nimg, prd)); }
+TMPS_DEV double rsq64(const double* d) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+}
+
 template <typename T>
 TMPS_DEV T dot3(const T* a, const T* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
 template <typename T>

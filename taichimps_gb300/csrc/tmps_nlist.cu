@@ -50,30 +50,79 @@ __global__ void __launch_bounds__(kBlock) k_bin(tmps_atoms a, const tmps_box* __
     atomicAdd(&count[rank[lin]], 1);
 }
 
-// Exclusive scan of `count` (length m, by Morton rank) into start[0..m].
-// One block: each thread owns a contiguous chunk.  Runs once per rebuild.
-__global__ void __launch_bounds__(kScanBlock) k_scan(const int32_t* count, int32_t* start, int m) {
-    __shared__ int32_t part[kScanBlock];
-    const int t = threadIdx.x;
-    const int chunk = (m + kScanBlock - 1) / kScanBlock;
-    const int beg = t * chunk, end = min(m, beg + chunk);
-    int32_t s = 0;
-    for (int c = beg; c < end; ++c) s += count[c];
-    part[t] = s;
+// Exclusive scan of `count` (length m, by Morton rank) into start[0..m],
+// start[m] the total.  Two launches over tiles of kScanTile cells, one block
+// of kScanBlock threads per tile (each thread four consecutive cells):
+// k_scan_tiles writes each tile's total to tile_sum[tile]; k_scan_apply
+// adds the totals of the earlier tiles to a block-wide scan of its own tile.
+// Runs once per rebuild; ~74k cells (the 1M-sphere grid) are 19 tiles.
+constexpr int kScanTile = 4 * kScanBlock;
+
+__device__ __forceinline__ int32_t scan_tile_block(int32_t v, int32_t* wsum, int32_t& total) {
+    // exclusive block scan of one value per thread; total of the block
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
     __syncthreads();
-    // Hillis-Steele inclusive scan of the per-thread sums
-    for (int o = 1; o < kScanBlock; o <<= 1) {
-        int32_t v = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+    if (w == 0) {
+        int32_t s = wsum[lane];  // kScanBlock / 32 == 32 warps
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        wsum[lane] = s;
     }
-    int32_t run = part[t] - s;
-    for (int c = beg; c < end; ++c) {
-        start[c] = run;
-        run += count[c];
+    __syncthreads();
+    total = wsum[31];
+    return (w > 0 ? wsum[w - 1] : 0) + x - v;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_tiles(const int32_t* __restrict__ count, int m,
+                                                          int32_t* __restrict__ tile_sum) {
+    __shared__ int32_t wsum[kScanBlock / 32];
+    const int c0 = blockIdx.x * kScanTile + 4 * threadIdx.x;
+    int32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (c0 + k < m) v += count[c0 + k];
+    int32_t total;
+    scan_tile_block(v, wsum, total);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_apply(const int32_t* __restrict__ count,
+                                                          int32_t* __restrict__ start, int m,
+                                                          const int32_t* __restrict__ tile_sum) {
+    __shared__ int32_t wsum[kScanBlock / 32];
+    __shared__ int32_t base;
+    if (threadIdx.x < 32) {
+        int32_t s = 0;
+        for (int t = threadIdx.x; t < (int)blockIdx.x; t += 32) s += tile_sum[t];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) base = s;
     }
-    if (t == kScanBlock - 1) start[m] = part[t];
+    const int c0 = blockIdx.x * kScanTile + 4 * threadIdx.x;
+    int32_t cnt[4], v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        cnt[k] = c0 + k < m ? count[c0 + k] : 0;
+        v += cnt[k];
+    }
+    int32_t total;
+    int32_t run = scan_tile_block(v, wsum, total) + base;  // scan_tile_block's barriers publish `base`
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (c0 + k < m) start[c0 + k] = run;
+        run += cnt[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) start[m] = base + total;
 }
 
 __global__ void __launch_bounds__(kBlock) k_scatter(int n, const int32_t* __restrict__ rank,
@@ -311,6 +360,14 @@ bool launch_ok() { return cudaPeekAtLastError() == cudaSuccess; }
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// start = exclusive scan of count over m cells; tile_sum (at least one word per
+// kScanTile cells, m words always suffice) holds the tile totals in between
+void scan_cells(const int32_t* count, int32_t* start, int32_t* tile_sum, int m, cudaStream_t s) {
+    const int tiles = (m + kScanTile - 1) / kScanTile;
+    k_scan_tiles<<<tiles, kScanBlock, 0, s>>>(count, m, tile_sum);
+    k_scan_apply<<<tiles, kScanBlock, 0, s>>>(count, start, m, tile_sum);
+}
+
 }  // namespace
 
 extern "C" {
@@ -348,15 +405,16 @@ int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_bo
     float4* off32 = (float4*)w;
 
     if (cudaMemsetAsync(count, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
-    if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
     const int gb = grid_for(n, kBlock);
     k_bin<<<gb, kBlock, 0, s>>>(*src, d_box, cell_rank, old_cell, count, d_status);
-    k_scan<<<1, kScanBlock, 0, s>>>(count, start, m);
+    scan_cells(count, start, fill, m, s);
+    // `fill` held the scan's tile totals; the scatter counts in it from zero
+    if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
     k_scatter<<<gb, kBlock, 0, s>>>(n, cell_rank, old_cell, start, fill, order);
     k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
     k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, d_box, order, old_cell, cell_of, off32);
     k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, off32, d_status);
-    note_launches(6);
+    note_launches(7);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 
@@ -434,14 +492,15 @@ extern "C" int tmps_nlist_build_noalloc(const tmps_atoms* src, const tmps_atoms*
     const int m = ncell;
     // the previous call left its counts behind: both counters must start at zero
     if (cudaMemsetAsync(count, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
-    if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
     const int gb = grid_for(n, kBlock);
     k_bin<<<gb, kBlock, 0, s>>>(*src, d_box, cell_rank, old_cell, count, d_status);
-    k_scan<<<1, kScanBlock, 0, s>>>(count, start, m);
+    scan_cells(count, start, fill, m, s);
+    // `fill` held the scan's tile totals; the scatter counts in it from zero
+    if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
     k_scatter<<<gb, kBlock, 0, s>>>(n, cell_rank, old_cell, start, fill, order);
     k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
     k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, d_box, order, old_cell, cell_of, nullptr);
     k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, nullptr, d_status);
-    note_launches(6);
+    note_launches(7);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }

@@ -226,10 +226,12 @@ class FusedEngine:
         _lib.check(rc, "tmps_mixed_history")
         self._hist_dw = dw
 
-    def _launch_step(self, L, st, atoms, nl_struct, params) -> None:
+    def _launch_step(self, L, st, atoms, nl_struct, params, chained: bool = False) -> None:
+        """One step's launches; `chained`: the previous launch on the stream was this engine's S (a
+        step of the same chunk), which lets A start its loads before its dependency wait."""
         dbox, eng = self.sim.domain.dbox, self._eng.data_ptr()
         with _device.timed("fused_a"):
-            rc = L.tmps_fused_a(atoms, dbox, eng, self.a_blocks, self.part.data_ptr(), st)
+            rc = L.tmps_fused_a(atoms, dbox, eng, self.a_blocks, self.part.data_ptr(), 1 if chained else 0, st)
         _lib.check(rc, "tmps_fused_a")
         with _device.timed("fused_c"):
             rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.c_blocks, self.part.data_ptr(), st)
@@ -277,8 +279,8 @@ class FusedEngine:
             if self.graphs and count == self.chunk and _device.TIMED is None:
                 self._replay_chunk(L, atoms, nl_struct, params)
             else:
-                for _ in range(count):
-                    self._launch_step(L, st, atoms, nl_struct, params)
+                for k in range(count):
+                    self._launch_step(L, st, atoms, nl_struct, params, chained=k > 0)
             self._check_status()
         sim.timestep = target
 
@@ -292,8 +294,8 @@ class FusedEngine:
 
             def chunk():
                 st = _device.stream()
-                for _ in range(self.chunk):
-                    self._launch_step(L, st, atoms, nl_struct, params)
+                for k in range(self.chunk):
+                    self._launch_step(L, st, atoms, nl_struct, params, chained=k > 0)
 
             self._graph, self._graph_key = _device.capture_graph(chunk), key
         self._graph.replay()

@@ -248,7 +248,7 @@ def tile_packing(cell: dict, reps=(4, 4, 4)) -> dict:
 # The contact-dense counterpart of the 1M-sphere servo run: a 15,625-sphere
 # cell compressed to p = 1 with the run's own contact law, tiled 4 x 4 x 4.
 DENSE_CELL_FILE = "dense_cell_hertz2e5_15625.npz"
-DENSE_CELL_ARGS = dict(n=15625, seed=11, kn=2.0e5, dt=2.5e-4, max_rate=0.005, cycles=100, relax_cycles=10,
+DENSE_CELL_ARGS = dict(n=15625, seed=11, kn=2.0e5, dt=2.5e-4, max_rate=0.005, cycles=100, relax_cycles=40,
                        cycle_steps=2000, precision="mixed")
 
 

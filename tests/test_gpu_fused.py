@@ -57,7 +57,9 @@ def test_mixed_matches_oracle_within_stated_error(gpu, oracle):
     assert rel_err(g["v"], o["v"]) < MIXED_V, rel_err(g["v"], o["v"])
     assert rel_err(g["f"], o["f"]) < MIXED_F, rel_err(g["f"], o["f"])
     assert rel_err(g["torque"], o["torque"]) < MIXED_F, rel_err(g["torque"], o["torque"])
-    assert rel_err(sim.fixes[-1].last_pressure(), osim.last_pressure) < MIXED_P
+    ep = rel_err(sim.fixes[-1].last_pressure(), osim.last_pressure)
+    print(f"mixed vs oracle after 60 servo steps: pressure {ep:.2e}, f {rel_err(g['f'], o['f']):.2e}")
+    assert ep < MIXED_P, ep
     np.testing.assert_allclose(sim.domain.prd, osim.domain.prd, rtol=1e-12)
 
 
@@ -204,9 +206,12 @@ def test_pressure_record_each_step(gpu, oracle, precision):
     assert np.isfinite(rows).all() and np.abs(rows).max() > 0
     tol = 1e-10 if precision == "fp64" else MIXED_P
     osim.run(62)
+    errs = []
     for k, s in enumerate(range(63, 71)):
         osim.step()
-        assert rel_err(rows[k], osim.last_pressure) < tol, (s, rel_err(rows[k], osim.last_pressure))
+        errs.append(rel_err(rows[k], osim.last_pressure))
+        assert errs[-1] < tol, (s, errs[-1])
+    print(f"{precision} pressure record vs oracle, steps 63-70: max {max(errs):.2e}")
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -302,7 +307,9 @@ def test_triaxial_loading_matches_oracle(gpu, oracle, precision):
     oq = np.array(oq)
     assert np.abs(oq).max() > 0
     tol = 1e-10 if precision == "fp64" else MIXED_P
-    assert np.abs(q - oq).max() / np.abs(oq).max() < tol, np.abs(q - oq).max() / np.abs(oq).max()
+    eq = np.abs(q - oq).max() / np.abs(oq).max()
+    print(f"{precision} triaxial q vs oracle over 120 steps: {eq:.2e}")
+    assert eq < tol, eq
     sim.domain.pull()
     np.testing.assert_allclose(np.array(sim.domain.boxhi) - np.array(sim.domain.boxlo), osim.domain.prd,
                                rtol=1e-12 if precision == "fp64" else 1e-9)

@@ -63,6 +63,8 @@ def test_long_run_matches_oracle(gpu, oracle, oracle_run, precision):
     pg = np.mean(rows[-500:, :3])
     po = np.mean(o["press"][-500:])
     tol_p = 1e-8 if precision == "fp64" else 1e-5
+    print(f"{precision} long run: mean pressure over the last 500 steps vs oracle {abs(pg - po) / abs(po):.2e}, "
+          f"box strain {np.abs(strain_g - strain_o).max() / np.abs(strain_o).max():.2e}")
     assert abs(pg - po) <= tol_p * abs(po), (pg, po)
     # coordination number at the end
     cn = ComputeContactAtom(max_atoms=len(o["x"])).compute(sim.atom, sim.domain, sim.neighbor)
