@@ -423,9 +423,13 @@ int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32
  * caller memory: flag words, per-group and per-atom gaps, then the
  * d_eng->nblocks virial partial sums, A's blocks then C's).  c_blocks: C's
  * grid from tmps_fused_shape, or <= 0 for the default; d_eng->nblocks must be
- * A's blocks + C's blocks of the same shape. */
+ * A's blocks + C's blocks of the same shape.  rows != 0 takes the per-atom-row
+ * path instead: every atom's row, one thread per atom, no group ruled out --
+ * for contact-dense states, where the screen rules out almost nothing.  Both
+ * paths sum each atom's contacts in slot order and keep the flag words'
+ * meaning, so they may alternate between builds. */
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
-                 const tmps_pair_params* p, int32_t c_blocks, void* scratch, void* stream);
+                 const tmps_pair_params* p, int32_t c_blocks, void* scratch, int32_t rows, void* stream);
 
 /* Launch S: rebuild decision, virial total (from C's scratch), servo. */
 int tmps_fused_servo(tmps_box* d_box, tmps_servo* d_servo, tmps_engine* d_eng, const void* scratch,

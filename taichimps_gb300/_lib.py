@@ -210,7 +210,7 @@ _SIGS = {
                                   ctypes.POINTER(PairParams), c_i32, c_vp, c_vp]),
     "tmps_fused_a": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
     "tmps_fused_c": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
-                             ctypes.POINTER(PairParams), c_i32, c_vp, c_vp]),
+                             ctypes.POINTER(PairParams), c_i32, c_vp, c_i32, c_vp]),
     "tmps_fused_servo": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "tmps_fused_blocks": (c_i32, [c_i32, c_i32, c_i32]),
     "tmps_probe_fp64": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp]),

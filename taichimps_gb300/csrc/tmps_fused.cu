@@ -609,7 +609,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-template <int STYLE, bool MIXED>
+template <int STYLE, bool MIXED, bool DENSE>
 __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L, const tmps_pair_params& P,
                                         const tmps_box* __restrict__ B, tmps_engine* __restrict__ E,
                                         uint32_t* __restrict__ flags, const float* __restrict__ gap,
@@ -619,12 +619,13 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
     using T = typename std::conditional<MIXED, float, double>::type;
     // histories: doubles in the FP64 form, FP32 double words in the mixed form
     using HT = typename std::conditional<MIXED, DW, double>::type;
+    using S4 = typename std::conditional<MIXED, float4, double4>::type;  // a state word
     __shared__ double smem[6 * (kBlockC / 32)];
     __shared__ uint32_t cwords[kBlockC / 32][kLive];
     // the kLive groups of the batch in hand: group, old and near words (warp-uniform)
     __shared__ int32_t bgrp[kBlockC / 32][kLive];
     __shared__ uint32_t bold[kBlockC / 32][kLive], bnear[kBlockC / 32][kLive];
-    __shared__ CfWarp<MIXED> cwarp[kBlockC / 32];
+    __shared__ CfWarp<MIXED> cwarp[DENSE ? 1 : kBlockC / 32];
     pdl_enter();
     if (E->aborted || E->step >= E->stop_step) return;
     const int64_t s = E->step + 1;
@@ -683,7 +684,7 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
     double Vd[6] = {0, 0, 0, 0, 0, 0};
     float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};  // mixed: per-thread double words
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    CfWarp<MIXED>& W = cwarp[wib];
+    CfWarp<MIXED>& W = cwarp[DENSE ? 0 : wib];
     const int ngroups = (n + 31) >> 5;
     const int nwarps = (nblk * blockDim.x) >> 5;
     const size_t ss = (size_t)L.slots * n;
@@ -696,6 +697,234 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
         const float md = sqrtf(__uint_as_float(E->maxd2_bits));
         thr = ((2.0f * md) * 1.0001f + E->shift_bound) + E->cull_tol;
     }
+
+    // The contact of row atom ia (its state words Pi, PLi (mixed: low words and
+    // radius lo), Vi, Wi and packed cell Ci) with the partner of row entry e at
+    // slot k (its high position word Pj), `was` its touch bit: whether they
+    // touch, and if so the row atom's force, torque and pair virial terms in
+    // fc, tc, vc; the contact's history is updated in place.  Every other load
+    // of the contact is issued here together (one round trip).
+    auto contact_core = [&](const int ia, const int e, const int k, const bool was, const S4 Pi, const float4 PLi,
+                            const S4 Vi, const S4 Wi, const int32_t Ci, const S4 Pj, T (&fc)[3], T (&tc)[3],
+                            T (&vc)[6]) -> bool {
+        (void)PLi;
+        (void)Ci;
+        const int j = e & kNbrIndexMask;
+        const bool lo = ia < j;
+        const size_t so = (size_t)k * n + ia;
+        // every load of the contact at once: one round trip
+        T xi[3], xj[3], ri, rj;
+        int32_t ci = 0, cj = 0;
+        float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
+        T vi[3], wi[3], mi, vj[3], wj[3], mj;
+        HT shr[3] = {}, rlr[3] = {};
+        if constexpr (MIXED) {
+            const float4 pi = Pi, pj = Pj;
+            il = PLi;
+            jl = ld4f(A.pos32lo, j);
+            const float4 v = Vi, w = Wi;
+            const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
+            if (vremap) {
+                ci = Ci;
+                cj = A.cell32[j];
+            }
+            xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+            xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+            vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+            wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+        } else {
+            const double4 pi = Pi, pj = Pj;
+            const double4 v = Vi, w = Wi;
+            const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
+            xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
+            xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
+            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
+            wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
+            vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
+            wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
+        }
+        if (hist && was) {
+            const HT* hs = reinterpret_cast<const HT*>(L.shear);
+            shr[0] = hs[so];
+            shr[1] = hs[ss + so];
+            shr[2] = hs[2 * ss + so];
+            if (roll) {
+                const HT* hr = reinterpret_cast<const HT*>(L.rolling);
+                rlr[0] = hr[so];
+                rlr[1] = hr[ss + so];
+                rlr[2] = hr[2 * ss + so];
+            }
+        }
+        // separation x_i - x_j
+        T d[3];
+        T nimg[3] = {0, 0, 0};
+        const int code = (unsigned)e >> kNbrIndexBits;
+        float offh[3] = {0.f, 0.f, 0.f}, offl[3] = {0.f, 0.f, 0.f};
+        if constexpr (MIXED) {
+            const float4 so = soff[code], sl = sofl[code];
+            offh[0] = so.x; offh[1] = so.y; offh[2] = so.z;
+            offl[0] = sl.x; offl[1] = sl.y; offl[2] = sl.z;
+            // offsets are relative to each atom's own cell: j's cell is
+            // the stencil offset (ox, oy, oz) away from i's, so
+            // x_i - x_j = (o_i - o_j) - offset * h
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                d[c] = (xi[c] - xj[c]) - offh[c];
+                if (single[c]) {
+                    nimg[c] = rintf(d[c] * iprd[c]);
+                    d[c] -= nimg[c] * prd[c];
+                }
+            }
+            if (vremap) {  // image count for the partner velocity shift
+                const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+                const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
+                                   cell_z(ci) + off[2] - cell_z(cj)};
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / gdim[c]);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                d[c] = xi[c] - xj[c];
+                if (per[c] == 1) {
+                    nimg[c] = rint(d[c] * iprd[c]);
+                    d[c] = image_sub64(d[c], nimg[c], prd[c]);
+                }
+            }
+        }
+        PairIn<T> in;
+        const T sg = lo ? T(1) : T(-1);
+        in.ra = lo ? ri : rj;
+        in.rb = lo ? rj : ri;
+        bool near;
+        if constexpr (MIXED) {
+            // separation, |d|^2, |d| and the overlap from the high and
+            // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
+            // FP32 difference of two unit-size numbers keeps 2^-24)
+            const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
+            float dh[3], dl[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float s1, e1, s2, e2;
+                two_sum(xi[c], -xj[c], s1, e1);
+                two_sum(s1, -offh[c], s2, e2);
+                const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), offl[c]), __fadd_rn(e1, e2));
+                two_sum(s2, low, dh[c], dl[c]);
+                if (single[c]) {
+                    const float ni = rintf(dh[c] * iprd[c]);
+                    float s3, e3;
+                    two_sum(dh[c], -ni * prd[c], s3, e3);
+                    two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * prdlo[c]), e3), dh[c], dl[c]);
+                }
+                dh[c] = sg * dh[c];
+                dl[c] = sg * dl[c];
+            }
+            // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
+            float pp[3], pe[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                pp[c] = __fmul_rn(dh[c], dh[c]);
+                pe[c] = __fmaf_rn(dh[c], dh[c], -pp[c]);
+            }
+            float t1, te1, rh, re;
+            two_sum(pp[0], pp[1], t1, te1);
+            two_sum(t1, pp[2], rh, re);
+            const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]),
+                                                                    __fmul_rn(dh[1], dl[1])),
+                                                         __fmul_rn(dh[2], dl[2])));
+            const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])),
+                                        cross);
+            float rsh, rsl;
+            two_sum(rh, rl0, rsh, rsl);
+            // r_hi need not be the rounded root: the residual rsh - r_hi^2 (one FMA,
+            // within an ulp of exact for an r_hi a few ulp off) corrects it in r_lo
+            const float r_hi = lsqrt(rsh);
+            const float res = __fmaf_rn(-r_hi, r_hi, rsh);
+            const float r_lo = __fdividef(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
+            // ra + rb, both words
+            const float4 al = lo ? il : jl, bl = lo ? jl : il;
+            float sh_, se_;
+            two_sum(in.ra, in.rb, sh_, se_);
+            const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
+            const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
+            near = delta > 0.0f && rsh > 1e-28f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
+            in.rsq = rsh;
+            in.r = r_hi;
+            in.delta = delta;
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
+            in.rsq = rsq64(in.d);
+            const T radsum = in.ra + in.rb;
+            near = in.rsq < __dmul_rn(radsum, radsum) && in.rsq > T(1e-28);
+            if (near) {
+                in.r = sqrt(in.rsq);
+                in.delta = radsum - in.r;
+            }
+        }
+        if (near) {
+            T dv[3] = {0, 0, 0};
+            if (vremap) {
+                // image count of x_a - x_b, then n . h_rate for partner b
+                T na[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
+                dv[0] = (na[0] * hrate[0] + na[1] * hshear[2]) + na[2] * hshear[1];
+                dv[1] = na[1] * hrate[1] + na[2] * hshear[0];
+                dv[2] = na[2] * hrate[2];
+            }
+            in.ma = lo ? mi : mj;
+            in.mb = lo ? mj : mi;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                in.va[c] = lo ? vi[c] : vj[c];
+                in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
+                in.wa[c] = lo ? wi[c] : wj[c];
+                in.wb[c] = lo ? wj[c] : wi[c];
+            }
+            HT sh[3] = {}, rl[3] = {};
+            if (hist && was) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    sh[c] = hsign(shr[c], lo);
+                    rl[c] = hsign(rlr[c], lo);
+                }
+            }
+            PairOut<T> out;
+            if constexpr (MIXED) contact_law<T, STYLE>(sP, dt, 1, in, sh, rl, out);
+            else contact_law<T, STYLE>(P, dt, 1, in, sh, rl, out);
+            if (hist) {
+                HT* hs = reinterpret_cast<HT*>(L.shear);
+                hs[so] = hsign(sh[0], lo);
+                hs[ss + so] = hsign(sh[1], lo);
+                hs[2 * ss + so] = hsign(sh[2], lo);
+                if (roll) {
+                    HT* hr = reinterpret_cast<HT*>(L.rolling);
+                    hr[so] = hsign(rl[0], lo);
+                    hr[ss + so] = hsign(rl[1], lo);
+                    hr[2 * ss + so] = hsign(rl[2], lo);
+                }
+            }
+            const T arm = lo ? out.arm_a : out.arm_b;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                fc[c] = sg * out.f[c];
+                tc[c] = arm * out.tor[c] + sg * out.troll[c];
+            }
+            vc[0] = T(0.5) * (in.d[0] * out.f[0]);
+            vc[1] = T(0.5) * (in.d[1] * out.f[1]);
+            vc[2] = T(0.5) * (in.d[2] * out.f[2]);
+            vc[3] = T(0.5) * (in.d[0] * out.f[1]);
+            vc[4] = T(0.5) * (in.d[0] * out.f[2]);
+            vc[5] = T(0.5) * (in.d[1] * out.f[2]);
+        }
+        return near;
+    };
 
     // 4. the contact law for `cnt` (<= 32) queued contacts from ring position
     // qhead, one per lane, and their in-order reduction onto the roster atoms
@@ -714,222 +943,13 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
         T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
         if (live) {
             const int ia = W.idx[a];
-            const int j = e & kNbrIndexMask;
-            const bool lo = ia < j;
             const bool was = ((W.touch[a] >> k) & 1ull) != 0;
-            const size_t so = (size_t)k * n + ia;
-            // every load of the contact at once: one round trip
-            T xi[3], xj[3], ri, rj;
-            int32_t ci = 0, cj = 0;
-            float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
-            T vi[3], wi[3], mi, vj[3], wj[3], mj;
-            HT shr[3] = {}, rlr[3] = {};
-            if constexpr (MIXED) {
-                const float4 pi = W.p[a], pj = W.qp[slot];
-                il = W.pl[a];
-                jl = ld4f(A.pos32lo, j);
-                const float4 v = W.v[a], w = W.w[a];
-                const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
-                if (vremap) {
-                    ci = W.cell[a];
-                    cj = A.cell32[j];
-                }
-                xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
-                xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
-                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-            } else {
-                const double4 pi = W.p[a], pj = ld4(A.xr, j);
-                const double4 v = W.v[a], w = W.w[a];
-                const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
-                xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
-                xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
-                vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
-                wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
-                vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
-                wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-            }
-            if (hist && was) {
-                const HT* hs = reinterpret_cast<const HT*>(L.shear);
-                shr[0] = hs[so];
-                shr[1] = hs[ss + so];
-                shr[2] = hs[2 * ss + so];
-                if (roll) {
-                    const HT* hr = reinterpret_cast<const HT*>(L.rolling);
-                    rlr[0] = hr[so];
-                    rlr[1] = hr[ss + so];
-                    rlr[2] = hr[2 * ss + so];
-                }
-            }
-            // separation x_i - x_j
-            T d[3];
-            T nimg[3] = {0, 0, 0};
-            const int code = (unsigned)e >> kNbrIndexBits;
-            float offh[3] = {0.f, 0.f, 0.f}, offl[3] = {0.f, 0.f, 0.f};
-            if constexpr (MIXED) {
-                const float4 so = soff[code], sl = sofl[code];
-                offh[0] = so.x; offh[1] = so.y; offh[2] = so.z;
-                offl[0] = sl.x; offl[1] = sl.y; offl[2] = sl.z;
-                // offsets are relative to each atom's own cell: j's cell is
-                // the stencil offset (ox, oy, oz) away from i's, so
-                // x_i - x_j = (o_i - o_j) - offset * h
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    d[c] = (xi[c] - xj[c]) - offh[c];
-                    if (single[c]) {
-                        nimg[c] = rintf(d[c] * iprd[c]);
-                        d[c] -= nimg[c] * prd[c];
-                    }
-                }
-                if (vremap) {  // image count for the partner velocity shift
-                    const int off[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
-                    const int cc[3] = {cell_x(ci) + off[0] - cell_x(cj), cell_y(ci) + off[1] - cell_y(cj),
-                                       cell_z(ci) + off[2] - cell_z(cj)};
-#pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        if (!single[c] && per[c] == 1) nimg[c] = (T)(cc[c] / gdim[c]);
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    d[c] = xi[c] - xj[c];
-                    if (per[c] == 1) {
-                        nimg[c] = rint(d[c] * iprd[c]);
-                        d[c] = image_sub64(d[c], nimg[c], prd[c]);
-                    }
-                }
-            }
-            PairIn<T> in;
-            const T sg = lo ? T(1) : T(-1);
-            in.ra = lo ? ri : rj;
-            in.rb = lo ? rj : ri;
-            bool near;
-            if constexpr (MIXED) {
-                // separation, |d|^2, |d| and the overlap from the high and
-                // low FP32 words, so the overlap keeps ~2^-48 of |d| (an
-                // FP32 difference of two unit-size numbers keeps 2^-24)
-                const float xil[3] = {il.x, il.y, il.z}, xjl[3] = {jl.x, jl.y, jl.z};
-                float dh[3], dl[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    float s1, e1, s2, e2;
-                    two_sum(xi[c], -xj[c], s1, e1);
-                    two_sum(s1, -offh[c], s2, e2);
-                    const float low = __fadd_rn(__fsub_rn(__fsub_rn(xil[c], xjl[c]), offl[c]), __fadd_rn(e1, e2));
-                    two_sum(s2, low, dh[c], dl[c]);
-                    if (single[c]) {
-                        const float ni = rintf(dh[c] * iprd[c]);
-                        float s3, e3;
-                        two_sum(dh[c], -ni * prd[c], s3, e3);
-                        two_sum(s3, __fadd_rn(__fsub_rn(dl[c], ni * prdlo[c]), e3), dh[c], dl[c]);
-                    }
-                    dh[c] = sg * dh[c];
-                    dl[c] = sg * dl[c];
-                }
-                // |d|^2 = sum hi^2 (exact via FMA) + 2 hi lo
-                float pp[3], pe[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    pp[c] = __fmul_rn(dh[c], dh[c]);
-                    pe[c] = __fmaf_rn(dh[c], dh[c], -pp[c]);
-                }
-                float t1, te1, rh, re;
-                two_sum(pp[0], pp[1], t1, te1);
-                two_sum(t1, pp[2], rh, re);
-                const float cross = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(dh[0], dl[0]),
-                                                                        __fmul_rn(dh[1], dl[1])),
-                                                             __fmul_rn(dh[2], dl[2])));
-                const float rl0 = __fadd_rn(__fadd_rn(__fadd_rn(te1, re), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2])),
-                                            cross);
-                float rsh, rsl;
-                two_sum(rh, rl0, rsh, rsl);
-                // r_hi need not be the rounded root: the residual rsh - r_hi^2 (one FMA,
-                // within an ulp of exact for an r_hi a few ulp off) corrects it in r_lo
-                const float r_hi = lsqrt(rsh);
-                const float res = __fmaf_rn(-r_hi, r_hi, rsh);
-                const float r_lo = __fdividef(__fadd_rn(res, rsl), __fmul_rn(2.0f, r_hi));
-                // ra + rb, both words
-                const float4 al = lo ? il : jl, bl = lo ? jl : il;
-                float sh_, se_;
-                two_sum(in.ra, in.rb, sh_, se_);
-                const float rad_lo = __fadd_rn(__fadd_rn(al.w, bl.w), se_);
-                const float delta = __fadd_rn(__fsub_rn(sh_, r_hi), __fsub_rn(rad_lo, r_lo));
-                near = delta > 0.0f && rsh > 1e-28f;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) in.d[c] = dh[c];
-                in.rsq = rsh;
-                in.r = r_hi;
-                in.delta = delta;
-            } else {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) in.d[c] = sg * d[c];
-                in.rsq = rsq64(in.d);
-                const T radsum = in.ra + in.rb;
-                near = in.rsq < __dmul_rn(radsum, radsum) && in.rsq > T(1e-28);
-                if (near) {
-                    in.r = sqrt(in.rsq);
-                    in.delta = radsum - in.r;
-                }
-            }
-            if (near) {
-                contact = true;
-                T dv[3] = {0, 0, 0};
-                if (vremap) {
-                    // image count of x_a - x_b, then n . h_rate for partner b
-                    T na[3];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) na[c] = sg * nimg[c];
-                    dv[0] = (na[0] * hrate[0] + na[1] * hshear[2]) + na[2] * hshear[1];
-                    dv[1] = na[1] * hrate[1] + na[2] * hshear[0];
-                    dv[2] = na[2] * hrate[2];
-                }
-                in.ma = lo ? mi : mj;
-                in.mb = lo ? mj : mi;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    in.va[c] = lo ? vi[c] : vj[c];
-                    in.vb[c] = (lo ? vj[c] : vi[c]) + dv[c];
-                    in.wa[c] = lo ? wi[c] : wj[c];
-                    in.wb[c] = lo ? wj[c] : wi[c];
-                }
-                HT sh[3] = {}, rl[3] = {};
-                if (hist && was) {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        sh[c] = hsign(shr[c], lo);
-                        rl[c] = hsign(rlr[c], lo);
-                    }
-                }
-                PairOut<T> out;
-                if constexpr (MIXED) contact_law<T, STYLE>(sP, dt, 1, in, sh, rl, out);
-                else contact_law<T, STYLE>(P, dt, 1, in, sh, rl, out);
-                if (hist) {
-                    HT* hs = reinterpret_cast<HT*>(L.shear);
-                    hs[so] = hsign(sh[0], lo);
-                    hs[ss + so] = hsign(sh[1], lo);
-                    hs[2 * ss + so] = hsign(sh[2], lo);
-                    if (roll) {
-                        HT* hr = reinterpret_cast<HT*>(L.rolling);
-                        hr[so] = hsign(rl[0], lo);
-                        hr[ss + so] = hsign(rl[1], lo);
-                        hr[2 * ss + so] = hsign(rl[2], lo);
-                    }
-                }
-                const T arm = lo ? out.arm_a : out.arm_b;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    fc[c] = sg * out.f[c];
-                    tc[c] = arm * out.tor[c] + sg * out.troll[c];
-                }
-                vc[0] = T(0.5) * (in.d[0] * out.f[0]);
-                vc[1] = T(0.5) * (in.d[1] * out.f[1]);
-                vc[2] = T(0.5) * (in.d[2] * out.f[2]);
-                vc[3] = T(0.5) * (in.d[0] * out.f[1]);
-                vc[4] = T(0.5) * (in.d[0] * out.f[2]);
-                vc[5] = T(0.5) * (in.d[1] * out.f[2]);
-            }
+            if constexpr (MIXED)
+                contact = contact_core(ia, e, k, was, W.p[a], W.pl[a], W.v[a], W.w[a], vremap ? W.cell[a] : 0,
+                                       W.qp[slot], fc, tc, vc);
+            else
+                contact = contact_core(ia, e, k, was, W.p[a], make_float4(0.f, 0.f, 0.f, 0.f), W.v[a], W.w[a], 0,
+                                       ld4(A.xr, e & kNbrIndexMask), fc, tc, vc);
         }
         if (contact) atomicOr(reinterpret_cast<unsigned long long*>(&W.ntouch[a]), 1ull << k);
         if constexpr (MIXED) {
@@ -1195,6 +1215,162 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
         }
     };
 
+    if constexpr (DENSE) {
+        // Per-atom rows (the contact-dense path): every atom, one lane each,
+        // whole 32-atom groups per warp.  Its row entries are loaded four at a
+        // time (coalesced over the lanes) with their partners' high position
+        // words, and the near test (the screened path's, word for word) marks
+        // the near slots; the contacts of the near slots then run in ascending
+        // slot order, each lane on its own atom, summed into the atom's force,
+        // torque and virial in that order -- the sums the screened path forms
+        // for the same atom.  Nothing is staged in shared memory and no group
+        // is ruled out, which suits a state where nearly every atom touches.
+        for (int base = bid * (int)blockDim.x + (int)(threadIdx.x & ~31u); base < n; base += nblk * (int)blockDim.x) {
+            const int i = base + lane;
+            const bool mine = i < n;
+            S4 Pi{}, Vi{}, Wi{};
+            float4 PLi = make_float4(0.f, 0.f, 0.f, 0.f);
+            int32_t Ci = 0;
+            int nn = 0;
+            uint64_t touch = 0ull;
+            if (mine) {
+                nn = L.nnb[i];
+                if (hist) touch = L.touch[i];
+                if constexpr (MIXED) {
+                    Pi = ld4f(A.pos32, i);
+                    PLi = ld4f(A.pos32lo, i);
+                    Vi = ld4f(A.vel32, i);
+                    Wi = ld4f(A.om32, i);
+                    if (vremap) Ci = A.cell32[i];
+                } else {
+                    Pi = ld4(A.xr, i);
+                    Vi = ld4(A.vm, i);
+                    Wi = ld4(A.om, i);
+                }
+            }
+            const uint32_t old = flags[base >> 5];
+            // near test of the row, four entries at a time
+            uint64_t nmask = 0ull;
+            for (int k0 = 0; k0 < nn; k0 += 4) {
+                int ee[4];
+                S4 pj[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) ee[u] = k0 + u < nn ? L.nbr[(size_t)(k0 + u) * n + i] : 0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (k0 + u < nn) {
+                        if constexpr (MIXED) pj[u] = ld4f(A.pos32, ee[u] & kNbrIndexMask);
+                        else pj[u] = ld4(A.xr, ee[u] & kNbrIndexMask);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (k0 + u >= nn) continue;
+                    bool nr;
+                    if constexpr (MIXED) {
+                        const float4 so = soff[(unsigned)ee[u] >> kNbrIndexBits];
+                        const float xi[3] = {Pi.x, Pi.y, Pi.z}, xj[3] = {pj[u].x, pj[u].y, pj[u].z};
+                        const float oh[3] = {so.x, so.y, so.z};
+                        float d[3];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            d[c] = (xi[c] - xj[c]) - oh[c];
+                            if (single[c]) d[c] -= rintf(d[c] * iprd[c]) * prd[c];
+                        }
+                        const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+                        const float rs = (Pi.w + pj[u].w) * 1.00001f;
+                        nr = rq < rs * rs;
+                    } else {
+                        double d[3] = {Pi.x - pj[u].x, Pi.y - pj[u].y, Pi.z - pj[u].z};
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            if (per[c] == 1) d[c] = image_sub64(d[c], rint(d[c] * iprd[c]), prd[c]);
+                        const double rsq = rsq64(d);
+                        const double radsum = Pi.w + pj[u].w;
+                        nr = rsq < __dmul_rn(radsum, radsum) && rsq > 1e-28;
+                    }
+                    if (nr) nmask |= 1ull << (k0 + u);
+                }
+            }
+            // the near slots' contacts in ascending slot order
+            T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
+            uint64_t nt = 0ull;
+            for (uint64_t m = nmask; m; m &= m - 1ull) {
+                const int k = __ffsll((long long)m) - 1;
+                const int e = L.nbr[(size_t)k * n + i];
+                S4 Pj;
+                if constexpr (MIXED) Pj = ld4f(A.pos32, e & kNbrIndexMask);
+                else Pj = ld4(A.xr, e & kNbrIndexMask);
+                T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
+                if (contact_core(i, e, k, ((touch >> k) & 1ull) != 0, Pi, PLi, Vi, Wi, Ci, Pj, fc, tc, vc))
+                    nt |= 1ull << k;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    F[c] += fc[c];
+                    Tq[c] += tc[c];
+                }
+#pragma unroll
+                for (int c = 0; c < 6; ++c) V[c] += vc[c];
+            }
+            // finish the atom (the screened path's step 5)
+            if (mine) {
+                if (hist && nt != touch) L.touch[i] = nt;
+                if (nmask != 0ull) {
+                    const T vi[3] = {Vi.x, Vi.y, Vi.z}, wi[3] = {Wi.x, Wi.y, Wi.z};
+                    const T mi = Vi.w;
+                    if (E->cundall) {  // FixDampingCundall.post_force_kernel
+                        T gl, ga;
+                        if constexpr (MIXED) {
+                            gl = E->gamma_lin32;
+                            ga = E->gamma_ang32;
+                        } else {
+                            gl = E->gamma_lin;
+                            ga = E->gamma_ang;
+                        }
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            const T sf = F[c] * vi[c] >= T(0) ? T(1) : T(-1);
+                            F[c] *= T(1) - gl * sf;
+                            const T st = Tq[c] * wi[c] >= T(0) ? T(1) : T(-1);
+                            Tq[c] *= T(1) - ga * st;
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        if constexpr (MIXED) {
+                            A.f32[c * n + i] = F[c];
+                            A.torque32[c * n + i] = Tq[c];
+                        } else {
+                            A.f[c * n + i] = F[c];
+                            A.torque[c * n + i] = Tq[c];
+                        }
+                    }
+                    T im;
+                    if constexpr (MIXED) im = __fdividef(1.0f, mi);
+                    else im = A.rinv[i];
+                    const T hdt = T(0.5) * dt;
+                    T vf[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) vf[c] = vi[c] + hdt * (F[c] * im);
+                    const T kin[6] = {(mi * vf[0]) * vf[0], (mi * vf[1]) * vf[1], (mi * vf[2]) * vf[2],
+                                      (mi * vf[0]) * vf[1], (mi * vf[0]) * vf[2], (mi * vf[1]) * vf[2]};
+                    const T kh[6] = {(mi * vi[0]) * vi[0], (mi * vi[1]) * vi[1], (mi * vi[2]) * vi[2],
+                                     (mi * vi[0]) * vi[1], (mi * vi[0]) * vi[2], (mi * vi[1]) * vi[2]};
+                    if constexpr (MIXED) {
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) dw_add(Vh[c], Vl[c], V[c] + (kin[c] - kh[c]));
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) Vd[c] += (V[c] + kin[c]) - kh[c];
+                    }
+                }
+            }
+            // the group's new flag word; stale forces of atoms no longer flagged
+            const uint32_t w = __ballot_sync(0xffffffffu, mine && nmask != 0ull);
+            if (lane == 0 && w != old) flags[base >> 5] = w;
+            if (mine && ((old >> lane) & 1u) && !((w >> lane) & 1u)) zero_force<MIXED>(A, i);
+        }
+    } else {
     if (lane < kLive) cwords[wib][lane] = 0u;
     __syncwarp();
     // Ordered pass: after the first pass that follows the bounds (which
@@ -1301,6 +1477,7 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
             __syncwarp();
         }
     }
+    }  // screened path
     if constexpr (MIXED) {
         block_sum_dw<6, kBlockC>(Vh, Vl, reinterpret_cast<float2*>(smem));
         if (threadIdx.x == 0) {
@@ -1317,13 +1494,13 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
     if (threadIdx.x == 0 && bid == 0) E->final_pending = 1;
 }
 
-template <int STYLE, bool MIXED>
+template <int STYLE, bool MIXED, bool DENSE = false>
 __global__ void __launch_bounds__(kBlockC, MIXED ? 4 : 3)
     k_cf(tmps_atoms A, tmps_nlist L, tmps_pair_params P, const tmps_box* __restrict__ B,
          tmps_engine* __restrict__ E, uint32_t* __restrict__ flags, const float* __restrict__ gap,
          const float* __restrict__ agap, double* __restrict__ part) {
     const char* sc = reinterpret_cast<const char*>(flags);  // the scratch base
-    cf_body<STYLE, MIXED>(A, L, P, B, E, flags, gap, agap, reinterpret_cast<const int32_t*>(sc + lay_order(A.n)),
+    cf_body<STYLE, MIXED, DENSE>(A, L, P, B, E, flags, gap, agap, reinterpret_cast<const int32_t*>(sc + lay_order(A.n)),
                           reinterpret_cast<const float*>(sc + lay_sgap(A.n)), part, blockIdx.x, gridDim.x);
 }
 
@@ -1692,7 +1869,7 @@ __global__ void __launch_bounds__(kBlockC, MIXED ? 4 : 3)
     char* sc = static_cast<char*>(I.scratch);
     const int n = I.a.n;
     double* part = reinterpret_cast<double*>(sc + lay_part(n));
-    cf_body<STYLE, MIXED>(I.a, I.nl, I.p, I.box, I.eng, reinterpret_cast<uint32_t*>(sc),
+    cf_body<STYLE, MIXED, false>(I.a, I.nl, I.p, I.box, I.eng, reinterpret_cast<uint32_t*>(sc),
                           reinterpret_cast<const float*>(sc + lay_gap(n)), reinterpret_cast<const float*>(sc + lay_agap(n)),
                           reinterpret_cast<const int32_t*>(sc + lay_order(n)),
                           reinterpret_cast<const float*>(sc + lay_sgap(n)), part, (int)blockIdx.x - I.c_first,
@@ -2070,7 +2247,7 @@ int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32
 }
 
 int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_box, tmps_engine* d_eng,
-                 const tmps_pair_params* p, int32_t c_blocks, void* scratch, void* stream) {
+                 const tmps_pair_params* p, int32_t c_blocks, void* scratch, int32_t rows, void* stream) {
     if (!a || !nl || !d_box || !d_eng || !p || !scratch || a->n < 0 || nl->n != a->n) return TMPS_ERR_BAD_ARG;
     if (!a->pos32 && !a->rinv) return TMPS_ERR_BAD_ARG;
     if (p->style < 0 || p->style > 4 || nl->slots < 1 || nl->slots > kMaxSlots) return TMPS_ERR_BAD_ARG;
@@ -2087,8 +2264,12 @@ int tmps_fused_c(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box* d_bo
     double* part2 = (double*)((char*)scratch + part_offset(n));
     cudaStream_t s = (cudaStream_t)stream;
     if (mixed && !mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-#define TMPS_LAUNCH_C(ST)                                                                                    \
-    if (mixed) launch_pdl(k_cf<ST, true>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, flags, gap, agap, part2); \
+#define TMPS_LAUNCH_C(ST)                                                                                          \
+    if (mixed && rows) launch_pdl(k_cf<ST, true, true>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, flags, gap, agap, \
+                                  part2);                                                                        \
+    else if (mixed) launch_pdl(k_cf<ST, true>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, flags, gap, agap, part2); \
+    else if (rows) launch_pdl(k_cf<ST, false, true>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, flags, gap, agap,   \
+                              part2);                                                                            \
     else launch_pdl(k_cf<ST, false>, g2, kBlockC, s, *a, *nl, *p, d_box, d_eng, flags, gap, agap, part2);
     switch (p->style) {
         case 0: TMPS_LAUNCH_C(0) break;

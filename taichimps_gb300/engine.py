@@ -55,9 +55,14 @@ class FusedEngine:
     LAUNCHES_PER_STEP = 3
 
     def __init__(self, sim, precision: str = "fp64", chunk: int = 64, graphs: bool = True,
-                 cull: bool = True, launch_shape: tuple[int, int] | None = None) -> None:
+                 cull: bool = True, launch_shape: tuple[int, int] | None = None,
+                 contact_path: str | None = None) -> None:
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
+        if contact_path is None:
+            contact_path = getattr(sim, "contact_path", "auto")
+        if contact_path not in ("auto", "screened", "rows"):
+            raise ValueError("contact_path must be 'auto', 'screened' or 'rows'")
         # the Simulation keeps its last engine (Simulation.last_engine); the engine refers back
         # weakly, so a finished run's device memory goes with the Simulation instead of waiting
         # for the cycle collector
@@ -79,6 +84,13 @@ class FusedEngine:
         # C skips 32-atom groups whose gap bound rules out any contact (exact;
         # off screens every group, with bit-identical results)
         self.cull = bool(cull)
+        # C's path (tmps_fused_c): "screened" rules contact-free 32-atom groups out and runs the contacts
+        # of the rest 32 at a time; "rows" runs every atom's row, one thread per atom; "auto" picks rows
+        # at a build where more than half of the atoms touch or overlap at the build positions (their
+        # gap bound is <= 0), screened otherwise.  Both give the same forces (each atom's contacts summed
+        # in slot order); only the order of the virial partial sums differs.
+        self.contact_path = contact_path
+        self.rows = contact_path == "rows"
         # launch shape (tmps_fused_shape): 32-atom groups per warp of A and of C, 0 = the default grid;
         # it fixes the order of the virial sum, so equal shapes give bit-identical runs
         shape = getattr(sim, "launch_shape", (0, 0)) if launch_shape is None else launch_shape
@@ -214,6 +226,13 @@ class FusedEngine:
         rc = L.tmps_fused_bounds(atoms, sim.history.cstruct(nl), sim.domain.dbox, self._eng.data_ptr(),
                                  sim.pair_style.params, 1 if self.cull else 0, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_bounds")
+        if self.contact_path == "auto":
+            n = self._n
+            ng = (n + 31) // 32
+            r256 = lambda b: (b + 255) // 256 * 256
+            off = r256((ng + 1) * 4) + r256(ng * 4)  # scratch: flag words, group gaps, then the atom gaps
+            agap = self.part[off:off + 4 * n].view(torch.float32)
+            self.rows = n > 0 and int((agap <= 0).sum()) * 2 > n
         self._history_form(True)
 
     def _history_form(self, dw: bool) -> None:
@@ -234,7 +253,8 @@ class FusedEngine:
             rc = L.tmps_fused_a(atoms, dbox, eng, self.a_blocks, self.part.data_ptr(), 1 if chained else 0, st)
         _lib.check(rc, "tmps_fused_a")
         with _device.timed("fused_c"):
-            rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.c_blocks, self.part.data_ptr(), st)
+            rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.c_blocks, self.part.data_ptr(),
+                                1 if self.rows else 0, st)
         _lib.check(rc, "tmps_fused_c")
         with _device.timed("fused_s"):
             rc = L.tmps_fused_servo(dbox, self._servo_ptr(), eng, self.part.data_ptr(), self.status.data_ptr(), st)
@@ -288,7 +308,7 @@ class FusedEngine:
         """One chunk of steps as a CUDA graph (captured on first use and after a rebuild)."""
         sim = self.sim
         key = (sim.neighbor.build_count, sim.atom.buffers.xr.data_ptr(), sim.history.touch.data_ptr(),
-               sim.neighbor.nbr.data_ptr())
+               sim.neighbor.nbr.data_ptr(), self.rows)
         if self._graph is None or self._graph_key != key:
             self._graph = None
 
@@ -363,7 +383,7 @@ class FusedEngine:
         nl_struct = sim.history.cstruct(nl)
         dbox, eng = sim.domain.dbox, self._eng.data_ptr()
         _lib.check(L.tmps_fused_c(atoms, nl_struct, dbox, eng, sim.pair_style.params, self.c_blocks,
-                                  self.part.data_ptr(), st), "tmps_fused_c")
+                                  self.part.data_ptr(), 1 if self.rows else 0, st), "tmps_fused_c")
         _lib.check(L.tmps_fused_servo(dbox, self._servo_ptr(), eng, self.part.data_ptr(), self.status.data_ptr(),
                                       st), "tmps_fused_servo")
 

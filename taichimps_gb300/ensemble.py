@@ -55,8 +55,9 @@ class BatchedEngine:
             raise ValueError("launch_shape is 'auto' or (a_groups_per_warp, c_groups_per_warp)")
         self.launch_shape = (0, 0) if self._tune else (int(launch_shape[0]), int(launch_shape[1]))
         self.tuning = None
+        # the batched C (tmps_batch_c) runs the screened path for every instance
         self.engines = [FusedEngine(s, precision, chunk=chunk, graphs=False, cull=cull,
-                                    launch_shape=self.launch_shape) for s in self.sims]
+                                    launch_shape=self.launch_shape, contact_path="screened") for s in self.sims]
         self.dev = _device.device()
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self._graph = None

@@ -45,6 +45,9 @@ class Simulation:
         # launch shape of the fused step (tmps_fused_shape): 32-atom groups
         # per warp of its update and contact kernels, 0 = the default grids
         self.launch_shape = (0, 0)
+        # path of the fused step's contact kernel (FusedEngine): "auto" (by the
+        # packing at each build), "screened" or "rows"
+        self.contact_path = "auto"
         self.last_engine = None
         self.dt = dt
         self.float_type = float_type

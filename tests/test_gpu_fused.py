@@ -20,7 +20,7 @@ MIXED_X = 1e-9     # positions (relative to the box)
 MIXED_P = 1e-5     # pressure tensor driving the servo
 
 
-def _servo_twin(oracle, precision, n=512, box=8.2, steps=60, seed=21, fused=True, remap="x"):
+def _servo_twin(oracle, precision, n=512, box=8.2, steps=60, seed=21, fused=True, remap="x", path="auto"):
     rng = np.random.default_rng(seed)
     x, r = dense_packing(rng, n, box, 0.48, 0.56)
     deform = dict(axes={d: {"style": "pressure", "ptarget": 1.0, "pgain": 1e-3} for d in "xyz"}, couple="xyz",
@@ -29,13 +29,16 @@ def _servo_twin(oracle, precision, n=512, box=8.2, steps=60, seed=21, fused=True
                           cundall=(0.7, 0.7), deform=deform)
     sim.precision = precision
     sim.fused = fused
+    sim.contact_path = path
     sim.run(steps)
     osim.run(steps)
     return sim, osim
 
 
-def test_fused_fp64_matches_per_hook_and_oracle(gpu, oracle):
-    sim_f, osim = _servo_twin(oracle, "fp64", fused=True)
+@pytest.mark.parametrize("path", ["screened", "rows"])
+def test_fused_fp64_matches_per_hook_and_oracle(gpu, oracle, path):
+    sim_f, osim = _servo_twin(oracle, "fp64", fused=True, path=path)
+    assert sim_f.last_engine.rows == (path == "rows")
     sim_h, _ = _servo_twin(oracle, "fp64", fused=False)
     assert sim_f.last_engine is not None and sim_h.last_engine is None
     gf, gh, o = gpu_state(sim_f), gpu_state(sim_h), oracle_state(osim)
@@ -47,8 +50,10 @@ def test_fused_fp64_matches_per_hook_and_oracle(gpu, oracle):
     assert sim_f.timestep == osim.timestep == 60
 
 
-def test_mixed_matches_oracle_within_stated_error(gpu, oracle):
-    sim, osim = _servo_twin(oracle, "mixed")
+@pytest.mark.parametrize("path", ["screened", "rows"])
+def test_mixed_matches_oracle_within_stated_error(gpu, oracle, path):
+    sim, osim = _servo_twin(oracle, "mixed", path=path)
+    assert sim.last_engine.rows == (path == "rows")
     assert sim.last_engine.mixed
     g, o = gpu_state(sim), oracle_state(osim)
     assert np.abs(o["f"]).max() > 0
@@ -115,8 +120,9 @@ def test_fused_second_run_continues(gpu, oracle):
     assert rel_err(g["v"], o["v"]) < 1e-10 and rel_err(g["f"], o["f"]) < 1e-9
 
 
+@pytest.mark.parametrize("path", ["screened", "rows"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_graph_replay_matches_eager_launches(gpu, oracle, precision):
+def test_graph_replay_matches_eager_launches(gpu, oracle, precision, path):
     """Chunks replayed as CUDA graphs give bit-identical results to launching step by step,
     across skin-triggered rebuilds (which force a new capture)."""
     rng = np.random.default_rng(9)
@@ -130,7 +136,7 @@ def test_graph_replay_matches_eager_launches(gpu, oracle, precision):
         from taichimps_gb300.engine import FusedEngine
         sim.setup_run(200)
         sim.init_simulation()
-        eng = FusedEngine(sim, precision, chunk=32, graphs=graphs)
+        eng = FusedEngine(sim, precision, chunk=32, graphs=graphs, contact_path=path)
         eng.begin()
         eng.run(200)
         eng.finish()
@@ -160,7 +166,7 @@ def test_contact_bound_culling_is_exact(gpu, oracle, precision):
                               dt=5e-5, cundall=(0.7, 0.7), deform=deform)
         sim.setup_run(steps)
         sim.init_simulation()
-        eng = FusedEngine(sim, precision, chunk=32, cull=cull)
+        eng = FusedEngine(sim, precision, chunk=32, cull=cull, contact_path="screened")
         eng.begin()
         eng.run(steps // 2)
         culled.append(eng.cull_stats())
@@ -241,8 +247,9 @@ def test_fused_rolling_resistance(gpu, oracle, precision):
         assert rel_err(g["omega"], o["omega"]) < MIXED_V, rel_err(g["omega"], o["omega"])
 
 
+@pytest.mark.parametrize("path", ["screened", "rows"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_partial_last_group_flags_and_no_spurious_rebuild(gpu, oracle, precision):
+def test_partial_last_group_flags_and_no_spurious_rebuild(gpu, oracle, precision, path):
     """An atom count that is not a multiple of 32: the flag words set after a
     build carry no bit past the last atom (a set bit makes C clear that atom's
     force, so a bit past the end would write past the force arrays), and a
@@ -260,7 +267,7 @@ def test_partial_last_group_flags_and_no_spurious_rebuild(gpu, oracle, precision
                        deform=deform)
     sim.setup_run(40)
     sim.init_simulation()
-    eng = FusedEngine(sim, precision, chunk=8)
+    eng = FusedEngine(sim, precision, chunk=8, contact_path=path)
     eng.begin()
     ng = (n + 31) // 32
     words = eng.part[:4 * ng].view(torch.int32).cpu().numpy().view(np.uint32)
@@ -393,3 +400,54 @@ def test_fused_neighbor_delay_every_check(gpu, oracle, precision):
     else:
         assert rel_err(g["v"], o["v"]) < MIXED_V, rel_err(g["v"], o["v"])
         assert rel_err(g["f"], o["f"]) < MIXED_F, rel_err(g["f"], o["f"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("pair", ["hertz/history", "granular/rolling"])
+def test_rows_path_equals_screened_path(gpu, oracle, precision, pair):
+    """C's per-atom-row path and its screened path sum each atom's contacts in slot order with the same
+    arithmetic, so forces, torques and histories are bit-identical; without a servo the order of the
+    virial partial sums feeds nothing back, so whole runs with rebuilds are bit-identical too."""
+    import torch
+    rng = np.random.default_rng(5)
+    x, r = dense_packing(rng, 512, 8.2, 0.48, 0.56)
+    v = rng.normal(scale=0.05, size=x.shape)
+    w = rng.normal(scale=0.5, size=x.shape)
+    states = []
+    for path in ("screened", "rows"):
+        sim, _ = make_twin(oracle, x, r, 2.5, [0.0] * 3, [8.2] * 3, v=v, w=w, pair=pair, dt=5e-5,
+                           cundall=(0.7, 0.7))
+        sim.precision = precision
+        sim.contact_path = path
+        sim.run(40)
+        assert sim.last_engine.rows == (path == "rows")
+        st = gpu_state(sim)
+        st["touch"] = sim.history.touch.cpu().numpy()
+        st["shear"] = sim.history.shear.cpu().numpy()
+        st["builds"] = sim.neighbor.build_count
+        states.append(st)
+    assert np.abs(states[0]["f"]).max() > 0 and np.count_nonzero(states[0]["touch"]) > 256
+    assert states[0]["builds"] == states[1]["builds"]
+    for k in ("x", "v", "omega", "f", "torque", "touch"):
+        np.testing.assert_array_equal(states[0][k], states[1][k])
+    live = (states[0]["touch"][None, :] >> np.arange(states[0]["shear"].shape[1], dtype=np.int64)[:, None]) & 1
+    for c in range(3):
+        np.testing.assert_array_equal(states[0]["shear"][c][live == 1], states[1]["shear"][c][live == 1])
+
+
+def test_auto_contact_path(gpu, oracle):
+    """contact_path "auto": the per-atom-row path on a packing where most atoms overlap at the build, the
+    screened path on a loose one."""
+    from taichimps_gb300.packing import make_packing_box
+    rng = np.random.default_rng(6)
+    x, r = dense_packing(rng, 512, 8.2, 0.48, 0.56)
+    sim, _ = make_twin(oracle, x, r, 2.5, [0.0] * 3, [8.2] * 3, pair="hertz/history", dt=5e-5)
+    sim.precision = "mixed"
+    sim.run(5)
+    assert sim.last_engine.rows
+    p = make_packing_box(1363, 0.8, 1.2, 0.45, seed=17)
+    sim, _ = make_twin(oracle, p["x"], p["radius"], 2.5, [0.0] * 3, [float(v) for v in p["L"]],
+                       pair="hertz/history", dt=5e-5)
+    sim.precision = "mixed"
+    sim.run(5)
+    assert not sim.last_engine.rows
