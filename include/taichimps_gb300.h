@@ -410,12 +410,9 @@ int tmps_fused_bounds(const tmps_atoms* a, const tmps_nlist* nl, const tmps_box*
  * the last C (an unflagged atom's force and torque are exact zeros and are
  * not loaded) and writes the first virial partials, the kinetic term
  * sum m v v of every atom at mid-step velocity.  a_blocks: A's grid from
- * tmps_fused_shape, or <= 0 for the default.  chained != 0 states that the
- * previous launch on `stream` is tmps_fused_servo of the previous step of
- * the same system: A (mixed form) then loads the first atom of each thread
- * before its dependency wait, overlapping that S; pass 0 otherwise. */
+ * tmps_fused_shape, or <= 0 for the default. */
 int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32_t a_blocks, void* scratch,
-                 int32_t chained, void* stream);
+                 void* stream);
 
 /* Launch C: per 32-atom group a bound check (tmps_fused_bounds), a screen of
  * the atoms the bounds leave (finishes contact-free ones, flags the rest) and

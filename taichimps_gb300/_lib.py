@@ -208,7 +208,7 @@ _SIGS = {
     "tmps_mixed_history": (c_i32, [ctypes.POINTER(NList), c_i32, c_vp]),
     "tmps_fused_bounds": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
                                   ctypes.POINTER(PairParams), c_i32, c_vp, c_vp]),
-    "tmps_fused_a": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
+    "tmps_fused_a": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_i32, c_vp, c_vp]),
     "tmps_fused_c": (c_i32, [ctypes.POINTER(Atoms), ctypes.POINTER(NList), c_vp, c_vp,
                              ctypes.POINTER(PairParams), c_i32, c_vp, c_i32, c_vp]),
     "tmps_fused_servo": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -56,6 +56,13 @@ TMPS_DEV double rsq64(const double* d) {
     return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
 }
 
+// a * b and a + b rounded as written (no multiply-add contraction), for sums
+// whose rounding must not depend on where the compiler inlines them
+TMPS_DEV float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+TMPS_DEV double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+TMPS_DEV float add_rn(float a, float b) { return __fadd_rn(a, b); }
+TMPS_DEV double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
 template <typename T>
 TMPS_DEV T dot3(const T* a, const T* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
 template <typename T>

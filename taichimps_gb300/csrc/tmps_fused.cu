@@ -248,33 +248,6 @@ __device__ __forceinline__ int cell_z(int32_t c) { return (c >> 20) & 1023; }
 __device__ __forceinline__ float4 ld4f_cs(const float* p, int i) { return __ldcs(reinterpret_cast<const float4*>(p) + i); }
 __device__ __forceinline__ void st4f_cs(float* p, int i, float4 v) { __stcs(reinterpret_cast<float4*>(p) + i, v); }
 
-// Resident blocks of the mixed A per SM (both variants: one grid size).
-constexpr int kMinBlocksA32 = 4;
-
-// The six state words of atom i (position, velocity, angular velocity; high
-// and low), through L2 only (the loads A issues before its dependency wait,
-// see a32_body).
-struct A32State {
-    float4 p, pl, v, vl, w, wl;
-};
-
-__device__ __forceinline__ void a32_prefetch(const tmps_atoms& a, int i, A32State& W) {
-    W.p = __ldcg(reinterpret_cast<const float4*>(a.pos32) + i);
-    W.pl = __ldcg(reinterpret_cast<const float4*>(a.pos32lo) + i);
-    W.v = __ldcg(reinterpret_cast<const float4*>(a.vel32) + i);
-    W.vl = __ldcg(reinterpret_cast<const float4*>(a.vel32lo) + i);
-    W.w = __ldcg(reinterpret_cast<const float4*>(a.om32) + i);
-    W.wl = __ldcg(reinterpret_cast<const float4*>(a.om32lo) + i);
-}
-
-// CHAINED: the launch that precedes this one on its stream is the S of the
-// previous step of the same system (the host says so).  That S let this grid
-// launch only after its own dependency wait returned, i.e. after the previous
-// step's A and C had completed with their writes visible, and S writes no
-// per-atom word.  So each thread loads the six state words of its first atom
-// before this grid's own dependency wait (through L2, bypassing the SM's L1),
-// and those loads overlap S.  Otherwise every load follows the wait.
-template <bool CHAINED>
 __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __restrict__ b,
                                          tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
                                          double* __restrict__ part, const int bid, const int nblk) {
@@ -283,15 +256,11 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
     // a double<->float conversion costs as much as a DFMA, so this kernel
     // issues no FP64 instruction at all.
     __shared__ float2 smem[6 * (kBlockA / 32)];
-    const int n = a.n;
-    const int lane = threadIdx.x & 31;
-    const int i_first = bid * blockDim.x + threadIdx.x;  // this thread's first atom
-    const bool pre = CHAINED && i_first < n;
-    A32State W0;
-    if (pre) a32_prefetch(a, i_first, W0);
     pdl_enter();
     if (e->aborted || e->step >= e->stop_step) return;
+    const int n = a.n;
     const int nb = e->nblocks;  // partials are component-major, [6][nb]
+    const int lane = threadIdx.x & 31;
     const int32_t s = (int32_t)(e->step + 1);
     const float dth = e->dt_hi, dtl = e->dt_lo;
     // merged half-kicks: the previous step's second and this step's first
@@ -300,8 +269,13 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
     bool hit = false;
     float dd = 0.0f;
     float Kh[6] = {0, 0, 0, 0, 0, 0}, Kl[6] = {0, 0, 0, 0, 0, 0};
-    // one atom's update from its state words
-    auto update = [&](float4 p, float4 pl, float4 v, float4 vl, float4 w, float4 wl, const int i) {
+    const int stride = nblk * blockDim.x;
+    for (int b0 = bid * blockDim.x + (threadIdx.x & ~31); b0 < n; b0 += stride) {
+        const int i = b0 + lane;
+        if (i >= n) continue;
+        float4 p = ld4f(a.pos32, i), pl = ld4f_cs(a.pos32lo, i);
+        float4 v = ld4f(a.vel32, i), vl = ld4f_cs(a.vel32lo, i);
+        float4 w = ld4f(a.om32, i), wl = ld4f_cs(a.om32lo, i);
         if (force_live(flags, i)) {  // an unflagged atom's force is an exact zero: nothing to add
             const float km = kick * vl.w, kI = kick * wl.w;  // vel32lo.w = 1/m, om32lo.w = 1/I
             dw_add(v.x, vl.x, km * __ldcs(a.f32 + i));
@@ -340,18 +314,6 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
                               (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
 #pragma unroll
         for (int k = 0; k < 6; ++k) dw_add(Kh[k], Kl[k], kin[k]);
-    };
-    const int stride = nblk * blockDim.x;
-    int b0 = bid * blockDim.x + (threadIdx.x & ~31);
-    if (pre) {  // the first atom, loaded before the wait (its registers are free after this)
-        update(W0.p, W0.pl, W0.v, W0.vl, W0.w, W0.wl, i_first);
-        b0 += stride;
-    }
-    for (; b0 < n; b0 += stride) {
-        const int i = b0 + lane;
-        if (i >= n) continue;
-        update(ld4f(a.pos32, i), ld4f_cs(a.pos32lo, i), ld4f(a.vel32, i), ld4f_cs(a.vel32lo, i), ld4f(a.om32, i),
-               ld4f_cs(a.om32lo, i), i);
     }
     if (__any_sync(0xffffffffu, hit) && lane == 0) e->disp_stamp = s;
     note_displacement(e, dd);
@@ -362,11 +324,10 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
     }
 }
 
-template <bool CHAINED>
-__global__ void __launch_bounds__(kBlockA, kMinBlocksA32) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
+__global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
                                                      tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
                                                      double* __restrict__ part) {
-    a32_body<CHAINED>(a, b, e, flags, part, blockIdx.x, gridDim.x);
+    a32_body(a, b, e, flags, part, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------- C
@@ -914,7 +875,9 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 fc[c] = sg * out.f[c];
-                tc[c] = arm * out.tor[c] + sg * out.troll[c];
+                // rounded as written: both products may be fused into the sum, and which one is
+                // must not depend on the path the contact is inlined into
+                tc[c] = add_rn(mul_rn(arm, out.tor[c]), sg * out.troll[c]);
             }
             vc[0] = T(0.5) * (in.d[0] * out.f[0]);
             vc[1] = T(0.5) * (in.d[1] * out.f[1]);
@@ -1857,7 +1820,7 @@ __global__ void __launch_bounds__(kBlockA, 4) kb_a32(const tmps_instance* __rest
     __shared__ tmps_instance si;
     const tmps_instance& I = stage_instance(si, inst, block_inst[blockIdx.x]);
     char* sc = static_cast<char*>(I.scratch);
-    a32_body<false>(I.a, I.box, I.eng, reinterpret_cast<const uint32_t*>(sc), reinterpret_cast<double*>(sc + lay_part(I.a.n)),
+    a32_body(I.a, I.box, I.eng, reinterpret_cast<const uint32_t*>(sc), reinterpret_cast<double*>(sc + lay_part(I.a.n)),
              (int)blockIdx.x - I.a_first, I.a_blocks);
 }
 
@@ -2109,7 +2072,7 @@ int contact_wave(int style, bool mixed) {
 int a_wave(bool mixed) {
     static int w[2] = {0, 0};
     int& v = w[mixed ? 1 : 0];
-    if (!v) v = mixed ? wave_blocks(k_a32<true>, kBlockA) : wave_blocks(k_a64, kBlockA);
+    if (!v) v = mixed ? wave_blocks(k_a32, kBlockA) : wave_blocks(k_a64, kBlockA);
     return v;
 }
 int a_blocks(int n, bool mixed) { const int b = grid_for(n, kBlockA); return b < a_wave(mixed) ? b : a_wave(mixed); }
@@ -2223,7 +2186,7 @@ int tmps_mixed_unpack(const tmps_atoms* a, const tmps_box* d_box, void* stream) 
 }
 
 int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32_t a_blocks_, void* scratch,
-                 int32_t chained, void* stream) {
+                 void* stream) {
     if (!a || !d_box || !d_eng || !scratch || a->n < 0) return TMPS_ERR_BAD_ARG;
     if (!a->pos32 && (!a->rinv || !a->x0)) return TMPS_ERR_BAD_ARG;
     if (a->n == 0) return TMPS_OK;
@@ -2237,8 +2200,7 @@ int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32
     double* part = (double*)((char*)scratch + part_offset(n));  // A's partials come first
     if (mixed) {
         if (!mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-        if (chained) launch_pdl(k_a32<true>, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
-        else launch_pdl(k_a32<false>, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
+        launch_pdl(k_a32, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     } else {
         launch_pdl(k_a64, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     }

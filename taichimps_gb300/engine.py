@@ -245,12 +245,10 @@ class FusedEngine:
         _lib.check(rc, "tmps_mixed_history")
         self._hist_dw = dw
 
-    def _launch_step(self, L, st, atoms, nl_struct, params, chained: bool = False) -> None:
-        """One step's launches; `chained`: the previous launch on the stream was this engine's S (a
-        step of the same chunk), which lets A start its loads before its dependency wait."""
+    def _launch_step(self, L, st, atoms, nl_struct, params) -> None:
         dbox, eng = self.sim.domain.dbox, self._eng.data_ptr()
         with _device.timed("fused_a"):
-            rc = L.tmps_fused_a(atoms, dbox, eng, self.a_blocks, self.part.data_ptr(), 1 if chained else 0, st)
+            rc = L.tmps_fused_a(atoms, dbox, eng, self.a_blocks, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_a")
         with _device.timed("fused_c"):
             rc = L.tmps_fused_c(atoms, nl_struct, dbox, eng, params, self.c_blocks, self.part.data_ptr(),
@@ -299,8 +297,8 @@ class FusedEngine:
             if self.graphs and count == self.chunk and _device.TIMED is None:
                 self._replay_chunk(L, atoms, nl_struct, params)
             else:
-                for k in range(count):
-                    self._launch_step(L, st, atoms, nl_struct, params, chained=k > 0)
+                for _ in range(count):
+                    self._launch_step(L, st, atoms, nl_struct, params)
             self._check_status()
         sim.timestep = target
 
@@ -314,8 +312,8 @@ class FusedEngine:
 
             def chunk():
                 st = _device.stream()
-                for k in range(self.chunk):
-                    self._launch_step(L, st, atoms, nl_struct, params, chained=k > 0)
+                for _ in range(self.chunk):
+                    self._launch_step(L, st, atoms, nl_struct, params)
 
             self._graph, self._graph_key = _device.capture_graph(chunk), key
         self._graph.replay()
