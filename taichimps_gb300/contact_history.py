@@ -41,9 +41,10 @@ class ContactHistory:
         self._nlist = None
         self._restart = None        # records from load_restart, applied at the next build
 
-    def _alloc(self, n: int, slots: int) -> None:
+    def _alloc(self, n: int, slots: int) -> bool:
+        """Arrays for n atoms x slots; True when they were just allocated (and so are zeros)."""
         if self._shape == (n, slots):
-            return
+            return False
         self.touch = torch.zeros(n, dtype=torch.int64, device=self.dev)
         self.shear = torch.zeros((3, slots, n), dtype=torch.float64, device=self.dev)
         self._touch_alt = torch.zeros_like(self.touch)
@@ -52,6 +53,7 @@ class ContactHistory:
             self.rolling = torch.zeros_like(self.shear)
             self._rolling_alt = torch.zeros_like(self.shear)
         self._shape = (n, slots)
+        return True
 
     def enable_rolling(self) -> None:
         """Keep a rolling displacement beside the shear (a pair with a rolling model asks for it)."""
@@ -123,8 +125,8 @@ class ContactHistory:
                 self._shape = (nlist._n, nlist.slots)
             self._synced_build = nlist.build_count
         else:
-            self._alloc(nlist._n, nlist.slots)
-            self.reset()
+            if not self._alloc(nlist._n, nlist.slots):  # fresh arrays are zeros already
+                self.reset()
             self._synced_build = nlist.build_count
         self._saved_build = None
         self.setup_pending = False

@@ -570,6 +570,19 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// The partner-side words of one contact (partner j of row atom i at slot k):
+// its state words and the contact's history as it enters the step.
+template <bool MIXED>
+struct CfLoad {
+    using S4 = typename std::conditional<MIXED, float4, double4>::type;
+    using HT = typename std::conditional<MIXED, DW, double>::type;
+    S4 pj, v2, w2;
+    float4 jl;
+    int32_t cj;
+    bool was;
+    HT shr[3], rlr[3];
+};
+
 template <int STYLE, bool MIXED, bool DENSE>
 __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L, const tmps_pair_params& P,
                                         const tmps_box* __restrict__ B, tmps_engine* __restrict__ E,
@@ -665,29 +678,78 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
     // touch, and if so the row atom's force, torque and pair virial terms in
     // fc, tc, vc; the contact's history is updated in place.  Every other load
     // of the contact is issued here together (one round trip).
-    auto contact_core = [&](const int ia, const int e, const int k, const bool was, const S4 Pi, const float4 PLi,
-                            const S4 Vi, const S4 Wi, const int32_t Ci, const S4 Pj, T (&fc)[3], T (&tc)[3],
+    // The loads of a contact (row atom ia, row entry e at slot k, touch bit
+    // `was`, partner high position word Pj), all issued at once: one round trip.
+    auto contact_fetch = [&](const int ia, const int e, const int k, const bool was, const S4 Pj) {
+        CfLoad<MIXED> cl;
+        const int j = e & kNbrIndexMask;
+        const size_t so = (size_t)k * n + ia;
+        cl.pj = Pj;
+        cl.was = was;
+        cl.cj = 0;
+        if constexpr (MIXED) {
+            cl.jl = ld4f(A.pos32lo, j);
+            cl.v2 = ld4f(A.vel32, j);
+            cl.w2 = ld4f(A.om32, j);
+            if (vremap) cl.cj = A.cell32[j];
+        } else {
+            cl.jl = make_float4(0.f, 0.f, 0.f, 0.f);
+            cl.v2 = ld4(A.vm, j);
+            cl.w2 = ld4(A.om, j);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            cl.shr[c] = HT{};
+            cl.rlr[c] = HT{};
+        }
+        if (hist && was) {
+            const HT* hs = reinterpret_cast<const HT*>(L.shear);
+            cl.shr[0] = hs[so];
+            cl.shr[1] = hs[ss + so];
+            cl.shr[2] = hs[2 * ss + so];
+            if (roll) {
+                const HT* hr = reinterpret_cast<const HT*>(L.rolling);
+                cl.rlr[0] = hr[so];
+                cl.rlr[1] = hr[ss + so];
+                cl.rlr[2] = hr[2 * ss + so];
+            }
+        }
+        return cl;
+    };
+
+    // The contact of row atom ia (its state words Pi, PLi (mixed: low words and
+    // radius lo), Vi, Wi and packed cell Ci) with the partner of row entry e at
+    // slot k, from its loads `cl`: whether they touch, and if so the row atom's
+    // force, torque and pair virial terms in fc, tc, vc; the contact's history
+    // is updated in place.
+    auto contact_eval = [&](const int ia, const int e, const int k, const S4 Pi, const float4 PLi, const S4 Vi,
+                            const S4 Wi, const int32_t Ci, const CfLoad<MIXED>& cl, T (&fc)[3], T (&tc)[3],
                             T (&vc)[6]) -> bool {
         (void)PLi;
         (void)Ci;
         const int j = e & kNbrIndexMask;
         const bool lo = ia < j;
         const size_t so = (size_t)k * n + ia;
-        // every load of the contact at once: one round trip
+        const bool was = cl.was;
         T xi[3], xj[3], ri, rj;
         int32_t ci = 0, cj = 0;
         float4 il = make_float4(0.f, 0.f, 0.f, 0.f), jl = il;
         T vi[3], wi[3], mi, vj[3], wj[3], mj;
-        HT shr[3] = {}, rlr[3] = {};
+        HT shr[3], rlr[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            shr[c] = cl.shr[c];
+            rlr[c] = cl.rlr[c];
+        }
         if constexpr (MIXED) {
-            const float4 pi = Pi, pj = Pj;
+            const float4 pi = Pi, pj = cl.pj;
             il = PLi;
-            jl = ld4f(A.pos32lo, j);
+            jl = cl.jl;
             const float4 v = Vi, w = Wi;
-            const float4 v2 = ld4f(A.vel32, j), w2 = ld4f(A.om32, j);
+            const float4 v2 = cl.v2, w2 = cl.w2;
             if (vremap) {
                 ci = Ci;
-                cj = A.cell32[j];
+                cj = cl.cj;
             }
             xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
             xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
@@ -696,27 +758,15 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
             vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
             wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
         } else {
-            const double4 pi = Pi, pj = Pj;
+            const double4 pi = Pi, pj = cl.pj;
             const double4 v = Vi, w = Wi;
-            const double4 v2 = ld4(A.vm, j), w2 = ld4(A.om, j);
+            const double4 v2 = cl.v2, w2 = cl.w2;
             xi[0] = pi.x; xi[1] = pi.y; xi[2] = pi.z; ri = pi.w;
             xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; rj = pj.w;
             vi[0] = v.x; vi[1] = v.y; vi[2] = v.z; mi = v.w;
             wi[0] = w.x; wi[1] = w.y; wi[2] = w.z;
             vj[0] = v2.x; vj[1] = v2.y; vj[2] = v2.z; mj = v2.w;
             wj[0] = w2.x; wj[1] = w2.y; wj[2] = w2.z;
-        }
-        if (hist && was) {
-            const HT* hs = reinterpret_cast<const HT*>(L.shear);
-            shr[0] = hs[so];
-            shr[1] = hs[ss + so];
-            shr[2] = hs[2 * ss + so];
-            if (roll) {
-                const HT* hr = reinterpret_cast<const HT*>(L.rolling);
-                rlr[0] = hr[so];
-                rlr[1] = hr[ss + so];
-                rlr[2] = hr[2 * ss + so];
-            }
         }
         // separation x_i - x_j
         T d[3];
@@ -907,12 +957,15 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
         if (live) {
             const int ia = W.idx[a];
             const bool was = ((W.touch[a] >> k) & 1ull) != 0;
-            if constexpr (MIXED)
-                contact = contact_core(ia, e, k, was, W.p[a], W.pl[a], W.v[a], W.w[a], vremap ? W.cell[a] : 0,
-                                       W.qp[slot], fc, tc, vc);
-            else
-                contact = contact_core(ia, e, k, was, W.p[a], make_float4(0.f, 0.f, 0.f, 0.f), W.v[a], W.w[a], 0,
-                                       ld4(A.xr, e & kNbrIndexMask), fc, tc, vc);
+            if constexpr (MIXED) {
+                const CfLoad<MIXED> cl = contact_fetch(ia, e, k, was, W.qp[slot]);
+                contact = contact_eval(ia, e, k, W.p[a], W.pl[a], W.v[a], W.w[a], vremap ? W.cell[a] : 0, cl, fc,
+                                       tc, vc);
+            } else {
+                const CfLoad<MIXED> cl = contact_fetch(ia, e, k, was, ld4(A.xr, e & kNbrIndexMask));
+                contact = contact_eval(ia, e, k, W.p[a], make_float4(0.f, 0.f, 0.f, 0.f), W.v[a], W.w[a], 0, cl,
+                                       fc, tc, vc);
+            }
         }
         if (contact) atomicOr(reinterpret_cast<unsigned long long*>(&W.ntouch[a]), 1ull << k);
         if constexpr (MIXED) {
@@ -1255,7 +1308,10 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                     if (nr) nmask |= 1ull << (k0 + u);
                 }
             }
-            // the near slots' contacts in ascending slot order
+            // the near slots' contacts in ascending slot order (each contact's
+            // loads issued together, then its evaluation; issuing the next
+            // contact's loads before evaluating the current one was measured
+            // slower: the second set of registers spills)
             T F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
             uint64_t nt = 0ull;
             for (uint64_t m = nmask; m; m &= m - 1ull) {
@@ -1264,9 +1320,9 @@ __device__ __forceinline__ void cf_body(const tmps_atoms& A, const tmps_nlist& L
                 S4 Pj;
                 if constexpr (MIXED) Pj = ld4f(A.pos32, e & kNbrIndexMask);
                 else Pj = ld4(A.xr, e & kNbrIndexMask);
+                const CfLoad<MIXED> cl = contact_fetch(i, e, k, ((touch >> k) & 1ull) != 0, Pj);
                 T fc[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, vc[6] = {0, 0, 0, 0, 0, 0};
-                if (contact_core(i, e, k, ((touch >> k) & 1ull) != 0, Pi, PLi, Vi, Wi, Ci, Pj, fc, tc, vc))
-                    nt |= 1ull << k;
+                if (contact_eval(i, e, k, Pi, PLi, Vi, Wi, Ci, cl, fc, tc, vc)) nt |= 1ull << k;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     F[c] += fc[c];

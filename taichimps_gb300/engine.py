@@ -86,9 +86,10 @@ class FusedEngine:
         self.cull = bool(cull)
         # C's path (tmps_fused_c): "screened" rules contact-free 32-atom groups out and runs the contacts
         # of the rest 32 at a time; "rows" runs every atom's row, one thread per atom; "auto" picks rows
-        # at a build where more than half of the atoms touch or overlap at the build positions (their
-        # gap bound is <= 0), screened otherwise.  Both give the same forces (each atom's contacts summed
-        # in slot order); only the order of the virial partial sums differs.
+        # for the mixed form at a build where more than half of the atoms touch or overlap at the build
+        # positions (their gap bound is <= 0), screened otherwise (the FP64 form's screened path was
+        # measured faster on contact-dense states too).  Both paths sum each atom's contacts in slot
+        # order with the same per-contact code; only the order of the virial partial sums differs.
         self.contact_path = contact_path
         self.rows = contact_path == "rows"
         # launch shape (tmps_fused_shape): 32-atom groups per warp of A and of C, 0 = the default grid;
@@ -226,7 +227,9 @@ class FusedEngine:
         rc = L.tmps_fused_bounds(atoms, sim.history.cstruct(nl), sim.domain.dbox, self._eng.data_ptr(),
                                  sim.pair_style.params, 1 if self.cull else 0, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_bounds")
-        if self.contact_path == "auto":
+        if self.contact_path == "auto" and not self.mixed:
+            self.rows = False
+        elif self.contact_path == "auto":
             n = self._n
             ng = (n + 31) // 32
             r256 = lambda b: (b + 255) // 256 * 256

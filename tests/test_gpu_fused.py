@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 MIXED_F = 5e-4     # forces / torques, max-abs normalised
 MIXED_V = 5e-4     # velocities after the run
 MIXED_X = 1e-9     # positions (relative to the box)
-MIXED_P = 1e-5     # pressure tensor driving the servo
+MIXED_P = 1e-6     # pressure tensor driving the servo (the mixed form's accuracy gate; measured 1e-8 .. 6e-8)
+MIXED_Q = 3e-6     # deviatoric stress q = p_zz - (p_xx + p_yy)/2, a difference of pressures (measured 8e-7)
 
 
 def _servo_twin(oracle, precision, n=512, box=8.2, steps=60, seed=21, fused=True, remap="x", path="auto"):
@@ -313,7 +314,7 @@ def test_triaxial_loading_matches_oracle(gpu, oracle, precision):
         oq.append(P[2] - 0.5 * (P[0] + P[1]))
     oq = np.array(oq)
     assert np.abs(oq).max() > 0
-    tol = 1e-10 if precision == "fp64" else MIXED_P
+    tol = 1e-10 if precision == "fp64" else MIXED_Q
     eq = np.abs(q - oq).max() / np.abs(oq).max()
     print(f"{precision} triaxial q vs oracle over 120 steps: {eq:.2e}")
     assert eq < tol, eq
@@ -406,8 +407,10 @@ def test_fused_neighbor_delay_every_check(gpu, oracle, precision):
 @pytest.mark.parametrize("pair", ["hertz/history", "granular/rolling"])
 def test_rows_path_equals_screened_path(gpu, oracle, precision, pair):
     """C's per-atom-row path and its screened path sum each atom's contacts in slot order with the same
-    arithmetic, so forces, torques and histories are bit-identical; without a servo the order of the
-    virial partial sums feeds nothing back, so whole runs with rebuilds are bit-identical too."""
+    per-contact code; without a servo the order of the virial partial sums feeds nothing back.  For
+    gran/hertz/history the two runs (with rebuilds) are bit-identical.  The pair granular law has sums of
+    two products whose multiply-add contraction the compiler may pick differently in the two kernels, so
+    there the runs agree to rounding (FP64: 1e-12 after 40 steps; mixed: the mixed form's tolerances)."""
     import torch
     rng = np.random.default_rng(5)
     x, r = dense_packing(rng, 512, 8.2, 0.48, 0.56)
@@ -428,11 +431,18 @@ def test_rows_path_equals_screened_path(gpu, oracle, precision, pair):
         states.append(st)
     assert np.abs(states[0]["f"]).max() > 0 and np.count_nonzero(states[0]["touch"]) > 256
     assert states[0]["builds"] == states[1]["builds"]
-    for k in ("x", "v", "omega", "f", "torque", "touch"):
-        np.testing.assert_array_equal(states[0][k], states[1][k])
-    live = (states[0]["touch"][None, :] >> np.arange(states[0]["shear"].shape[1], dtype=np.int64)[:, None]) & 1
-    for c in range(3):
-        np.testing.assert_array_equal(states[0]["shear"][c][live == 1], states[1]["shear"][c][live == 1])
+    if pair == "hertz/history":
+        for k in ("x", "v", "omega", "f", "torque", "touch"):
+            np.testing.assert_array_equal(states[0][k], states[1][k])
+        live = (states[0]["touch"][None, :] >> np.arange(states[0]["shear"].shape[1], dtype=np.int64)[:, None]) & 1
+        for c in range(3):
+            np.testing.assert_array_equal(states[0]["shear"][c][live == 1], states[1]["shear"][c][live == 1])
+    else:
+        tol = {"x": 1e-12, "v": 1e-12, "omega": 1e-12, "f": 1e-12, "torque": 1e-12} if precision == "fp64" else \
+              {"x": MIXED_X, "v": MIXED_V, "omega": MIXED_V, "f": MIXED_F, "torque": MIXED_F}
+        for k, t in tol.items():
+            e = np.abs(states[0][k] - states[1][k]).max() / (8.2 if k == "x" else np.abs(states[0][k]).max())
+            assert e < t, (k, e)
 
 
 def test_auto_contact_path(gpu, oracle):

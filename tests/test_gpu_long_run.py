@@ -6,7 +6,7 @@ so the comparison is of the quantities the reference reports, within stated
 tolerances:
 
   box strain at the end                                      FP64 1e-9, mixed 1e-6 relative to the strain
-  mean pressure over the last 500 steps                      FP64 1e-8, mixed 1e-5 relative
+  mean pressure over the last 500 steps                      FP64 1e-8, mixed 1e-6 relative
   coordination number at the end                             FP64 exact, mixed within 1%
 """
 
@@ -62,7 +62,7 @@ def test_long_run_matches_oracle(gpu, oracle, oracle_run, precision):
     # mean pressure over the last 500 steps
     pg = np.mean(rows[-500:, :3])
     po = np.mean(o["press"][-500:])
-    tol_p = 1e-8 if precision == "fp64" else 1e-5
+    tol_p = 1e-8 if precision == "fp64" else 1e-6  # mixed: the accuracy gate (measured 3.7e-8)
     print(f"{precision} long run: mean pressure over the last 500 steps vs oracle {abs(pg - po) / abs(po):.2e}, "
           f"box strain {np.abs(strain_g - strain_o).max() / np.abs(strain_o).max():.2e}")
     assert abs(pg - po) <= tol_p * abs(po), (pg, po)
