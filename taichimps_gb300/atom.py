@@ -29,20 +29,22 @@ def _sphere_mass(rad: np.ndarray, dens: np.ndarray) -> tuple[np.ndarray, np.ndar
 
 
 class _Buffers:
-    """One complete set of per-atom device arrays (two exist: build permutes A -> B)."""
+    """One complete set of per-atom device arrays (two exist: build permutes A -> B).  `fill`: zeros;
+    without it the arrays are left unset (a permutation target, which the build writes in full)."""
 
-    def __init__(self, n: int, dev: torch.device) -> None:
+    def __init__(self, n: int, dev: torch.device, fill: bool = True) -> None:
         f64 = dict(dtype=torch.float64, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)
-        self.xr = torch.zeros((n, 4), **f64)
-        self.vm = torch.zeros((n, 4), **f64)
-        self.om = torch.zeros((n, 4), **f64)
-        self.f = torch.zeros((3, n), **f64)
-        self.torque = torch.zeros((3, n), **f64)
-        self.virial = torch.zeros((6, n), **f64)
-        self.tag = torch.zeros(n, **i32)
-        self.uid = torch.zeros(n, **i32)
-        self.x0 = torch.zeros((3, n), **f64)
+        new = torch.zeros if fill else torch.empty
+        self.xr = new((n, 4), **f64)
+        self.vm = new((n, 4), **f64)
+        self.om = new((n, 4), **f64)
+        self.f = new((3, n), **f64)
+        self.torque = new((3, n), **f64)
+        self.virial = new((6, n), **f64)
+        self.tag = new(n, **i32)
+        self.uid = new(n, **i32)
+        self.x0 = new((3, n), **f64)
 
 
 class FieldView:
@@ -235,7 +237,7 @@ class AtomSystem:
             nb.tag.copy_(up(tags))
             nb.uid.copy_(torch.arange(n, dtype=torch.int32, device=dev))
             self._buf = nb
-            self._alt = _Buffers(n, dev)
+            self._alt = _Buffers(n, dev, fill=False)
             self.atom_type_host = np.concatenate([self.atom_type_host, types])
             self.mask_host = np.concatenate([self.mask_host, np.ones(n_new, dtype=np.int32)])
             self.nlocal = n
@@ -314,7 +316,7 @@ class AtomSystem:
             nb.tag.copy_(torch.from_numpy(np.asarray(tag, dtype=np.int32)).to(dev))
         nb.uid.copy_(torch.arange(n, dtype=torch.int32, device=dev))
         self._buf = nb
-        self._alt = _Buffers(n, dev)
+        self._alt = _Buffers(n, dev, fill=False)
         self.atom_type_host = types
         self.mask_host = np.ones(n, dtype=np.int32)
         self.nlocal = n

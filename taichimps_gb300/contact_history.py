@@ -42,33 +42,44 @@ class ContactHistory:
         self._restart = None        # records from load_restart, applied at the next build
 
     def _alloc(self, n: int, slots: int) -> bool:
-        """Arrays for n atoms x slots; True when they were just allocated (and so are zeros)."""
+        """Arrays for n atoms x slots; True when they were just allocated (touch masks zero).
+
+        A slot's shear (and rolling) entry means something only while its touch bit is set: every
+        kernel and view reads it under that bit, and a contact that starts begins from zero whatever
+        the entry holds.  So only the touch masks are zeroed; the carry-over targets of a rebuild
+        (the *_alt arrays) are allocated at the first rebuild that carries history."""
         if self._shape == (n, slots):
             return False
         self.touch = torch.zeros(n, dtype=torch.int64, device=self.dev)
-        self.shear = torch.zeros((3, slots, n), dtype=torch.float64, device=self.dev)
-        self._touch_alt = torch.zeros_like(self.touch)
-        self._shear_alt = torch.zeros_like(self.shear)
-        if self.rolling_enabled:
-            self.rolling = torch.zeros_like(self.shear)
-            self._rolling_alt = torch.zeros_like(self.shear)
+        self.shear = torch.empty((3, slots, n), dtype=torch.float64, device=self.dev)
+        self._touch_alt = self._shear_alt = self._rolling_alt = None
+        self.rolling = torch.empty_like(self.shear) if self.rolling_enabled else None
         self._shape = (n, slots)
         return True
+
+    def _carry_targets(self, n: int, slots: int) -> None:
+        """The arrays a rebuild's carry-over writes (touch masks and every entry below the new row
+        lengths are written by it)."""
+        if self._shear_alt is None or tuple(self._shear_alt.shape) != (3, slots, n):
+            self._touch_alt = torch.empty(n, dtype=torch.int64, device=self.dev)
+            self._shear_alt = torch.empty((3, slots, n), dtype=torch.float64, device=self.dev)
+            self._rolling_alt = None
+        if self.rolling is not None and self._rolling_alt is None:
+            self._rolling_alt = torch.empty_like(self._shear_alt)
 
     def enable_rolling(self) -> None:
         """Keep a rolling displacement beside the shear (a pair with a rolling model asks for it)."""
         if not self.rolling_enabled:
             self.rolling_enabled = True
             if self.shear is not None:
+                # contacts may be touching already: their rolling displacement starts at zero
                 self.rolling = torch.zeros_like(self.shear)
-                self._rolling_alt = torch.zeros_like(self.shear)
+                self._rolling_alt = None
 
     def reset(self) -> None:
+        """No touching contacts (the entries behind clear touch bits are not read)."""
         if self.touch is not None:
             self.touch.zero_()
-            self.shear.zero_()
-            if self.rolling is not None:
-                self.rolling.zero_()
 
     def ensure(self, nlist) -> None:
         """Make the history match `nlist`'s current build (fresh zeros if it does not)."""
@@ -104,12 +115,8 @@ class ContactHistory:
                    and self._shape == (nlist._n, nlist.prev_slots))
         if carried:
             L = _device.lib()
-            if nlist.slots != nlist.prev_slots:
-                # the list changed its slot count (slots="auto"): new-sized targets for the carry
-                n = nlist._n
-                self._shear_alt = torch.zeros((3, nlist.slots, n), dtype=torch.float64, device=self.dev)
-                if self.rolling is not None:
-                    self._rolling_alt = torch.zeros_like(self._shear_alt)
+            # targets for the carry (new-sized when the list changed its slot count, slots="auto")
+            self._carry_targets(nlist._n, nlist.slots)
             old = nlist.cstruct(self.touch, self.shear, prev=True, rolling=self.rolling)
             new = nlist.cstruct(self._touch_alt, self._shear_alt, rolling=self._rolling_alt)
             _lib.check(L.tmps_history_remap(old, new, nlist.order.data_ptr(), _device.stream()),
@@ -119,9 +126,7 @@ class ContactHistory:
             if self.rolling is not None:
                 self.rolling, self._rolling_alt = self._rolling_alt, self.rolling
             if nlist.slots != nlist.prev_slots:
-                self._shear_alt = torch.zeros_like(self.shear)
-                if self.rolling is not None:
-                    self._rolling_alt = torch.zeros_like(self.shear)
+                self._shear_alt = self._touch_alt = self._rolling_alt = None
                 self._shape = (nlist._n, nlist.slots)
             self._synced_build = nlist.build_count
         else:

@@ -39,30 +39,57 @@ __global__ void __launch_bounds__(kBlock)
     const uint64_t touch = hist ? L.touch[i] : 0ull;
     uint64_t newtouch = 0ull;
     const size_t ss = (size_t)L.slots * n;
-    for (int k = 0; k < nn; ++k) {
-        const int j = L.nbr[(size_t)k * n + i] & kNbrIndexMask;
-        const double4 xj = ld4(A.xr, j);
+    // the separation of i and partner j in the canonical orientation (lower
+    // internal index first) and the contact test, as the reference makes it
+    auto geom = [&](const int j, const double4 xj, PairIn<double>& in, double (&nimg)[3]) -> bool {
         const bool lo = i < j;  // this atom is `a` of the canonical pair
         const double4 xa = lo ? xi : xj, xb = lo ? xj : xi;
-        PairIn<double> in;
         in.d[0] = xa.x - xb.x;
         in.d[1] = xa.y - xb.y;
         in.d[2] = xa.z - xb.z;
         // Image count.  rint(d / prd) and rint(d * (1/prd)) differ only for a
         // separation within an ulp of half a box, which a listed neighbor
         // (|d| < cut <= prd / 3 after the image) never is.
-        double nimg[3] = {0, 0, 0};
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
+        for (int c = 0; c < 3; ++c) {
+            nimg[c] = 0.0;
             if (per[c] == 1) {
                 nimg[c] = rint(in.d[c] * iprd[c]);
                 in.d[c] = image_sub64(in.d[c], nimg[c], prd[c]);
             }
+        }
         in.rsq = rsq64(in.d);
         in.ra = xa.w;
         in.rb = xb.w;
         const double radsum = in.ra + in.rb;
-        if (!(in.rsq < __dmul_rn(radsum, radsum) && in.rsq > 1e-28)) continue;
+        return in.rsq < __dmul_rn(radsum, radsum) && in.rsq > 1e-28;
+    };
+    // the contact test of every row entry, four at a time (all loads in
+    // flight together), then the law over the slots in contact, in slot order
+    uint64_t cmask = 0ull;
+    for (int k0 = 0; k0 < nn; k0 += 4) {
+        int jj[4];
+        double4 xj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) jj[u] = k0 + u < nn ? L.nbr[(size_t)(k0 + u) * n + i] & kNbrIndexMask : 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k0 + u < nn) xj[u] = ld4(A.xr, jj[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            PairIn<double> t;
+            double ni[3];
+            if (k0 + u < nn && geom(jj[u], xj[u], t, ni)) cmask |= 1ull << (k0 + u);
+        }
+    }
+    for (uint64_t m = cmask; m; m &= m - 1ull) {
+        const int k = __ffsll((long long)m) - 1;
+        const int j = L.nbr[(size_t)k * n + i] & kNbrIndexMask;
+        const bool lo = i < j;
+        PairIn<double> in;
+        double nimg[3];
+        geom(j, ld4(A.xr, j), in, nimg);
+        const double radsum = in.ra + in.rb;
         in.r = sqrt(in.rsq);
         in.delta = radsum - in.r;
         const double4 vj = ld4(A.vm, j), wj = ld4(A.om, j);
