@@ -26,6 +26,27 @@ inline int grid_for(int64_t n, int block) {
     return (int)(g < 1 ? 1 : g);
 }
 
+// A double as an FP32 value from its bits alone: the sign, the exponent
+// rebiased and the top 20 bits of the significand (the rest truncated), so
+// the relative error is below 2^-20; zero below the FP32 normal range,
+// infinity above it, NaN kept.  Integer operations only: on this part a
+// double -> float conversion issues on the narrow FP64 pipe, and screens that
+// reject far pairs before an exact FP64 test do not need a rounded value.
+TMPS_DEV float approx_f32(double x) {
+    const uint32_t hi = (uint32_t)__double2hiint(x);
+    const uint32_t sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const uint32_t m = hi & 0xfffffu;
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+    const int ef = e - 1023 + 127;
+    if (ef <= 0) return __uint_as_float(sign);
+    if (ef >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((uint32_t)ef << 23) | (m << 3));
+}
+
+// |a| + |b| + |c|
+TMPS_DEV float l1f(float a, float b, float c) { return (fabsf(a) + fabsf(b)) + fabsf(c); }
+
 TMPS_DEV double4 ld4(const double* p, int i) { return reinterpret_cast<const double4*>(p)[i]; }
 TMPS_DEV void st4(double* p, int i, double4 v) { reinterpret_cast<double4*>(p)[i] = v; }
 TMPS_DEV float4 ld4f(const float* p, int i) { return reinterpret_cast<const float4*>(p)[i]; }

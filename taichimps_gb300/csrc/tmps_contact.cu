@@ -64,8 +64,21 @@ __global__ void __launch_bounds__(kBlock)
         const double radsum = in.ra + in.rb;
         return in.rsq < __dmul_rn(radsum, radsum) && in.rsq > 1e-28;
     };
-    // the contact test of every row entry, four at a time (all loads in
-    // flight together), then the law over the slots in contact, in slot order
+    // The contact test of every row entry, four at a time (all loads in
+    // flight together), then the law over the slots in contact, in slot order.
+    // An FP32 screen from the positions' truncated copies (approx_f32) first
+    // rules out the entries that cannot touch, by a margin of 1e-5 of the
+    // magnitudes involved, far above its error (2^-20 of each value plus
+    // FP32 rounding); only the rest take the exact FP64 test, whose cost on
+    // this part's narrow FP64 pipe is per warp, however few lanes are active.
+    const float xi32[3] = {approx_f32(xi.x), approx_f32(xi.y), approx_f32(xi.z)}, ri32 = approx_f32(xi.w);
+    float prd32[3], iprd32[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        prd32[c] = approx_f32(prd[c]);
+        iprd32[c] = approx_f32(iprd[c]);
+    }
+    const float base32 = l1f(xi32[0], xi32[1], xi32[2]) + l1f(prd32[0], prd32[1], prd32[2]);
     uint64_t cmask = 0ull;
     for (int k0 = 0; k0 < nn; k0 += 4) {
         int jj[4];
@@ -77,9 +90,21 @@ __global__ void __launch_bounds__(kBlock)
             if (k0 + u < nn) xj[u] = ld4(A.xr, jj[u]);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
+            if (k0 + u >= nn) continue;
+            const float xj32[3] = {approx_f32(xj[u].x), approx_f32(xj[u].y), approx_f32(xj[u].z)};
+            float d[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                d[c] = xi32[c] - xj32[c];
+                if (per[c] == 1) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
+            }
+            const float rq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+            const float rs = ri32 + approx_f32(xj[u].w);
+            const float lim = rs + 1e-5f * ((base32 + l1f(xj32[0], xj32[1], xj32[2])) + rs);
+            if (rq > lim * lim) continue;  // out of reach beyond doubt (a NaN goes on to the exact test)
             PairIn<double> t;
             double ni[3];
-            if (k0 + u < nn && geom(jj[u], xj[u], t, ni)) cmask |= 1ull << (k0 + u);
+            if (geom(jj[u], xj[u], t, ni)) cmask |= 1ull << (k0 + u);
         }
     }
     for (uint64_t m = cmask; m; m &= m - 1ull) {

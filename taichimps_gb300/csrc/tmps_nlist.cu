@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kBlock) k_permute(tmps_atoms src, tmps_atoms d
         float o[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const double h = b->prd[k] / (double)b->g[k];
+            const double h = b->hcell[k];  // prd / g, kept with the box (no division per atom)
             o[k] = (float)(xx[k] - (b->lo[k] + (double)cc[k] * h));
         }
         off32[p] = make_float4(o[0], o[1], o[2], (float)x.w);

@@ -103,28 +103,74 @@ def test_fp32_decisions_agree_with_the_fp64_test():
     assert checked_band > 1000
 
 
+def approx_f32(x):
+    """The device's approx_f32 (tmps_common.cuh): sign, rebiased exponent and the top 20 significand
+    bits of a double, truncated, as an FP32 value; zero below the FP32 normal range."""
+    hi = (np.asarray(x, dtype=np.float64).view(np.uint64) >> np.uint64(32)).astype(np.int64)
+    sign = hi & 0x80000000
+    e = (hi >> 20) & 0x7FF
+    m = hi & 0xFFFFF
+    ef = e - 1023 + 127
+    bits = np.where(e == 0x7FF, sign | 0x7F800000 | np.where(m != 0, 0x400000, 0),
+                    np.where(ef <= 0, sign, np.where(ef >= 255, sign | 0x7F800000, sign | (ef << 23) | (m << 3))))
+    return bits.astype(np.uint32).view(f32)
+
+
+def test_approx_f32_truncates_within_2e_20():
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-1e4, 1e4, 100_000), rng.normal(size=100_000) * 1e-3,
+                        [0.0, -0.0, 1.0, -1.0, 1e-300, 1e300, np.inf, -np.inf]])
+    a = approx_f32(x)
+    fin = np.isfinite(x) & (np.abs(x) > 1e-37) & (np.abs(x) < 1e38)
+    rel = np.abs(a[fin].astype(np.float64) - x[fin]) / np.abs(x[fin])
+    assert rel.max() < 2.0 ** -20
+    assert np.all(np.abs(a[fin]) <= np.abs(x[fin]))  # truncation toward zero
+    assert a[-8] == 0.0 and a[-6] == 1.0 and a[-5] == -1.0 and a[-4] == 0.0
+    assert a[-3] == f32(np.inf) and a[-2] == f32(np.inf) and a[-1] == -f32(np.inf)
+    assert np.isnan(approx_f32(np.array([np.nan])))[0]
+
+
 def test_fp32_gap_bound_is_a_lower_bound():
-    """The contact bound (tmps_fused.cu, k_bounds) forms the separation in FP64, the distance and the
-    gap in FP32, and lowers the gap by 1e-6 (r + ri + rj): it must never exceed the FP64 gap, or a
-    group could be ruled out while one of its pairs can still close."""
+    """The contact bound (tmps_fused.cu, k_bounds) forms the separation, distance and gap in FP32 from
+    the positions' and radii's truncated FP32 copies (approx_f32) and lowers the gap by 1e-5 of the
+    magnitudes involved: it must never exceed the FP64 gap, or a group could be ruled out while one of
+    its pairs can still close.  Pairs at the contact distance within 1e-3, atoms up to 1e4 from the
+    origin, periodic images in a box of 1.2e3 (a listed pair is never near half a box)."""
     rng = np.random.default_rng(7)
     m = 400_000
+    prd = np.array([1200.0, 1100.0, 1300.0])
     r = np.concatenate([rng.uniform(0.0, 1.5, size=m // 2), rng.uniform(0.5, 0.7, size=m // 2)])
     u = rng.normal(size=(m, 3))
     u /= np.linalg.norm(u, axis=1, keepdims=True)
     d = u * r[:, None] * rng.uniform(0.999, 1.001, size=(m, 1))
     ri = rng.uniform(0.25, 0.6, size=m)
     rj = rng.uniform(0.25, 0.6, size=m)
-    exact = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]) - (ri + rj)
-    fd = d.astype(f32)
+    scale = np.where(rng.uniform(size=m) < 0.5, 1e4, 50.0)
+    xi = rng.uniform(-1.0, 1.0, size=(m, 3)) * scale[:, None]
+    img = rng.integers(-2, 3, size=(m, 3))
+    xj = (xi - d) + img * prd          # the partner seen through a periodic image
+    dd = xi - xj
+    dd -= np.rint(dd / prd) * prd      # the exact minimum image
+    exact = np.sqrt((dd ** 2).sum(axis=1)) - (ri + rj)
+    xi32, xj32 = approx_f32(xi), approx_f32(xj)
+    prd32, iprd32 = approx_f32(prd), approx_f32(1.0 / prd)
+    bprd = (np.abs(prd32[0]) + np.abs(prd32[1])).astype(f32) + np.abs(prd32[2])
+    l1 = lambda v: ((np.abs(v[:, 0]) + np.abs(v[:, 1])).astype(f32) + np.abs(v[:, 2])).astype(f32)
     for fused in (False, True):
+        fd = []
+        for c in range(3):
+            x = (xi32[:, c] - xj32[:, c]).astype(f32)
+            nimg = np.rint((x * iprd32[c]).astype(f32)).astype(f32)
+            x = _fma(-nimg, np.full_like(x, prd32[c]), x) if fused else (x - (nimg * prd32[c]).astype(f32)).astype(f32)
+            fd.append(x)
         if fused:
-            rq = _fma(fd[:, 2], fd[:, 2], _fma(fd[:, 1], fd[:, 1], (fd[:, 0] * fd[:, 0]).astype(f32)))
+            rq = _fma(fd[2], fd[2], _fma(fd[1], fd[1], (fd[0] * fd[0]).astype(f32)))
         else:
-            rq = ((fd[:, 0] * fd[:, 0] + fd[:, 1] * fd[:, 1]).astype(f32) + (fd[:, 2] * fd[:, 2]).astype(f32))
+            rq = ((fd[0] * fd[0] + fd[1] * fd[1]).astype(f32) + (fd[2] * fd[2]).astype(f32)).astype(f32)
         rf = np.sqrt(rq.astype(f32)).astype(f32)
-        rs = (ri.astype(f32) + rj.astype(f32)).astype(f32)
-        gp = ((rf - rs).astype(f32) - (f32(1e-6) * (rf + rs)).astype(f32)).astype(f32)
+        rs = (approx_f32(ri) + approx_f32(rj)).astype(f32)
+        mag = ((((l1(xi32) + bprd).astype(f32) + l1(xj32)).astype(f32) + rf).astype(f32) + rs).astype(f32)
+        gp = ((rf - rs).astype(f32) - (f32(1e-5) * mag).astype(f32)).astype(f32)
         assert np.all(gp.astype(np.float64) <= exact), "FP32 gap above the FP64 gap"
-        # and not needlessly low: within a few 1e-6 of the pair's size
-        assert np.all(exact - gp <= 5e-6 * (r + ri + rj) + 1e-12)
+        # and not needlessly low: within 2e-5 of the magnitudes
+        assert np.all(exact - gp <= 2e-5 * mag + 1e-12)
