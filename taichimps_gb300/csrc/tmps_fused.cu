@@ -387,39 +387,45 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
         iprd[c] = B->inv_prd[c];
         single = single || (per[c] == 1 && B->g[c] == 1);
     }
-    // The bound only has to be a lower bound, so it is formed in FP32 from the
-    // positions' and radii's truncated FP32 copies (approx_f32: integer
-    // operations, no FP64 instruction), and the gap is lowered by 1e-5 of the
-    // magnitudes involved -- far over its error (2^-20 of each value plus
-    // FP32 rounding; a listed pair is never near half a box, so the image is
-    // the FP64 one): a bound a little low only culls a little less.
+    // The bound only has to be a lower bound.  The separation is the FP64
+    // difference of the positions, taken to FP32 by truncation (approx_f32:
+    // integer operations, no FP64 conversion), its periodic image and the
+    // distance and gap then in FP32, and the gap is lowered by 3e-6 of the
+    // magnitudes involved -- the separation before the image, the image shift,
+    // r and the radii: over twice the error (2^-20 of each truncated value plus
+    // FP32 rounding, ~1.2e-6 of them), while a pair away from the boundary
+    // keeps a margin of ~1e-5 (a listed pair is never near half a box, so the
+    // image is the FP64 one).  A bound a little low only culls a little less.
     float prd32[3], iprd32[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         prd32[c] = approx_f32(prd[c]);
         iprd32[c] = approx_f32(iprd[c]);
     }
-    const float bprd = l1f(prd32[0], prd32[1], prd32[2]);
     for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += nwarps) {
         const int i = (g << 5) + lane;
         float gmin = 3e38f;
         if (i < n) {
-            const float xi[3] = {approx_f32(A.x0[i]), approx_f32(A.x0[n + i]), approx_f32(A.x0[2 * n + i])};
+            const double xi[3] = {A.x0[i], A.x0[n + i], A.x0[2 * n + i]};
             const float ri = approx_f32(A.xr[4 * (size_t)i + 3]);
-            const float bi = l1f(xi[0], xi[1], xi[2]) + bprd;
             const int nn = L.nnb[i];
             for (int k = 0; k < nn; ++k) {
                 const int j = L.nbr[(size_t)k * n + i] & kNbrIndexMask;
-                const float xj[3] = {approx_f32(A.x0[j]), approx_f32(A.x0[n + j]), approx_f32(A.x0[2 * n + j])};
-                float d[3];
+                const double dd[3] = {xi[0] - A.x0[j], xi[1] - A.x0[n + j], xi[2] - A.x0[2 * n + j]};
+                float d[3], mag = 0.0f;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    d[c] = xi[c] - xj[c];
-                    if (per[c] == 1) d[c] -= rintf(d[c] * iprd32[c]) * prd32[c];
+                    d[c] = approx_f32(dd[c]);
+                    mag += fabsf(d[c]);
+                    if (per[c] == 1) {
+                        const float nimg = rintf(d[c] * iprd32[c]);
+                        d[c] -= nimg * prd32[c];
+                        mag += fabsf(nimg) * prd32[c];
+                    }
                 }
                 const float r = sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
                 const float rs = ri + approx_f32(A.xr[4 * (size_t)j + 3]);
-                const float gp = (r - rs) - 1e-5f * (((bi + l1f(xj[0], xj[1], xj[2])) + r) + rs);
+                const float gp = (r - rs) - 3e-6f * ((mag + r) + rs);
                 gmin = gp == gp ? fminf(gmin, gp) : -3e38f;  // a NaN pair pins the group
             }
             if ((hist && L.touch[i] != 0ull) || single) gmin = -3e38f;
