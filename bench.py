@@ -155,20 +155,20 @@ def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float, flag
     """Bytes per atom a launch must move through HBM.
 
     fused_a (A), every atom: the Verlet stream of the step plus the skin check's reference words.
-      mixed: reads the position, velocity and angular velocity (high and low FP32 words, 72), m, 1/m
-             and 1/I (12), the offset at the last build (12) and the packed cell (4); writes the three
-             vectors, both words (72)                                                             = 172
+      mixed: reads and writes the position, velocity and angular velocity (high and low FP32 words,
+             72 + 72), reads m (kinetic term, 4), the offset at the last build (12) and the packed cell
+             (4)                                                                                  = 164
+             plus per flagged atom (`flagged` = fraction) the force and torque and 1/m, 1/I: 32
       FP64:  reads x, v, omega (72), 1/m and 1/I (16), x at the last build (24); writes x, v, omega (72)
-                                                                                                  = 184
-      plus, per flagged atom (`flagged` = fraction), the force and torque: 24 (mixed) / 48 (FP64).
-      The records A actually streams are float4 / double4 words whose fourth lanes hold per-build
-      constants (radius, m, I, 1/m, 1/I) for C's gathers, so A reads and writes those too
-      (layout_bytes: 208 mixed / 232 FP64); those extra bytes are not counted here.
+             = 184, plus per flagged atom the force and torque: 48
+      A's records also carry per-build constants in their fourth lanes for C's gathers (radius hi and
+      lo, m), which it reads and writes with them (layout_bytes: 184 mixed / 232 FP64 per atom); those
+      are not counted here.
     fused_c (C): the contact kernel's per-atom bytes, S + 4 n_nb + 52 n_c (own state read once and
       force written once, S = 84 mixed / 140 FP64; 4 per neighbor index; 4 partner + 48 shear per
       touching slot)."""
     if kernel == "fused_a":
-        return (172.0 + 24.0 * flagged) if precision == "mixed" else (184.0 + 48.0 * flagged)
+        return (164.0 + 32.0 * flagged) if precision == "mixed" else (184.0 + 48.0 * flagged)
     if kernel == "fused_c":
         return (84.0 if precision == "mixed" else 140.0) + 4.0 * n_nb + 52.0 * n_c
     return 0.0
@@ -177,7 +177,7 @@ def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float, flag
 def layout_bytes(kernel: str, precision: str, flagged: float) -> float:
     """Bytes per atom A's record layout makes it read and write (see algorithmic_bytes)."""
     if kernel == "fused_a":
-        return (208.0 + 24.0 * flagged) if precision == "mixed" else (232.0 + 48.0 * flagged)
+        return (184.0 + 32.0 * flagged) if precision == "mixed" else (232.0 + 48.0 * flagged)
     return 0.0
 
 

@@ -91,17 +91,21 @@ typedef struct tmps_atoms {
     float* pos32;       /* float[n][4]: offset from cell origin, radius */
     int32_t* cell32;    /* cell coordinate, cx | cy << 10 | cz << 20 */
     float* vel32;       /* float[n][4]: v, mass */
-    float* om32;        /* float[n][4]: omega, inertia */
+    float* om32;        /* float[n][4]: omega, v lo x (see the low words below) */
     float* f32;         /* float[3][n] contact force, mixed form */
     float* torque32;    /* float[3][n] */
     float* o0_32;       /* float[3][n]: offsets at the last build (mixed skin check) */
     double* rinv;       /* double[2][n]: 1/m, 1/I (fused FP64 step) */
     /* Low words of the mixed form's double-word state: value = hi + lo with
-     * both FP32 (~48-bit significand).  pos32lo = (offset lo, radius lo),
-     * vel32lo = (v lo, 1/m), om32lo = (w lo, 1/I). */
+     * both FP32 (~48-bit significand).  pos32lo = (offset lo, radius lo);
+     * the velocity and angular velocity low words are packed so that the
+     * update kernel rewrites no per-build constant beside them: v lo x in
+     * om32's fourth lane, lo32 = (v lo y, v lo z, omega lo x, omega lo y),
+     * wlz32 = omega lo z; inv32 = (1/m, 1/I), read only. */
     float* pos32lo;
-    float* vel32lo;
-    float* om32lo;
+    float* lo32;        /* float[n][4] */
+    float* wlz32;       /* float[n] */
+    float* inv32;       /* float[n][2] */
 } tmps_atoms;
 
 /* Full neighbor list with its contact history. */

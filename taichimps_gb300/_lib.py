@@ -39,8 +39,8 @@ class Atoms(ctypes.Structure):
         ("xr", c_vp), ("vm", c_vp), ("om", c_vp), ("f", c_vp), ("torque", c_vp), ("virial", c_vp),
         ("tag", c_vp), ("uid", c_vp), ("x0", c_vp),
         ("pos32", c_vp), ("cell32", c_vp), ("vel32", c_vp), ("om32", c_vp), ("f32", c_vp),
-        ("torque32", c_vp), ("o0_32", c_vp), ("rinv", c_vp), ("pos32lo", c_vp), ("vel32lo", c_vp),
-        ("om32lo", c_vp),
+        ("torque32", c_vp), ("o0_32", c_vp), ("rinv", c_vp), ("pos32lo", c_vp), ("lo32", c_vp),
+        ("wlz32", c_vp), ("inv32", c_vp),
     ]
 
 

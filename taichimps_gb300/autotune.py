@@ -62,7 +62,7 @@ class _Trial:
         b = sim.atom.buffers
         if eng.mixed:
             for name, t in (("pos32", eng.pos32), ("pos32lo", eng.pos32lo), ("vel32", eng.vel32),
-                            ("vel32lo", eng.vel32lo), ("om32", eng.om32), ("om32lo", eng.om32lo),
+                            ("lo32", eng.lo32), ("wlz32", eng.wlz32), ("om32", eng.om32),
                             ("f32", eng.f32), ("torque32", eng.t32)):
                 setattr(d.a, name, redirect(getattr(d.a, name), t))
         else:

@@ -241,6 +241,48 @@ __device__ __forceinline__ int cell_x(int32_t c) { return c & 1023; }
 __device__ __forceinline__ int cell_y(int32_t c) { return (c >> 10) & 1023; }
 __device__ __forceinline__ int cell_z(int32_t c) { return (c >> 20) & 1023; }
 
+// The mixed form's velocity and angular velocity words of atom i as four
+// float4: v = (v hi, m), vl = (v lo, 1/m), w = (omega hi, -), wl = (omega lo,
+// 1/I).  In memory the low words are packed so that no per-build constant is
+// rewritten with them: om32 = (omega hi, v lo x), lo32 = (v lo y, v lo z,
+// omega lo x, omega lo y), wlz32 = omega lo z, inv32 = (1/m, 1/I) (read only).
+// CS: the low words with streaming (evict-first) hints; INV: also 1/m and 1/I
+// (else vl.w and wl.w are left 0).
+template <bool CS, bool INV = true>
+__device__ __forceinline__ void load_vw(const tmps_atoms& a, int i, float4& v, float4& vl, float4& w, float4& wl) {
+    v = ld4f(a.vel32, i);
+    const float4 o = ld4f(a.om32, i);
+    float4 q;
+    float wz;
+    float2 inv = make_float2(0.0f, 0.0f);
+    if constexpr (CS) {
+        q = __ldcs(reinterpret_cast<const float4*>(a.lo32) + i);
+        wz = __ldcs(a.wlz32 + i);
+        if constexpr (INV) inv = __ldcs(reinterpret_cast<const float2*>(a.inv32) + i);
+    } else {
+        q = ld4f(a.lo32, i);
+        wz = a.wlz32[i];
+        if constexpr (INV) inv = reinterpret_cast<const float2*>(a.inv32)[i];
+    }
+    w = make_float4(o.x, o.y, o.z, 0.0f);
+    vl = make_float4(o.w, q.x, q.y, inv.x);
+    wl = make_float4(q.z, q.w, wz, inv.y);
+}
+
+template <bool CS>
+__device__ __forceinline__ void store_vw(const tmps_atoms& a, int i, float4 v, float4 vl, float4 w, float4 wl) {
+    st4f(a.vel32, i, v);
+    st4f(a.om32, i, make_float4(w.x, w.y, w.z, vl.x));
+    const float4 q = make_float4(vl.y, vl.z, wl.x, wl.y);
+    if constexpr (CS) {
+        __stcs(reinterpret_cast<float4*>(a.lo32) + i, q);
+        __stcs(a.wlz32 + i, wl.z);
+    } else {
+        reinterpret_cast<float4*>(a.lo32)[i] = q;
+        a.wlz32[i] = wl.z;
+    }
+}
+
 // Streaming (evict-first) loads and stores for the per-atom words only A
 // touches each step: A moves ~150 MB through the 129 MB L2 every step, and
 // marking that traffic evict-first keeps C's working set (flag words, gap
@@ -274,10 +316,11 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
         const int i = b0 + lane;
         if (i >= n) continue;
         float4 p = ld4f(a.pos32, i), pl = ld4f_cs(a.pos32lo, i);
-        float4 v = ld4f(a.vel32, i), vl = ld4f_cs(a.vel32lo, i);
-        float4 w = ld4f(a.om32, i), wl = ld4f_cs(a.om32lo, i);
+        float4 v, vl, w, wl;
+        load_vw<true, false>(a, i, v, vl, w, wl);
         if (force_live(flags, i)) {  // an unflagged atom's force is an exact zero: nothing to add
-            const float km = kick * vl.w, kI = kick * wl.w;  // vel32lo.w = 1/m, om32lo.w = 1/I
+            const float2 inv = __ldcs(reinterpret_cast<const float2*>(a.inv32) + i);  // 1/m, 1/I
+            const float km = kick * inv.x, kI = kick * inv.y;
             dw_add(v.x, vl.x, km * __ldcs(a.f32 + i));
             dw_add(v.y, vl.y, km * __ldcs(a.f32 + n + i));
             dw_add(v.z, vl.z, km * __ldcs(a.f32 + 2 * n + i));
@@ -297,10 +340,7 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
         dw_add_prod(p.z, pl.z, dth, dtl, v.z, vl.z);
         st4f(a.pos32, i, p);
         st4f_cs(a.pos32lo, i, pl);
-        st4f(a.vel32, i, v);
-        st4f_cs(a.vel32lo, i, vl);
-        st4f(a.om32, i, w);
-        st4f_cs(a.om32lo, i, wl);
+        store_vw<true>(a, i, v, vl, w, wl);
         // displacement since the build: offset change + cell origin change
         const int32_t c = __ldcs(a.cell32 + i);
         const float d0 = ((p.x - __ldcs(a.o0_32 + i)) + pl.x) + (float)cell_x(c) * e->dh32[0] + e->dlo32[0];
@@ -1964,10 +2004,9 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
     float vh[3], vlo[3], wh[3], wlo[3];
     split(v.x, vh[0], vlo[0]); split(v.y, vh[1], vlo[1]); split(v.z, vh[2], vlo[2]);
     split(w.x, wh[0], wlo[0]); split(w.y, wh[1], wlo[1]); split(w.z, wh[2], wlo[2]);
-    st4f(a.vel32, i, make_float4(vh[0], vh[1], vh[2], (float)v.w));
-    st4f(a.vel32lo, i, make_float4(vlo[0], vlo[1], vlo[2], (float)(1.0 / v.w)));
-    st4f(a.om32, i, make_float4(wh[0], wh[1], wh[2], (float)w.w));
-    st4f(a.om32lo, i, make_float4(wlo[0], wlo[1], wlo[2], (float)(1.0 / w.w)));
+    reinterpret_cast<float2*>(a.inv32)[i] = make_float2((float)(1.0 / v.w), (float)(1.0 / w.w));
+    store_vw<false>(a, i, make_float4(vh[0], vh[1], vh[2], (float)v.w), make_float4(vlo[0], vlo[1], vlo[2], 0.0f),
+                    make_float4(wh[0], wh[1], wh[2], 0.0f), make_float4(wlo[0], wlo[1], wlo[2], 0.0f));
 }
 
 __global__ void k_prepare_engine(const tmps_box* __restrict__ b, tmps_engine* e, int64_t part_off) {
@@ -2000,8 +2039,8 @@ __global__ void __launch_bounds__(kBlockA) k_unpack(tmps_atoms a, const tmps_box
     if (i >= n) return;
     double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
     const float4 p = ld4f(a.pos32, i), pl = ld4f(a.pos32lo, i);
-    const float4 vv = ld4f(a.vel32, i), vl = ld4f(a.vel32lo, i);
-    const float4 ww = ld4f(a.om32, i), wl = ld4f(a.om32lo, i);
+    float4 vv, vl, ww, wl;
+    load_vw<false>(a, i, vv, vl, ww, wl);
     const int32_t c = a.cell32[i];
     const int cc[3] = {cell_x(c), cell_y(c), cell_z(c)};
     const float oh[3] = {p.x, p.y, p.z}, ol[3] = {pl.x, pl.y, pl.z};
@@ -2028,8 +2067,8 @@ __global__ void __launch_bounds__(kBlockA) k_settle(tmps_atoms a, const tmps_box
     if (i >= n) return;
     if constexpr (MIXED) {
         float4 p = ld4f(a.pos32, i), pl = ld4f(a.pos32lo, i);
-        float4 v = ld4f(a.vel32, i), vl = ld4f(a.vel32lo, i);
-        float4 w = ld4f(a.om32, i), wl = ld4f(a.om32lo, i);
+        float4 v, vl, w, wl;
+        load_vw<false>(a, i, v, vl, w, wl);
         if (e->final_pending) {
             const float dtf = 0.5f * e->dt_hi;
             const float km = dtf * vl.w, kI = dtf * wl.w;
@@ -2047,10 +2086,7 @@ __global__ void __launch_bounds__(kBlockA) k_settle(tmps_atoms a, const tmps_box
         }
         st4f(a.pos32, i, p);
         st4f(a.pos32lo, i, pl);
-        st4f(a.vel32, i, v);
-        st4f(a.vel32lo, i, vl);
-        st4f(a.om32, i, w);
-        st4f(a.om32lo, i, wl);
+        store_vw<false>(a, i, v, vl, w, wl);
         return;
     }
     double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
@@ -2103,7 +2139,7 @@ void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, A&&..
 }
 
 bool mixed_ok(const tmps_atoms* a) {
-    return a->pos32 && a->pos32lo && a->vel32 && a->vel32lo && a->om32 && a->om32lo && a->cell32 && a->f32 &&
+    return a->pos32 && a->pos32lo && a->vel32 && a->lo32 && a->om32 && a->wlz32 && a->inv32 && a->cell32 && a->f32 &&
            a->torque32 && a->o0_32;
 }
 

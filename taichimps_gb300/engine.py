@@ -124,8 +124,9 @@ class FusedEngine:
         if self.mixed:
             self.pos32 = torch.zeros((n, 4), **f32)
             self.pos32lo = torch.zeros((n, 4), **f32)
-            self.vel32lo = torch.zeros((n, 4), **f32)
-            self.om32lo = torch.zeros((n, 4), **f32)
+            self.lo32 = torch.zeros((n, 4), **f32)
+            self.wlz32 = torch.zeros(n, **f32)
+            self.inv32 = torch.zeros((n, 2), **f32)
             self.vel32 = torch.zeros((n, 4), **f32)
             self.om32 = torch.zeros((n, 4), **f32)
             self.f32 = torch.zeros((3, n), **f32)
@@ -162,7 +163,7 @@ class FusedEngine:
             s.f32, s.torque32, s.o0_32 = self.f32.data_ptr(), self.t32.data_ptr(), self.o0.data_ptr()
             s.cell32 = self.cell32.data_ptr()
             s.pos32lo = self.pos32lo.data_ptr()
-            s.vel32lo, s.om32lo = self.vel32lo.data_ptr(), self.om32lo.data_ptr()
+            s.lo32, s.wlz32, s.inv32 = self.lo32.data_ptr(), self.wlz32.data_ptr(), self.inv32.data_ptr()
         return s
 
     def _servo_ptr(self) -> int:
