@@ -272,15 +272,23 @@ def test_adjoint_matches_finite_differences(fd2048):
     measures a secant, not the derivative; they are printed, not judged.  Of the branch-keeping steps the
     two largest give the check: the difference at the largest (the parameters: rounding noise dominates
     below it) or its Richardson extrapolation with the next (the radii: the overlap's curvature makes the
-    h^2 truncation dominate at it); the adjoint must match one of them.  xmu: the next test."""
+    h^2 truncation dominate at it); the adjoint must match one of them.  A radius with fewer than two
+    branch-keeping steps (its contact sits on a threshold) is not judged; the four parameters and at least
+    four of the six radii must be.  xmu: the next test."""
     errs = {}
     for k, (a, rows) in fd2048.items():
         if k == "xmu":
+            continue
+        if sum(ok for _, _, ok in rows) < 2:
+            # a radius whose contact sits on a threshold: every step moves it across
+            print(f"{k}: fewer than two branch-keeping steps, not judged")
             continue
         d1, rich, h = _largest_smooth(rows)
         e1, er = abs(a - d1) / abs(d1), abs(a - rich) / abs(rich)
         errs[k] = min(e1, er)
         print(f"{k}: step {h:.1e}, relative error {e1:.2e} (difference), {er:.2e} (extrapolated)")
+    assert all(k in errs for k in ("kn", "kt", "gamman", "gammat")), errs
+    assert sum(k.startswith("r") for k in errs) >= 4, errs
     for k, e in errs.items():
         assert e < 1e-5, (k, fd2048[k], e)
 
