@@ -279,6 +279,8 @@ def run_gpu_arm(args, p, precision, rank, world):
     # the timed run continues the warm-up run: the engine is re-entered without a second setup;
     # steps run as replays of a captured CUDA graph (chunks of eng.chunk steps)
     eng = sim.last_engine
+    # the timed steps are whole graph replays: chunks of the largest divisor of K up to 64 steps
+    eng.chunk = max(c for c in range(1, min(64, K) + 1) if K % c == 0)
     eng.begin()
     eng.run(eng.chunk)                       # captures the graph (untimed, counts as warm-up)
     torch.cuda.synchronize()

@@ -310,7 +310,7 @@ class FusedEngine:
         """One chunk of steps as a CUDA graph (captured on first use and after a rebuild)."""
         sim = self.sim
         key = (sim.neighbor.build_count, sim.atom.buffers.xr.data_ptr(), sim.history.touch.data_ptr(),
-               sim.neighbor.nbr.data_ptr(), self.rows)
+               sim.neighbor.nbr.data_ptr(), self.rows, self.chunk)
         if self._graph is None or self._graph_key != key:
             self._graph = None
 
