@@ -279,6 +279,19 @@ class FusedEngine:
     def _engine_state(self) -> _lib.Engine:
         return _device.pull_struct(self._eng, _lib.Engine)
 
+    def _engine_and_status(self) -> tuple[_lib.Engine, int]:
+        """The engine record and the status word with one synchronisation (two copies into
+        page-locked memory)."""
+        nbytes = self._eng.numel()
+        if getattr(self, "_pull_host", None) is None or self._pull_host.numel() != nbytes + 4:
+            self._pull_host = torch.empty(nbytes + 4, dtype=torch.uint8, pin_memory=True)
+        h = self._pull_host
+        h[:nbytes].copy_(self._eng, non_blocking=True)
+        h[nbytes:].copy_(self.status.view(torch.uint8), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        raw = h.numpy()
+        return _lib.Engine.from_buffer_copy(raw[:nbytes].tobytes()), int(raw[nbytes:].view(np.int32)[0])
+
     def run(self, nsteps: int) -> None:
         """Advance `nsteps` steps."""
         sim = self.sim
@@ -287,7 +300,8 @@ class FusedEngine:
         start = sim.timestep
         target = start + int(nsteps)
         while True:
-            e = self._engine_state()
+            e, status = self._engine_and_status()  # after a chunk: its status too, in the same copy
+            self._check_status(status)
             done = int(e.step)
             if e.aborted:
                 self._rebuild_step(done + 1)
@@ -303,7 +317,6 @@ class FusedEngine:
             else:
                 for _ in range(count):
                     self._launch_step(L, st, atoms, nl_struct, params)
-            self._check_status()
         sim.timestep = target
 
     def _replay_chunk(self, L, atoms, nl_struct, params) -> None:
@@ -349,8 +362,8 @@ class FusedEngine:
         w = self.part[:4 * ng].view(torch.int32).cpu().numpy().view(np.uint32)
         return int(np.unpackbits(w.view(np.uint8)).sum())
 
-    def _check_status(self) -> None:
-        st = int(self.status.item())
+    def _check_status(self, st: int | None = None) -> None:
+        st = int(self.status.item()) if st is None else st
         if st & _lib.STATUS_BOX_NONPOSITIVE and self.deform is not None:
             self.deform.status.fill_(st)
             self.deform.check_status()
