@@ -101,6 +101,9 @@ class FusedEngine:
         self._hist_dw = False
         self.graph_replays = 0
         self.graph_kernel_launches = 0
+        # (engine record, status) as the last run() left them, while nothing has been launched since:
+        # the next run() starts from it instead of another synchronisation
+        self._known = None
 
     @property
     def sim(self):
@@ -146,6 +149,7 @@ class FusedEngine:
 
     def set_launch_shape(self, shape: tuple[int, int]) -> None:
         """Change the launch shape between steps (the scratch holds any shape's partials)."""
+        self._known = None
         self.launch_shape = (int(shape[0]), int(shape[1]))
         if self._n < 0:
             return
@@ -174,6 +178,7 @@ class FusedEngine:
     def begin(self, stop_step: int | None = None) -> None:
         """After Simulation.init_simulation(): hand the state to the fused step.  `stop_step`: fused
         launches do nothing once the step count reaches it (batched runs)."""
+        self._known = None
         sim = self.sim
         atom, nl = sim.atom, sim.neighbor
         n = atom.nlocal
@@ -219,6 +224,7 @@ class FusedEngine:
     def _prepare(self) -> None:
         """Split state and per-step constants for the current list, then the per-group
         contact bounds C uses to skip groups that cannot touch."""
+        self._known = None
         sim = self.sim
         nl = sim.neighbor
         L, st = _device.lib(), _device.stream()
@@ -250,6 +256,7 @@ class FusedEngine:
         self._hist_dw = dw
 
     def _launch_step(self, L, st, atoms, nl_struct, params) -> None:
+        self._known = None
         dbox, eng = self.sim.domain.dbox, self._eng.data_ptr()
         with _device.timed("fused_a"):
             rc = L.tmps_fused_a(atoms, dbox, eng, self.a_blocks, self.part.data_ptr(), st)
@@ -300,13 +307,18 @@ class FusedEngine:
         start = sim.timestep
         target = start + int(nsteps)
         while True:
-            e, status = self._engine_and_status()  # after a chunk: its status too, in the same copy
+            if self._known is not None:
+                e, status = self._known
+                self._known = None
+            else:
+                e, status = self._engine_and_status()  # after a chunk: its status too, in the same copy
             self._check_status(status)
             done = int(e.step)
             if e.aborted:
                 self._rebuild_step(done + 1)
                 continue
             if done >= target:
+                self._known = (e, status)
                 break
             atoms = self.atoms()
             nl_struct = sim.history.cstruct(sim.neighbor)
@@ -321,6 +333,7 @@ class FusedEngine:
 
     def _replay_chunk(self, L, atoms, nl_struct, params) -> None:
         """One chunk of steps as a CUDA graph (captured on first use and after a rebuild)."""
+        self._known = None
         sim = self.sim
         key = (sim.neighbor.build_count, sim.atom.buffers.xr.data_ptr(), sim.history.touch.data_ptr(),
                sim.neighbor.nbr.data_ptr(), self.rows, self.chunk)
@@ -370,6 +383,7 @@ class FusedEngine:
 
     def _rebuild_step(self, s: int) -> None:
         """Step `s` has had its first half-kick and drift; rebuild, then finish it."""
+        self._known = None
         sim = self.sim
         L = _device.lib()
         st = _device.stream()
@@ -404,6 +418,7 @@ class FusedEngine:
 
     def finish(self) -> None:
         """Settle pending updates and hand the state back to the per-hook path."""
+        self._known = None
         # the captured graph goes now, not whenever the engine is collected (which may be
         # during a later capture)
         self._graph = self._graph_key = None
