@@ -320,25 +320,29 @@ class FusedEngine:
             if done >= target:
                 self._known = (e, status)
                 break
-            atoms = self.atoms()
-            nl_struct = sim.history.cstruct(sim.neighbor)
-            params = sim.pair_style.params
             count = min(self.chunk, target - done)
             if self.graphs and count == self.chunk and _device.TIMED is None:
-                self._replay_chunk(L, atoms, nl_struct, params)
+                self._replay_chunk(L)
             else:
+                atoms = self.atoms()
+                nl_struct = sim.history.cstruct(sim.neighbor)
+                params = sim.pair_style.params
                 for _ in range(count):
                     self._launch_step(L, st, atoms, nl_struct, params)
         sim.timestep = target
 
-    def _replay_chunk(self, L, atoms, nl_struct, params) -> None:
-        """One chunk of steps as a CUDA graph (captured on first use and after a rebuild)."""
+    def _replay_chunk(self, L) -> None:
+        """One chunk of steps as a CUDA graph (captured on first use and after a rebuild; the launch
+        arguments are built only for a capture)."""
         self._known = None
         sim = self.sim
         key = (sim.neighbor.build_count, sim.atom.buffers.xr.data_ptr(), sim.history.touch.data_ptr(),
                sim.neighbor.nbr.data_ptr(), self.rows, self.chunk)
         if self._graph is None or self._graph_key != key:
             self._graph = None
+            atoms = self.atoms()
+            nl_struct = sim.history.cstruct(sim.neighbor)
+            params = sim.pair_style.params
 
             def chunk():
                 st = _device.stream()
