@@ -20,8 +20,6 @@
 //          last build), FP32 contact arithmetic and FP32 per-atom force
 //          accumulation; FP64 kept for the velocity and position updates, the
 //          per-contact shear history and the virial reduction.
-#include <atomic>
-
 #include "tmps_contact.cuh"
 #include "tmps_servo.cuh"
 
@@ -366,121 +364,10 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
     }
 }
 
-// A (single system) with its per-atom words staged in shared memory: each
-// thread copies the words of its next atom (the atom one grid stride on) into
-// shared memory with cp.async while it updates the current one, so a
-// thread's loads for two atoms are in flight at once without holding
-// registers.  Every thread reads only the slots it filled itself, so no
-// barrier is needed between the stages; two stages per block.  Same
-// arithmetic, order and outputs as a32_body.
-struct A32Stage {
-    float4 p[kBlockA], pl[kBlockA], v[kBlockA], w[kBlockA], q[kBlockA];
-    float wz[kBlockA], o0[3][kBlockA];
-    int32_t c[kBlockA];
-};
-constexpr size_t kA32StageBytes = 2 * sizeof(A32Stage);
-
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-
-__device__ __forceinline__ void a32_stage(const tmps_atoms& a, A32Stage& S, int i) {
-    const int t = threadIdx.x, n = a.n;
-    cp_async16(&S.p[t], reinterpret_cast<const float4*>(a.pos32) + i);
-    cp_async16(&S.pl[t], reinterpret_cast<const float4*>(a.pos32lo) + i);
-    cp_async16(&S.v[t], reinterpret_cast<const float4*>(a.vel32) + i);
-    cp_async16(&S.w[t], reinterpret_cast<const float4*>(a.om32) + i);
-    cp_async16(&S.q[t], reinterpret_cast<const float4*>(a.lo32) + i);
-    cp_async4(&S.wz[t], a.wlz32 + i);
-    cp_async4(&S.c[t], a.cell32 + i);
-    cp_async4(&S.o0[0][t], a.o0_32 + i);
-    cp_async4(&S.o0[1][t], a.o0_32 + n + i);
-    cp_async4(&S.o0[2][t], a.o0_32 + 2 * n + i);
-}
-
 __global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
                                                      tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
                                                      double* __restrict__ part) {
-    extern __shared__ __align__(16) unsigned char a32_smem[];
-    A32Stage* S = reinterpret_cast<A32Stage*>(a32_smem);
-    __shared__ float2 smem[6 * (kBlockA / 32)];
-    pdl_enter();
-    if (e->aborted || e->step >= e->stop_step) return;
-    const int n = a.n;
-    const int bid = blockIdx.x, nblk = gridDim.x;
-    const int nb = e->nblocks;  // partials are component-major, [6][nb]
-    const int t = threadIdx.x, lane = t & 31;
-    const int32_t s = (int32_t)(e->step + 1);
-    const float dth = e->dt_hi, dtl = e->dt_lo;
-    const float kick = e->final_pending ? dth : 0.5f * dth;  // merged half-kicks
-    const bool remap = b->remap_pending != 0;
-    bool hit = false;
-    float dd = 0.0f;
-    float Kh[6] = {0, 0, 0, 0, 0, 0}, Kl[6] = {0, 0, 0, 0, 0, 0};
-    const int stride = nblk * blockDim.x;
-    int i = bid * blockDim.x + t;
-    if (i < n) a32_stage(a, S[0], i);
-    cp_async_commit();
-    for (int buf = 0; i < n; i += stride, buf ^= 1) {
-        if (i + stride < n) a32_stage(a, S[buf ^ 1], i + stride);
-        cp_async_commit();
-        cp_async_wait1();  // this thread's copies of atom i have landed
-        const A32Stage& T = S[buf];
-        float4 p = T.p[t], pl = T.pl[t], v = T.v[t];
-        const float4 o = T.w[t], q = T.q[t];
-        float4 w = make_float4(o.x, o.y, o.z, 0.0f);
-        float4 vl = make_float4(o.w, q.x, q.y, 0.0f), wl = make_float4(q.z, q.w, T.wz[t], 0.0f);
-        if (force_live(flags, i)) {  // an unflagged atom's force is an exact zero: nothing to add
-            const float2 inv = __ldcs(reinterpret_cast<const float2*>(a.inv32) + i);  // 1/m, 1/I
-            const float km = kick * inv.x, kI = kick * inv.y;
-            dw_add(v.x, vl.x, km * __ldcs(a.f32 + i));
-            dw_add(v.y, vl.y, km * __ldcs(a.f32 + n + i));
-            dw_add(v.z, vl.z, km * __ldcs(a.f32 + 2 * n + i));
-            dw_add(w.x, wl.x, kI * __ldcs(a.torque32 + i));
-            dw_add(w.y, wl.y, kI * __ldcs(a.torque32 + n + i));
-            dw_add(w.z, wl.z, kI * __ldcs(a.torque32 + 2 * n + i));
-        }
-        if (remap) {
-            // remap x scales a cell-relative offset with the box: o += o * eps
-            dw_add(p.x, pl.x, p.x * e->eps_hi[0] + (p.x * e->eps_lo[0] + pl.x * e->eps_hi[0]));
-            dw_add(p.y, pl.y, p.y * e->eps_hi[1] + (p.y * e->eps_lo[1] + pl.y * e->eps_hi[1]));
-            dw_add(p.z, pl.z, p.z * e->eps_hi[2] + (p.z * e->eps_lo[2] + pl.z * e->eps_hi[2]));
-        }
-        // drift o += dt * v in double words
-        dw_add_prod(p.x, pl.x, dth, dtl, v.x, vl.x);
-        dw_add_prod(p.y, pl.y, dth, dtl, v.y, vl.y);
-        dw_add_prod(p.z, pl.z, dth, dtl, v.z, vl.z);
-        st4f(a.pos32, i, p);
-        st4f_cs(a.pos32lo, i, pl);
-        store_vw<true>(a, i, v, vl, w, wl);
-        // displacement since the build: offset change + cell origin change
-        const int32_t c = T.c[t];
-        const float d0 = ((p.x - T.o0[0][t]) + pl.x) + (float)cell_x(c) * e->dh32[0] + e->dlo32[0];
-        const float d1 = ((p.y - T.o0[1][t]) + pl.y) + (float)cell_y(c) * e->dh32[1] + e->dlo32[1];
-        const float d2 = ((p.z - T.o0[2][t]) + pl.z) + (float)cell_z(c) * e->dh32[2] + e->dlo32[2];
-        const float qq = (d0 * d0 + d1 * d1) + d2 * d2;
-        hit = hit || !(qq <= e->trigger32);  // NaN included (see a64_body)
-        dd = qq == qq ? fmaxf(dd, qq) : __int_as_float(0x7fffffff);
-        // kinetic term from the high words (vel32.w = m)
-        const float kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
-                              (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
-#pragma unroll
-        for (int k = 0; k < 6; ++k) dw_add(Kh[k], Kl[k], kin[k]);
-    }
-    if (__any_sync(0xffffffffu, hit) && lane == 0) e->disp_stamp = s;
-    note_displacement(e, dd);
-    block_sum_dw<6, kBlockA>(Kh, Kl, smem);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) reinterpret_cast<float2*>(part)[(size_t)k * nb + bid] = make_float2(Kh[k], Kl[k]);
-    }
+    a32_body(a, b, e, flags, part, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------- C
@@ -2237,23 +2124,18 @@ bool launch_ok() { return cudaPeekAtLastError() == cudaSuccess; }
 
 // Launch with programmatic stream serialization (see pdl_enter).
 template <typename... P, typename... A>
-void launch_pdl_smem(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t s, A&&... args) {
+void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, A&&... args) {
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3((unsigned)block);
-    cfg.dynamicSmemBytes = smem;
+    cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
-}
-
-template <typename... P, typename... A>
-void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, A&&... args) {
-    launch_pdl_smem(kernel, grid, block, 0, s, std::forward<A>(args)...);
 }
 
 bool mixed_ok(const tmps_atoms* a) {
@@ -2428,18 +2310,7 @@ int tmps_fused_a(const tmps_atoms* a, tmps_box* d_box, tmps_engine* d_eng, int32
     double* part = (double*)((char*)scratch + part_offset(n));  // A's partials come first
     if (mixed) {
         if (!mixed_ok(a)) return TMPS_ERR_BAD_ARG;
-        // the staged A's two stages need the opt-in shared memory size, set once per device
-        static std::atomic<uint64_t> smem_set{0};
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess) return TMPS_ERR_CUDA;
-        const uint64_t bit = 1ull << (dev & 63);
-        if (!(smem_set.load() & bit)) {
-            if (cudaFuncSetAttribute(k_a32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kA32StageBytes) !=
-                cudaSuccess)
-                return TMPS_ERR_CUDA;
-            smem_set.fetch_or(bit);
-        }
-        launch_pdl_smem(k_a32, g, kBlockA, kA32StageBytes, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
+        launch_pdl(k_a32, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     } else {
         launch_pdl(k_a64, g, kBlockA, s, *a, (const tmps_box*)d_box, d_eng, flags, part);
     }
