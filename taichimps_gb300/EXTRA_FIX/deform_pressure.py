@@ -287,6 +287,8 @@ class FixDeformPressure(Fix):
         dom.set_h_rate(self._strain_h_rate(dt), vremap=(self.remap == "v"))
         _device.push_struct(self._dservo, self.servo_struct())
         self.status.zero_()
+        # no kernel has written the status word since it was cleared: check_status need not read it
+        self.status_clean = True
 
     def end_of_step(self, atom, dt: float) -> None:
         if self.domain is None:
@@ -299,6 +301,7 @@ class FixDeformPressure(Fix):
             return
         L = _device.lib()
         st = _device.stream()
+        self.status_clean = False
         wsb = int(L.tmps_virial_workspace_bytes(atom.nlocal))
         if self._ws.numel() < wsb:
             self._ws = torch.zeros(wsb, dtype=torch.uint8, device=self.dev)
@@ -321,6 +324,8 @@ class FixDeformPressure(Fix):
         self.domain.mark_device_authoritative()
 
     def check_status(self) -> None:
+        if getattr(self, "status_clean", False):
+            return
         if int(self.status.item()) & _lib.STATUS_BOX_NONPOSITIVE:
             self.domain.pull()
             raise RuntimeError(

@@ -82,13 +82,48 @@ def struct_buffer(st: ctypes.Structure) -> torch.Tensor:
     return torch.zeros(ctypes.sizeof(st), dtype=torch.uint8, device=device())
 
 
+def _staged(raw: bytes) -> torch.Tensor:
+    """`raw` in page-locked host memory.  PyTorch's pinned-memory cache keeps the block from reuse
+    until the copies queued from it have run, so the caller need not wait for them."""
+    h = torch.empty(len(raw), dtype=torch.uint8, pin_memory=True)
+    ctypes.memmove(h.data_ptr(), raw, len(raw))
+    return h
+
+
 def push_struct(buf: torch.Tensor, st: ctypes.Structure) -> None:
-    """Host struct -> device buffer, ordered on the current stream."""
-    raw = np.frombuffer(bytes(st), dtype=np.uint8).copy()
-    buf.copy_(torch.from_numpy(raw), non_blocking=False)
+    """Host struct -> device buffer, ordered on the current stream (the host does not wait)."""
+    buf.copy_(_staged(bytes(st)), non_blocking=True)
+
+
+def push_fields(buf: torch.Tensor, st: ctypes.Structure, first: str, last: str) -> None:
+    """The fields `first` .. `last` (inclusive, in declaration order) of a host struct -> the same
+    bytes of the device buffer, ordered on the current stream; the other bytes are left as the device
+    has them."""
+    cls = type(st)
+    lo = getattr(cls, first).offset
+    hi = getattr(cls, last).offset + getattr(cls, last).size
+    buf[lo:hi].copy_(_staged(bytes(st)[lo:hi]), non_blocking=True)
 
 
 def pull_struct(buf: torch.Tensor, cls: type[ctypes.Structure]) -> ctypes.Structure:
     """Device buffer -> host struct (synchronises the stream)."""
-    raw = buf.cpu().numpy().tobytes()
-    return cls.from_buffer_copy(raw)
+    return pull_many([(buf, cls)])[0]
+
+
+def pull_many(items) -> list:
+    """Several device buffers -> host values with one synchronisation: `items` holds (buffer, ctypes
+    struct class) pairs, or (buffer, None) for the raw bytes as a numpy array."""
+    sizes = [b.numel() * b.element_size() for b, _ in items]
+    h = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
+    off = 0
+    for (b, _), sz in zip(items, sizes):
+        h[off:off + sz].copy_(b.reshape(-1).view(torch.uint8), non_blocking=True)
+        off += sz
+    torch.cuda.current_stream().synchronize()
+    raw = h.numpy()
+    out, off = [], 0
+    for (b, cls), sz in zip(items, sizes):
+        chunk = raw[off:off + sz]
+        out.append(cls.from_buffer_copy(chunk.tobytes()) if cls is not None else chunk.copy())
+        off += sz
+    return out

@@ -49,7 +49,15 @@ class Domain:
         """Bring the host mirror in step with the device (synchronises)."""
         if not self._host_stale:
             return
-        b = _device.pull_struct(self._dbox, _lib.Box)
+        self.take_pulled(_device.pull_struct(self._dbox, _lib.Box))
+
+    @property
+    def dbox_tensor(self):
+        """The device box record's byte buffer."""
+        return self._dbox
+
+    def take_pulled(self, b) -> None:
+        """Adopt a box record read from the device (the current one) as the host mirror."""
         self._boxlo = np.array(b.lo[:], dtype=np.float64)
         self._boxhi = np.array(b.hi[:], dtype=np.float64)
         self._prd = np.array(b.prd[:], dtype=np.float64)

@@ -98,6 +98,10 @@ class FusedEngine:
         self.launch_shape = (int(shape[0]), int(shape[1]))
         self._graph = None
         self._graph_key = None
+        # the arguments of the last chunk that ran as plain launches; the next chunk with the same
+        # arguments is captured (`capture_first`: capture at the first chunk instead)
+        self._seen_key = None
+        self.capture_first = False
         self._hist_dw = False
         self.graph_replays = 0
         self.graph_kernel_launches = 0
@@ -117,25 +121,25 @@ class FusedEngine:
     def _alloc(self, n: int) -> None:
         if n == self._n:
             return
-        f64 = dict(dtype=torch.float64, device=self.dev)
-        f32 = dict(dtype=torch.float32, device=self.dev)
-        self.rinv = None if self.mixed else torch.zeros((2, n), **f64)
+        # every per-atom array here is written in full by tmps_fused_prepare (and f32, t32 by begin)
+        # before any kernel reads it: left unset, in one allocation for the mixed form's eleven
+        self.rinv = None if self.mixed else torch.empty((2, n), dtype=torch.float64, device=self.dev)
         style, mixed = int(self.sim.pair_style.params.style), 1 if self.mixed else 0
         self._shape(n)
         self.part = torch.zeros(int(_device.lib().tmps_fused_scratch_bytes(n, style, mixed)), dtype=torch.uint8,
                                 device=self.dev)
         if self.mixed:
-            self.pos32 = torch.zeros((n, 4), **f32)
-            self.pos32lo = torch.zeros((n, 4), **f32)
-            self.lo32 = torch.zeros((n, 4), **f32)
-            self.wlz32 = torch.zeros(n, **f32)
-            self.inv32 = torch.zeros((n, 2), **f32)
-            self.vel32 = torch.zeros((n, 4), **f32)
-            self.om32 = torch.zeros((n, 4), **f32)
-            self.f32 = torch.zeros((3, n), **f32)
-            self.t32 = torch.zeros((3, n), **f32)
-            self.o0 = torch.zeros((3, n), **f32)
-            self.cell32 = torch.zeros(n, dtype=torch.int32, device=self.dev)
+            # (name, FP32 words per atom, shape); each slice starts on a 256-byte boundary
+            parts = [("pos32", 4, (n, 4)), ("pos32lo", 4, (n, 4)), ("lo32", 4, (n, 4)), ("wlz32", 1, (n,)),
+                     ("inv32", 2, (n, 2)), ("vel32", 4, (n, 4)), ("om32", 4, (n, 4)), ("f32", 3, (3, n)),
+                     ("t32", 3, (3, n)), ("o0", 3, (3, n)), ("cell32", 1, (n,))]
+            r64 = lambda w: (w + 63) // 64 * 64
+            flat = torch.empty(sum(r64(w * n) for _, w, _ in parts), dtype=torch.float32, device=self.dev)
+            off = 0
+            for name, w, shape in parts:
+                t = flat[off:off + w * n].view(shape)
+                setattr(self, name, t.view(torch.int32) if name == "cell32" else t)
+                off += r64(w * n)
         self._n = n
 
     def _shape(self, n: int) -> None:
@@ -205,10 +209,11 @@ class FusedEngine:
         e.stop_step = (1 << 62) if stop_step is None else int(stop_step)
         _device.push_struct(self._eng, e)
         if self.deform is not None:
+            # the run counters only; the rest of the servo record stays as the device has it
             fx = self.deform
-            sv = _device.pull_struct(fx._dservo, _lib.Servo)
+            sv = _lib.Servo()
             sv.nsteps, sv.nsteps_total, sv.step_count, sv.nevery = fx.nsteps, fx.nsteps_total, fx.step_count, fx.nevery
-            _device.push_struct(fx._dservo, sv)
+            _device.push_fields(fx._dservo, sv, "nsteps", "nevery")
         self._prepare()
         log = self.deform.pressure_log if self.deform is not None else None
         rc = _device.lib().tmps_fused_pressure_log(self._eng.data_ptr(), None if log is None else log.data_ptr(),
@@ -220,6 +225,9 @@ class FusedEngine:
             self.f32.copy_(b.f)
             self.t32.copy_(b.torque)
         self.status.zero_()
+        # the record as pushed above, in the fields run() reads (step, aborted), and a clear status:
+        # the first run() starts without a synchronisation
+        self._known = (e, 0)
 
     def _prepare(self) -> None:
         """Split state and per-step constants for the current list, then the per-group
@@ -343,6 +351,15 @@ class FusedEngine:
             atoms = self.atoms()
             nl_struct = sim.history.cstruct(sim.neighbor)
             params = sim.pair_style.params
+            if self._seen_key != key and not self.capture_first:
+                # a chunk whose arguments have not been seen before runs as plain launches: the device
+                # starts on it at once, where a capture would hold it idle, and a run of one chunk
+                # (or one chunk between rebuilds) never pays for a graph it would replay once
+                self._seen_key = key
+                st = _device.stream()
+                for _ in range(self.chunk):
+                    self._launch_step(L, st, atoms, nl_struct, params)
+                return
 
             def chunk():
                 st = _device.stream()
@@ -383,6 +400,7 @@ class FusedEngine:
         st = int(self.status.item()) if st is None else st
         if st & _lib.STATUS_BOX_NONPOSITIVE and self.deform is not None:
             self.deform.status.fill_(st)
+            self.deform.status_clean = False
             self.deform.check_status()
 
     def _rebuild_step(self, s: int) -> None:
@@ -435,15 +453,21 @@ class FusedEngine:
             _lib.check(L.tmps_mixed_unpack(atoms, sim.domain.dbox, st), "tmps_mixed_unpack")
         self._history_form(False)
         sim.domain.mark_device_authoritative()
-        e = self._engine_state()
+        # the engine record, the status word, the box and the servo record: one synchronisation
+        items = [(self._eng, _lib.Engine), (self.status, None), (sim.domain.dbox_tensor, _lib.Box)]
+        if self.deform is not None:
+            items.append((self.deform._dservo, _lib.Servo))
+        got = _device.pull_many(items)
+        e, status, box = got[0], int(got[1].view(np.int32)[0]), got[2]
+        sim.domain.take_pulled(box)
         sim.timestep = int(e.step)
         sim.neighbor.current_step = int(e.step)
         sim.neighbor.last_build_step = int(e.last_build_step)
         for fx in sim.fixes:
             fx.timestep = sim.timestep
         if self.deform is not None:
-            sv = _device.pull_struct(self.deform._dservo, _lib.Servo)
+            sv = got[3]
             self.deform.nsteps, self.deform.step_count = int(sv.nsteps), int(sv.step_count)
         if sim.integrator is not None:
             sim.integrator.timestep = sim.timestep
-        self._check_status()
+        self._check_status(status)

@@ -138,11 +138,40 @@ def test_graph_replay_matches_eager_launches(gpu, oracle, precision, path):
         sim.setup_run(200)
         sim.init_simulation()
         eng = FusedEngine(sim, precision, chunk=32, graphs=graphs, contact_path=path)
+        eng.capture_first = graphs  # every whole chunk a graph replay, the first after each rebuild too
         eng.begin()
         eng.run(200)
         eng.finish()
         if graphs:
             assert eng.graph_replays > 0 and eng.rebuilds > 0
+        states.append(gpu_state(sim))
+    for k in ("x", "v", "omega", "f", "torque"):
+        np.testing.assert_array_equal(states[0][k], states[1][k])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_first_chunk_runs_without_capture(gpu, oracle, precision):
+    """A chunk whose launch arguments are new runs as plain launches; the next chunk with the same
+    arguments is captured and replayed.  Three chunks without a rebuild: two replays, and the same
+    bits as capturing from the first chunk on."""
+    from taichimps_gb300.engine import FusedEngine
+    from taichimps_gb300.packing import make_packing_box
+    p = make_packing_box(1000, 0.8, 1.2, 0.45, seed=5, vel_sigma=0.5)
+    L = [float(v) for v in p["L"]]
+    states = []
+    for capture_first in (False, True):
+        sim, _ = make_twin(oracle, p["x"], p["radius"], 2.5, [0.0] * 3, L, v=p["v"], pair="hertz/history",
+                           dt=5e-5)
+        sim.precision = precision
+        sim.setup_run(24)
+        sim.init_simulation()
+        eng = FusedEngine(sim, precision, chunk=8)
+        eng.capture_first = capture_first
+        eng.begin()
+        eng.run(24)
+        eng.finish()
+        assert eng.rebuilds == 0
+        assert eng.graph_replays == (3 if capture_first else 2)
         states.append(gpu_state(sim))
     for k in ("x", "v", "omega", "f", "torque"):
         np.testing.assert_array_equal(states[0][k], states[1][k])
