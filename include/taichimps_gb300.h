@@ -274,6 +274,38 @@ int tmps_verlet_final(const tmps_atoms* a, double dt, void* stream);
 /* AtomSystem.clear_forces (src/taichimps/atom.py:201-220). */
 int tmps_clear_forces(const tmps_atoms* a, void* stream);
 
+/* ---- particle input and output ---------------------------------------- */
+
+/* AtomSystem.add_particles (src/taichimps/atom.py:55-145) for a system's first
+ * n = a->n particles: writes xr, vm, om (rmass = (4/3) pi r^3 density, moment
+ * of inertia 0.4 m r r), tag (1..n when `tag` is NULL), uid = 0..n-1, and
+ * zeroes f, torque, x0 and virial.  x, v, omega: double[n][3] (v, omega NULL:
+ * zero); radius, density: double[n], or NULL for radius_value /
+ * density_value on every atom.  Each input may be device memory or
+ * page-locked host memory (read in place); pageable memory is refused
+ * (TMPS_ERR_BAD_ARG).  *d_max_radius (device double) receives the largest
+ * radius. */
+int tmps_atoms_assemble(const tmps_atoms* a, const double* x, const double* v, const double* omega,
+                        const double* radius, double radius_value, const double* density, double density_value,
+                        const int32_t* tag, double* d_max_radius, void* stream);
+
+/* Fields of tmps_atoms_read (the Taichi fields of src/taichimps/atom.py:36-55). */
+enum {
+    TMPS_FIELD_X = 0,       /* double[n][3] */
+    TMPS_FIELD_V = 1,       /* double[n][3] */
+    TMPS_FIELD_OMEGA = 2,   /* double[n][3] */
+    TMPS_FIELD_RADIUS = 3,  /* double[n] */
+    TMPS_FIELD_RMASS = 4,   /* double[n] */
+    TMPS_FIELD_F = 5,       /* double[n][3] */
+    TMPS_FIELD_TORQUE = 6,  /* double[n][3] */
+    TMPS_FIELD_VIRIAL = 7,  /* double[n][6] */
+};
+
+/* The field's to_numpy(): its rows in insertion order (row j = the atom with
+ * uid j) into `out`, device memory or page-locked host memory (written in
+ * place).  d_slot_of: int32[n] device scratch. */
+int tmps_atoms_read(const tmps_atoms* a, int32_t field, int32_t* d_slot_of, double* out, void* stream);
+
 /* FixDampingCundall.post_force (src/taichimps/EXTRA_FIX/damping_cundall.py:206-234). */
 int tmps_damping_cundall(const tmps_atoms* a, double gamma_lin, double gamma_ang, void* stream);
 
@@ -469,6 +501,13 @@ int tmps_fused_pressure_log(tmps_engine* d_eng, double* h_log, int32_t len, void
  * on `stream` and count 8 x iters x blocks x threads DFMA.  Each thread
  * writes one double to d_out (blocks x threads slots); nothing is allocated. */
 int tmps_probe_fp64(int32_t blocks, int32_t threads, int32_t iters, double* d_out, void* stream);
+
+/* Self-check of the library's integer-operation double<->float conversions
+ * against the hardware's rounding: which 0 (float)a, 1 (double)(float)a,
+ * 2 the hi + lo split of a (two outputs per operand).  d_mine and d_hw
+ * (n doubles, 2n for which 2) must agree bit for bit.  No reference
+ * counterpart. */
+int tmps_selftest_arith(int32_t which, const double* d_a, int32_t n, double* d_mine, double* d_hw, void* stream);
 
 /* ---- batched runs ----------------------------------------------------------
  * Many independent systems of uneven size (each with its own box, contact

@@ -176,6 +176,8 @@ class AdjBar(ctypes.Structure):
 TMPS_OK, TMPS_ERR_BAD_ARG, TMPS_ERR_CUDA, TMPS_ERR_TOO_LARGE = 0, 1, 2, 3
 NOALLOC_MAX_ATOMS, NOALLOC_MAX_CELLS = 1048576, 200000
 STATUS_NLIST_OVERFLOW, STATUS_NONFINITE, STATUS_BOX_NONPOSITIVE, STATUS_CELL_OVERFLOW = 1, 2, 4, 8
+# fields of tmps_atoms_read
+FIELD = {"x": 0, "v": 1, "omega": 2, "radius": 3, "rmass": 4, "f": 5, "torque": 6, "virial": 7}
 
 # Every entry point the header declares, with its ctypes signature.
 _SIGS = {
@@ -186,6 +188,9 @@ _SIGS = {
     "tmps_verlet_initial": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),
     "tmps_verlet_final": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_vp]),
     "tmps_clear_forces": (c_i32, [ctypes.POINTER(Atoms), c_vp]),
+    "tmps_atoms_assemble": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp, c_vp, c_f64, c_vp, c_f64, c_vp, c_vp,
+                                    c_vp]),
+    "tmps_atoms_read": (c_i32, [ctypes.POINTER(Atoms), c_i32, c_vp, c_vp, c_vp]),
     "tmps_damping_cundall": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_f64, c_vp]),
     "tmps_skin_check": (c_i32, [ctypes.POINTER(Atoms), c_f64, c_i32, c_vp, c_vp]),
     "tmps_pbc": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp]),
@@ -214,6 +219,7 @@ _SIGS = {
     "tmps_fused_servo": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "tmps_fused_blocks": (c_i32, [c_i32, c_i32, c_i32]),
     "tmps_probe_fp64": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp]),
+    "tmps_selftest_arith": (c_i32, [c_i32, c_vp, c_i32, c_vp, c_vp, c_vp]),
     "tmps_fused_shape": (c_i32, [c_i32, c_i32, c_i32, c_i32, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32)]),
     "tmps_fused_scratch_bytes": (ctypes.c_int64, [c_i32, c_i32, c_i32]),
     "tmps_fused_settle": (c_i32, [ctypes.POINTER(Atoms), c_vp, c_vp, c_vp]),

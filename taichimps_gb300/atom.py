@@ -64,13 +64,20 @@ class FieldView:
         shape = (a.max_atoms,) if self._w == 1 else (a.max_atoms, self._w)
         if not a.nlocal:
             return np.zeros(shape, dtype=self._dtype)
-        # back to insertion order on the device, then one contiguous copy
-        vals = self._internal().detach()
-        ordered = torch.empty(vals.shape, dtype=vals.dtype, device=vals.device)
-        ordered[a.buffers.uid.long()] = vals
-        # through page-locked memory: a direct DMA at link speed instead of a staged copy
-        staged = torch.empty(vals.shape, dtype=vals.dtype, pin_memory=True)
-        staged.copy_(ordered, non_blocking=True)
+        if self._name in _lib.FIELD:
+            # one kernel writes the rows in insertion order straight into page-locked memory
+            shape_n = (a.nlocal,) if self._w == 1 else (a.nlocal, self._w)
+            staged = torch.empty(shape_n, dtype=torch.float64, pin_memory=True)
+            rc = _device.lib().tmps_atoms_read(a.cstruct(), _lib.FIELD[self._name], a.slot_scratch().data_ptr(),
+                                               staged.data_ptr(), _device.stream())
+            _lib.check(rc, "tmps_atoms_read")
+        else:
+            # back to insertion order on the device, then one contiguous copy
+            vals = self._internal().detach()
+            ordered = torch.empty(vals.shape, dtype=vals.dtype, device=vals.device)
+            ordered[a.buffers.uid.long()] = vals
+            staged = torch.empty(vals.shape, dtype=vals.dtype, pin_memory=True)
+            staged.copy_(ordered, non_blocking=True)
         torch.cuda.current_stream().synchronize()
         host = staged.numpy().astype(self._dtype, copy=False)
         if a.nlocal == a.max_atoms:
@@ -127,7 +134,9 @@ class AtomSystem:
         self.rmass = FieldView(self, "rmass", 1, np.float64)
         self.tag = FieldView(self, "tag", 1, np.int32)
         self.virial = FieldView(self, "virial", 6, np.float64)
-        self.max_radius = 0.0
+        self._max_radius, self._max_radius_dev = 0.0, None
+        self._pending_inputs = None
+        self._slot_of: torch.Tensor | None = None
         self._listeners: list = []
 
     # ------------------------------------------------------------ views
@@ -149,6 +158,12 @@ class AtomSystem:
             m, r = b.vm[:, 3], b.xr[:, 3]
             b.om[:, 3] = ((0.4 * m) * r) * r
             self.max_radius = float(b.xr[:, 3].max().item()) if self.nlocal else 0.0
+
+    def slot_scratch(self) -> torch.Tensor:
+        """int32[n] device scratch of tmps_atoms_read."""
+        if self._slot_of is None or self._slot_of.numel() < self.nlocal:
+            self._slot_of = torch.empty(max(self.nlocal, 1), dtype=torch.int32, device=self.device)
+        return self._slot_of
 
     def uid_host(self) -> np.ndarray:
         if self._uid_cache is None:
@@ -187,12 +202,13 @@ class AtomSystem:
         `rmass` (not in the reference): the masses as given, for a system read back from a restart
         file, which stores them -- recomputing them from a density would round differently."""
         tens = {k: a for k, a in (("x", x), ("v", v), ("omega", omega)) if isinstance(a, torch.Tensor)}
-        if isinstance(radius, torch.Tensor):
-            radius = radius.detach().cpu().numpy()
-        if tens and rmass is None and self.nlocal == 0 and all(t.dtype == torch.float64 and t.dim() == 2 and t.shape[1] == 3
-                                              for t in tens.values()):
+        if (tens and rmass is None and self.nlocal == 0 and "x" in tens
+                and all(t.dtype == torch.float64 and t.dim() == 2 and t.shape[1] == 3 for t in tens.values())
+                and all(isinstance(a, torch.Tensor) for a in (v, omega) if a is not None)):
             self._add_first_tensors(tens, radius, density, tag, atom_type)
             return
+        if isinstance(radius, torch.Tensor):
+            radius = radius.detach().cpu().numpy()
         x = x.detach().cpu().numpy() if isinstance(x, torch.Tensor) else x
         v = v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
         omega = omega.detach().cpu().numpy() if isinstance(omega, torch.Tensor) else omega
@@ -279,51 +295,86 @@ class AtomSystem:
 
     def _add_first_tensors(self, tens, radius, density, tag, atom_type) -> None:
         """add_particles into an empty system from float64 [n, 3] tensors (x; v and omega optional):
-        records, mass and inertia assembled on the device, in the reference's expression order
-        ((4/3 pi) r^3 density, ((0.4 m) r) r) with r^3 as r r r -- within an ulp of numpy's pow,
-        which the array path uses -- so a large system does not wait on element-wise host math."""
+        the records, masses and moments of inertia are assembled by one kernel (tmps_atoms_assemble)
+        that reads page-locked host or device arrays in place, with r^3 rounded once (as numpy's
+        r**3 of the array path rounds it) and the products in the reference's order; the largest
+        radius stays on the device until something reads it."""
         dev = self.device
-        xt = tens["x"]
+        L = _device.lib()
+        keep = []  # inputs staged for the kernel, alive until it has run
+
+        def readable(t: torch.Tensor, shape_n3: bool) -> torch.Tensor:
+            t = t.detach()
+            if t.dtype != torch.float64 or not t.is_contiguous():
+                t = t.to(torch.float64).contiguous()
+            if not (t.is_cuda or t.is_pinned()):
+                t = t.to(dev, non_blocking=False)
+            keep.append(t)
+            return t
+
+        xt = readable(tens["x"], True)
         n = int(xt.shape[0])
         if n > self.max_atoms:
             raise ValueError(f"Exceeded max_atoms capacity: {n} > {self.max_atoms}")
-        if torch.is_tensor(radius):
-            rad_d = radius.to(dev, dtype=torch.float64, non_blocking=True).reshape(-1)
-        else:
-            rad_np = np.asarray(radius, dtype=np.float64)
-            rad_d = (torch.full((n,), float(rad_np), dtype=torch.float64, device=dev) if rad_np.ndim == 0
-                     else torch.from_numpy(np.ascontiguousarray(rad_np)).to(dev))
-        if rad_d.numel() == 1 and n != 1:
-            rad_d = rad_d.expand(n).contiguous()
+
+        def per_atom(val, what):
+            """(pointer or None, value for every atom) of a per-atom double or a scalar."""
+            if torch.is_tensor(val):
+                t = readable(val.reshape(-1), False)
+                if t.numel() == 1:
+                    return None, float(t.cpu()[0])
+                if t.numel() != n:
+                    raise ValueError(f"{what}: {t.numel()} values for {n} particles")
+                return t.data_ptr(), 0.0
+            a = np.asarray(val, dtype=np.float64)
+            if a.ndim == 0 or a.size == 1:
+                return None, float(a.reshape(-1)[0])
+            if a.size != n:
+                raise ValueError(f"{what}: {a.size} values for {n} particles")
+            t = torch.from_numpy(np.ascontiguousarray(a.reshape(-1))).to(dev)
+            keep.append(t)
+            return t.data_ptr(), 0.0
+
+        r_ptr, r_val = per_atom(radius, "radius")
+        d_ptr, d_val = per_atom(density, "density")
+        v_ptr = readable(tens["v"], True).data_ptr() if "v" in tens else None
+        w_ptr = readable(tens["omega"], True).data_ptr() if "omega" in tens else None
+        tag_ptr = None
+        if tag is not None:
+            tt = torch.from_numpy(np.ascontiguousarray(np.asarray(tag, dtype=np.int32))).to(dev)
+            keep.append(tt)
+            tag_ptr = tt.data_ptr()
         types = (np.full(n, int(atom_type), dtype=np.int32) if np.isscalar(atom_type)
                  else np.asarray(atom_type, dtype=np.int32))
-        nb = _Buffers(n, dev)
-        nb.xr[:, :3] = xt.to(dev, non_blocking=True)
-        if "v" in tens:
-            nb.vm[:, :3] = tens["v"].to(dev, non_blocking=True)
-        if "omega" in tens:
-            nb.om[:, :3] = tens["omega"].to(dev, non_blocking=True)
-        dens_d = (float(density) if np.isscalar(density)
-                  else torch.from_numpy(np.ascontiguousarray(np.asarray(density, dtype=np.float64))).to(dev))
-        vol = ((4.0 / 3.0) * np.pi) * ((rad_d * rad_d) * rad_d)
-        mass = vol * dens_d
-        nb.xr[:, 3] = rad_d
-        nb.vm[:, 3] = mass
-        nb.om[:, 3] = ((0.4 * mass) * rad_d) * rad_d
-        if tag is None:
-            nb.tag.copy_(torch.arange(1, n + 1, dtype=torch.int32, device=dev))
-        else:
-            nb.tag.copy_(torch.from_numpy(np.asarray(tag, dtype=np.int32)).to(dev))
-        nb.uid.copy_(torch.arange(n, dtype=torch.int32, device=dev))
+        nb = _Buffers(n, dev, fill=False)  # the kernel writes every array
         self._buf = nb
         self._alt = _Buffers(n, dev, fill=False)
+        self.nlocal = n
+        rmax = torch.empty(1, dtype=torch.float64, device=dev)
+        rc = L.tmps_atoms_assemble(self.cstruct(nb), xt.data_ptr(), v_ptr, w_ptr, r_ptr, r_val, d_ptr, d_val,
+                                   tag_ptr, rmax.data_ptr(), _device.stream())
+        _lib.check(rc, "tmps_atoms_assemble")
+        # page-locked inputs are read in place: held until a synchronisation shows the kernel has run
+        self._pending_inputs = keep
         self.atom_type_host = types
         self.mask_host = np.ones(n, dtype=np.int32)
-        self.nlocal = n
         self._uid_cache = None
-        self.max_radius = float(rad_d.max()) if n else 0.0
+        self._max_radius, self._max_radius_dev = 0.0, rmax
         for cb in self._listeners:
             cb()
+
+    @property
+    def max_radius(self) -> float:
+        """The largest radius (a device value from tmps_atoms_assemble is read on first use)."""
+        if self._max_radius_dev is not None:
+            self._max_radius = float(self._max_radius_dev.item())
+            self._max_radius_dev = None
+            self._pending_inputs = None
+        return self._max_radius
+
+    @max_radius.setter
+    def max_radius(self, value: float) -> None:
+        self._max_radius, self._max_radius_dev = float(value), None
 
     def _gather_all(self) -> dict[str, np.ndarray]:
         """All per-atom arrays in insertion order (host copies)."""

@@ -47,6 +47,48 @@ TMPS_DEV float approx_f32(double x) {
 // |a| + |b| + |c|
 TMPS_DEV float l1f(float a, float b, float c) { return (fabsf(a) + fabsf(b)) + fabsf(c); }
 
+// Conversions between double and float done with integer operations, which
+// issue on the wide integer pipes instead of this part's narrow FP64 pipe.
+// Both give the same bits as the hardware conversion; the rare operands
+// outside the plain case (results below the FP32 normal range, infinities,
+// NaNs) go to the hardware conversion.
+
+// (float)x, round to nearest even
+TMPS_DEV float f32_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    if ((b << 1) == 0ull) return __uint_as_float(sign);  // +-0
+    const int e = (int)((b >> 52) & 0x7ff);
+    const int ef = e - 1023 + 127;
+    if (e == 0x7ff || ef <= 0 || ef >= 255) return (float)x;
+    const unsigned long long m = b & 0xfffffffffffffull;
+    uint32_t keep = (uint32_t)(m >> 29);
+    const uint32_t rest = (uint32_t)(m & 0x1fffffffull);
+    if (rest > 0x10000000u || (rest == 0x10000000u && (keep & 1u))) ++keep;
+    // a carry out of the significand steps the exponent (to infinity past the top)
+    return __uint_as_float(sign | (((uint32_t)ef << 23) + keep));
+}
+
+// (double)f, exact
+TMPS_DEV double f64_of(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const uint32_t e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) {
+        if ((u << 1) == 0u) return __longlong_as_double((long long)sign);  // +-0
+        return (double)f;
+    }
+    const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | m));
+}
+
+// hi + lo of a double as two floats: hi = (float)v, lo = (float)(v - hi)
+// (v - hi is exact in FP64)
+TMPS_DEV void split_dw(double v, float& hi, float& lo) {
+    hi = f32_rn(v);
+    lo = f32_rn(__dsub_rn(v, f64_of(hi)));
+}
+
 TMPS_DEV double4 ld4(const double* p, int i) { return reinterpret_cast<const double4*>(p)[i]; }
 TMPS_DEV void st4(double* p, int i, double4 v) { reinterpret_cast<double4*>(p)[i] = v; }
 TMPS_DEV float4 ld4f(const float* p, int i) { return reinterpret_cast<const float4*>(p)[i]; }

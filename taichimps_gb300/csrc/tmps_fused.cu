@@ -39,11 +39,8 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// hi + lo of a double as two floats
-__device__ __forceinline__ void split(double v, float& hi, float& lo) {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
-}
+// hi + lo of a double as two floats (integer-op conversions: off the FP64 pipe)
+__device__ __forceinline__ void split(double v, float& hi, float& lo) { split_dw(v, hi, lo); }
 
 // |a| >= |b| (or a == 0): s + e == a + b exactly
 __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
@@ -525,6 +522,9 @@ __global__ void __launch_bounds__(256) k_bitonic_global(uint64_t* __restrict__ k
 
 // Stages k_lo..k_hi of the bitonic sort inside chunks of `chunk` keys (the
 // first stage from j = j_first), one block of chunk / 2 threads per chunk.
+// (Measured: 2048-key chunks, one pair per thread and stage, beat 16384-key
+// chunks in 128 KB of shared memory -- fewer launches, but each block then
+// runs 91 barrier-separated stages at four pairs per thread.)
 constexpr int kSortChunk = 2048;
 __global__ void __launch_bounds__(kSortChunk / 2) k_bitonic_shared(uint64_t* __restrict__ keys, int chunk, int k_lo,
                                                                  int k_hi, int j_first) {
@@ -1994,7 +1994,7 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
         split(xx[k] - origin, oh[k], ol[k]);
         // the skin check's reference: the position at the last build, as an
         // offset from the same origin (x0 is kept by the build in FP64)
-        a.o0_32[k * n + i] = (float)(a.x0[k * n + i] - origin);
+        a.o0_32[k * n + i] = f32_rn(a.x0[k * n + i] - origin);
     }
     a.cell32[i] = cx | (cy << 10) | (cz << 20);
     float rh, rl;
@@ -2004,8 +2004,8 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
     float vh[3], vlo[3], wh[3], wlo[3];
     split(v.x, vh[0], vlo[0]); split(v.y, vh[1], vlo[1]); split(v.z, vh[2], vlo[2]);
     split(w.x, wh[0], wlo[0]); split(w.y, wh[1], wlo[1]); split(w.z, wh[2], wlo[2]);
-    reinterpret_cast<float2*>(a.inv32)[i] = make_float2((float)(1.0 / v.w), (float)(1.0 / w.w));
-    store_vw<false>(a, i, make_float4(vh[0], vh[1], vh[2], (float)v.w), make_float4(vlo[0], vlo[1], vlo[2], 0.0f),
+    reinterpret_cast<float2*>(a.inv32)[i] = make_float2(f32_rn(1.0 / v.w), f32_rn(1.0 / w.w));
+    store_vw<false>(a, i, make_float4(vh[0], vh[1], vh[2], f32_rn(v.w)), make_float4(vlo[0], vlo[1], vlo[2], 0.0f),
                     make_float4(wh[0], wh[1], wh[2], 0.0f), make_float4(wlo[0], wlo[1], wlo[2], 0.0f));
 }
 
@@ -2045,16 +2045,17 @@ __global__ void __launch_bounds__(kBlockA) k_unpack(tmps_atoms a, const tmps_box
     const int cc[3] = {cell_x(c), cell_y(c), cell_z(c)};
     const float oh[3] = {p.x, p.y, p.z}, ol[3] = {pl.x, pl.y, pl.z};
     double xx[3];
-    for (int k = 0; k < 3; ++k) xx[k] = (b->lo[k] + (double)cc[k] * b->hcell[k]) + ((double)oh[k] + (double)ol[k]);
+    // float -> double widenings with integer operations (exact; off the FP64 pipe)
+    for (int k = 0; k < 3; ++k) xx[k] = (b->lo[k] + (double)cc[k] * b->hcell[k]) + (f64_of(oh[k]) + f64_of(ol[k]));
     x.x = xx[0]; x.y = xx[1]; x.z = xx[2];
-    v.x = (double)vv.x + (double)vl.x; v.y = (double)vv.y + (double)vl.y; v.z = (double)vv.z + (double)vl.z;
-    w.x = (double)ww.x + (double)wl.x; w.y = (double)ww.y + (double)wl.y; w.z = (double)ww.z + (double)wl.z;
+    v.x = f64_of(vv.x) + f64_of(vl.x); v.y = f64_of(vv.y) + f64_of(vl.y); v.z = f64_of(vv.z) + f64_of(vl.z);
+    w.x = f64_of(ww.x) + f64_of(wl.x); w.y = f64_of(ww.y) + f64_of(wl.y); w.z = f64_of(ww.z) + f64_of(wl.z);
     st4(a.xr, i, x);
     st4(a.vm, i, v);
     st4(a.om, i, w);
     for (int k = 0; k < 3; ++k) {
-        a.f[k * n + i] = (double)a.f32[k * n + i];
-        a.torque[k * n + i] = (double)a.torque32[k * n + i];
+        a.f[k * n + i] = f64_of(a.f32[k * n + i]);
+        a.torque[k * n + i] = f64_of(a.torque32[k * n + i]);
     }
 }
 

@@ -21,31 +21,43 @@ constexpr int kScanBlock = 1024;
 // Cell of one position: floor(((x - lo) / prd) / csize), clamped.  The
 // reference's lamda for an orthogonal box adds products with zero tilt terms,
 // which leave the quotient unchanged.
-__device__ __forceinline__ int3 cell_coord(const tmps_box* __restrict__ b, double x, double y,
-                                           double z) {
-    double xx[3] = {x, y, z};
-    int c[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        double lam = __ddiv_rn(__dsub_rn(xx[k], b->lo[k]), b->prd[k]);
-        double q = floor(__ddiv_rn(lam, b->csize[k]));
-        // clamp in floating point first so a stray NaN/Inf cannot overflow
-        // the int conversion; NaN falls to cell 0
-        int ck = q >= (double)(b->g[k] - 1) ? b->g[k] - 1 : (q > 0.0 ? (int)q : 0);
-        c[k] = ck;
-    }
-    return make_int3(c[0], c[1], c[2]);
+//
+// The two divisions are correctly rounded, and only the floor of the second
+// quotient matters: t = (x - lo) * (1/prd) * (1/csize) with the reciprocals
+// rounded once differs from the exact chain's quotient by a few ulps of t
+// (relative ~1e-15), so wherever t lies further than 1e-12 (1 + |t|) from an
+// integer both floors agree and no division is needed; within that margin
+// (or for a NaN) the exact chain decides.  `rcp` holds 1/prd and 1/csize.
+__device__ __forceinline__ int cell_axis(double x, double lo, double prd, double csize, double rprd,
+                                         double rcs, int g) {
+    const double d = __dsub_rn(x, lo);
+    const double t = __dmul_rn(__dmul_rn(d, rprd), rcs);
+    double q = floor(t);
+    const double r = __dsub_rn(t, q);
+    const double m = 1e-12 * (1.0 + fabs(t));
+    if (!(r > m && r < 1.0 - m)) q = floor(__ddiv_rn(__ddiv_rn(d, prd), csize));
+    // clamp in floating point first so a stray NaN/Inf cannot overflow the
+    // int conversion; NaN falls to cell 0
+    return q >= (double)(g - 1) ? g - 1 : (q > 0.0 ? (int)q : 0);
 }
 
 __global__ void __launch_bounds__(kBlock) k_bin(tmps_atoms a, const tmps_box* __restrict__ b,
                                                 const int32_t* __restrict__ rank, int32_t* old_cell,
                                                 int32_t* count, int32_t* status) {
+    __shared__ double rprd[3], rcs[3];
+    if (threadIdx.x < 3) {
+        rprd[threadIdx.x] = 1.0 / b->prd[threadIdx.x];
+        rcs[threadIdx.x] = 1.0 / b->csize[threadIdx.x];
+    }
+    __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double4 x = ld4(a.xr, i);
     if (!isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z)) atomicOr(status, TMPS_STATUS_NONFINITE);
-    int3 c = cell_coord(b, x.x, x.y, x.z);
-    int lin = c.x + c.y * b->g[0] + c.z * b->g[0] * b->g[1];
+    const int cx = cell_axis(x.x, b->lo[0], b->prd[0], b->csize[0], rprd[0], rcs[0], b->g[0]);
+    const int cy = cell_axis(x.y, b->lo[1], b->prd[1], b->csize[1], rprd[1], rcs[1], b->g[1]);
+    const int cz = cell_axis(x.z, b->lo[2], b->prd[2], b->csize[2], rprd[2], rcs[2], b->g[2]);
+    int lin = cx + cy * b->g[0] + cz * b->g[0] * b->g[1];
     old_cell[i] = lin;
     atomicAdd(&count[rank[lin]], 1);
 }
@@ -179,9 +191,9 @@ __global__ void __launch_bounds__(kBlock) k_permute(tmps_atoms src, tmps_atoms d
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const double h = b->hcell[k];  // prd / g, kept with the box (no division per atom)
-            o[k] = (float)(xx[k] - (b->lo[k] + (double)cc[k] * h));
+            o[k] = f32_rn(xx[k] - (b->lo[k] + (double)cc[k] * h));
         }
-        off32[p] = make_float4(o[0], o[1], o[2], (float)x.w);
+        off32[p] = make_float4(o[0], o[1], o[2], f32_rn(x.w));
     }
     st4(dst.xr, p, x);
     st4(dst.vm, p, ld4(src.vm, i));
@@ -201,6 +213,28 @@ __global__ void __launch_bounds__(kBlock) k_permute(tmps_atoms src, tmps_atoms d
     dst.x0[n + p] = x.y;
     dst.x0[2 * n + p] = x.z;
     cell_of[p] = old_cell[i];
+}
+
+// The three cells of one axis at stencil offsets -1, 0, +1 (neighbor.py:
+// 329-351): wrapped on a periodic axis (a stencil offset is at most one cell,
+// so one add or subtract does it), -1 where the stencil leaves a non-periodic
+// grid, and -1 for the off-centre cells of a periodic axis of a single bin.
+struct AxisCells {
+    int m, c, p;  // offsets -1, 0, +1
+    __device__ __forceinline__ int at(int o) const { return o < 0 ? m : (o == 0 ? c : p); }
+};
+
+__device__ __forceinline__ AxisCells axis_cells(int c, int g, int per) {
+    AxisCells a;
+    a.c = c;
+    if (per == 1) {
+        a.m = g == 1 ? -1 : (c == 0 ? g - 1 : c - 1);
+        a.p = g == 1 ? -1 : (c == g - 1 ? 0 : c + 1);
+    } else {
+        a.m = c > 0 ? c - 1 : -1;
+        a.p = c < g - 1 ? c + 1 : -1;
+    }
+    return a;
 }
 
 // The full list.  Stencil order and wrap/skip rules of neighbor.py:329-351;
@@ -231,50 +265,57 @@ __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* 
     const int px = b->per[0], py = b->per[1], pz = b->per[2];
     const int lin = cell_of[p];
     const int cz = lin / gxy, cy = (lin - cz * gxy) / gx, cx = lin - cz * gxy - cy * gx;
+    const AxisCells nxs = axis_cells(cx, gx, px), nys = axis_cells(cy, gy, py), nzs = axis_cells(cz, gz, pz);
     const double4 xi = ld4(a.xr, p);
     const double prd[3] = {b->prd[0], b->prd[1], b->prd[2]};
     const bool pre = off32 != nullptr && !(px == 1 && gx < 3) && !(py == 1 && gy < 3) && !(pz == 1 && gz < 3);
     float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
-    float h32[3] = {0.f, 0.f, 0.f}, hsum = 0.f, mi = 0.f;
+    float h32[3] = {0.f, 0.f, 0.f}, base = 0.f, wi = 0.f;
     const float skin32 = (float)skin;
     if (pre) {
         oi = off32[p];
+        float hsum = 0.f;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            h32[k] = (float)(prd[k] / (double)b->g[k]);
+            h32[k] = f32_rn(b->hcell[k]);  // hcell = prd / g, the box keeps it so
             hsum += h32[k];
         }
-        mi = fmaxf(fmaxf(fabsf(oi.x), fabsf(oi.y)), fabsf(oi.z));
+        base = hsum + fmaxf(fmaxf(fabsf(oi.x), fabsf(oi.y)), fabsf(oi.z));
+        wi = oi.w + skin32;
     }
     int count = 0;
     bool overflow = false;
-    for (int ox = -1; ox <= 1; ++ox)
-        for (int oy = -1; oy <= 1; ++oy)
+    for (int ox = -1; ox <= 1; ++ox) {
+        const int nx = nxs.at(ox);
+        if (nx < 0) continue;
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int ny = nys.at(oy);
+            if (ny < 0) continue;
             for (int oz = -1; oz <= 1; ++oz) {
-                bool skip = (px == 1 && gx == 1 && ox != 0) || (py == 1 && gy == 1 && oy != 0) ||
-                            (pz == 1 && gz == 1 && oz != 0);
-                int nx = cx + ox, ny = cy + oy, nz = cz + oz;
-                if (px == 1) nx = (nx % gx + gx) % gx;
-                if (py == 1) ny = (ny % gy + gy) % gy;
-                if (pz == 1) nz = (nz % gz + gz) % gz;
-                if (skip || nx < 0 || nx >= gx || ny < 0 || ny >= gy || nz < 0 || nz >= gz) continue;
+                const int nz = nzs.at(oz);
+                if (nz < 0) continue;
                 const int r = rank[nx + ny * gx + nz * gxy];
                 const int code = (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1);
                 const int beg = start[r], end = start[r + 1];
-                const float fx = (float)ox * h32[0], fy = (float)oy * h32[1], fz = (float)oz * h32[2];
+                // the row atom's offset moved by the stencil offset: d = (o_i - f) - o_j
+                const float ax = oi.x - (float)ox * h32[0], ay = oi.y - (float)oy * h32[1],
+                            az = oi.z - (float)oz * h32[2];
                 for (int q = beg; q < end; ++q) {
                     if (q == p) continue;
                     bool inside = false;
                     if (pre) {
+                        // within reach beyond doubt, out of reach beyond doubt, or the
+                        // exact test: the slack is ten times the FP32 error bound of
+                        // d and of the cut, ~1e-6 of the magnitudes involved
                         const float4 oj = off32[q];
-                        const float dx = (oi.x - oj.x) - fx, dy = (oi.y - oj.y) - fy, dz = (oi.z - oj.z) - fz;
+                        const float dx = ax - oj.x, dy = ay - oj.y, dz = az - oj.z;
                         const float rq = (dx * dx + dy * dy) + dz * dz;
                         const float mj = fmaxf(fmaxf(fabsf(oj.x), fabsf(oj.y)), fabsf(oj.z));
-                        const float cut = (oi.w + oj.w) + skin32;
-                        const float slack = 1e-5f * (((hsum + mi) + mj) + cut);
+                        const float cut = wi + oj.w;
+                        const float slack = 1e-5f * ((base + mj) + cut);
                         const float lim = cut + slack, near = cut - slack;
-                        if (!(rq < lim * lim) && rq == rq) continue;  // out of reach (a NaN goes on to the exact test)
-                        inside = near > 0.0f && rq < near * near;     // within reach beyond doubt
+                        if (!(rq < lim * lim) && rq == rq) continue;  // a NaN goes on to the exact test
+                        inside = near > 0.0f && rq < near * near;
                     }
                     if (inside) {
                         if (count < nl.slots) {
@@ -304,6 +345,8 @@ __global__ void __launch_bounds__(kBlock) k_build(tmps_atoms a, const tmps_box* 
                     }
                 }
             }
+        }
+    }
     nl.nnb[p] = count;
     if (overflow) atomicOr(status, TMPS_STATUS_NLIST_OVERFLOW);
 }

@@ -35,3 +35,52 @@ extern "C" int tmps_probe_fp64(int32_t blocks, int32_t threads, int32_t iters, d
     note_launches(1);
     return cudaPeekAtLastError() == cudaSuccess ? TMPS_OK : TMPS_ERR_CUDA;
 }
+
+// Self-check of the integer-operation conversions (tmps_common.cuh) against
+// the hardware's rounding, on the caller's operands: mine[i] and hw[i] must
+// agree bit for bit.  No reference counterpart.
+//   which 0: (float)a[i]             f32_rn    vs the hardware conversion (float bits)
+//   which 1: (double)(float)a[i]     f64_of    vs the hardware widening
+//   which 2: hi, lo split of a[i]    split_dw  vs the hardware's (float bits, two outputs per operand)
+namespace {
+
+__global__ void k_selftest(int which, const double* __restrict__ a, int n, double* __restrict__ mine,
+                           double* __restrict__ hw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = a[i];
+    switch (which) {
+        case 0:
+            mine[i] = (double)__float_as_uint(f32_rn(x));
+            hw[i] = (double)__float_as_uint(__double2float_rn(x));
+            break;
+        case 1: {
+            const float f = __double2float_rn(x);
+            mine[i] = f64_of(f);
+            hw[i] = (double)f;
+            break;
+        }
+        default: {
+            float h, l;
+            split_dw(x, h, l);
+            const float hh = __double2float_rn(x);
+            const float ll = __double2float_rn(x - (double)hh);
+            mine[2 * i] = (double)__float_as_uint(h);
+            mine[2 * i + 1] = (double)__float_as_uint(l);
+            hw[2 * i] = (double)__float_as_uint(hh);
+            hw[2 * i + 1] = (double)__float_as_uint(ll);
+            break;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int tmps_selftest_arith(int32_t which, const double* d_a, int32_t n, double* d_mine, double* d_hw,
+                                   void* stream) {
+    if (which < 0 || which > 2 || n < 0 || !d_a || !d_mine || !d_hw) return TMPS_ERR_BAD_ARG;
+    if (n == 0) return TMPS_OK;
+    k_selftest<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(which, d_a, n, d_mine, d_hw);
+    note_launches(1);
+    return cudaPeekAtLastError() == cudaSuccess ? TMPS_OK : TMPS_ERR_CUDA;
+}

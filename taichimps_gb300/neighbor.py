@@ -65,6 +65,12 @@ def morton_rank(gx: int, gy: int, gz: int) -> np.ndarray:
     return rank
 
 
+@lru_cache(maxsize=8)
+def _rank_on_device(gx: int, gy: int, gz: int, dev_index: int) -> torch.Tensor:
+    """morton_rank on the device, shared by every list with this grid (read only)."""
+    return torch.from_numpy(morton_rank(gx, gy, gz)).to(torch.device("cuda", dev_index))
+
+
 def setup_grid_dims(prd, periodicity, max_cutoff: float, skin: float, max_cells: int):
     """
     NeighborList.setup_grid (neighbor.py:143-189) for an orthogonal box, with the
@@ -198,7 +204,7 @@ class NeighborList:
         self._alloc(n)
         key = tuple(int(v) for v in self.grid_dim)
         if key != self._rank_key:
-            self._rank_t = torch.from_numpy(morton_rank(*key)).to(self.dev)
+            self._rank_t = _rank_on_device(*key, self.dev.index)
             self._rank_key = key
         ncell = int(np.prod(self.grid_dim))
         wsb = int(L.tmps_nlist_workspace_bytes(n, ncell))
