@@ -265,10 +265,10 @@ int tmps_box_set(tmps_box* d_box, const tmps_box* h_box, void* stream);
 
 /* ---- integrator / fixes ----------------------------------------------- */
 
-/* FixNVESphere.initial_integrate (src/taichimps/EXTRA_FIX/nve_sphere.py:100-133,155-162). */
+/* FixNVESphere.initial_integrate (src/taichimps/EXTRA_FIX/nve_sphere.py:44-77,155-162). */
 int tmps_verlet_initial(const tmps_atoms* a, double dt, void* stream);
 
-/* FixNVESphere.final_integrate (src/taichimps/EXTRA_FIX/nve_sphere.py:135-153,164-171). */
+/* FixNVESphere.final_integrate (src/taichimps/EXTRA_FIX/nve_sphere.py:79-96,164-171). */
 int tmps_verlet_final(const tmps_atoms* a, double dt, void* stream);
 
 /* AtomSystem.clear_forces (src/taichimps/atom.py:201-220). */
@@ -306,7 +306,7 @@ enum {
  * place).  d_slot_of: int32[n] device scratch. */
 int tmps_atoms_read(const tmps_atoms* a, int32_t field, int32_t* d_slot_of, double* out, void* stream);
 
-/* FixDampingCundall.post_force (src/taichimps/EXTRA_FIX/damping_cundall.py:206-234). */
+/* FixDampingCundall.post_force (src/taichimps/EXTRA_FIX/damping_cundall.py:36-63). */
 int tmps_damping_cundall(const tmps_atoms* a, double gamma_lin, double gamma_ang, void* stream);
 
 /* NeighborList.check_displacement (src/taichimps/neighbor.py:214-245).
@@ -370,7 +370,7 @@ int tmps_history_remap(const tmps_nlist* old_nl, const tmps_nlist* new_nl, const
 /* ---- contact force ------------------------------------------------------ */
 
 /* GranularPair.compute for every style (src/taichimps/GRANULAR/base.py:25-38,
- * hooke.py:52-173, hooke_history.py:108-255, hertz.py:46-148,
+ * hooke.py:52-173, hooke_history.py:71-217, hertz.py:46-148,
  * hertz_history.py:57-193, granular.py:282-452): full list, one thread per
  * atom, no atomics; each contact is evaluated in one fixed orientation
  * (lower internal index first) by both of its atoms, so the two copies of

@@ -398,7 +398,7 @@ static inline void rotate_rescale(double* vec, const double* n) {
  * One contact of every pair style, in the i -> j orientation of the half
  * list.  Follows, operation for operation:
  *   OR_HOOKE          hooke.py:65-155
- *   OR_HOOKE_HISTORY  hooke_history.py:125-233
+ *   OR_HOOKE_HISTORY  hooke_history.py:71-195
  *   OR_HERTZ          hertz.py:59-130
  *   OR_HERTZ_HISTORY  hertz_history.py:74-171
  *   OR_GRANULAR       granular.py:303-430
@@ -621,7 +621,7 @@ static void pair_one(int style, const or_pair_t* P, const or_box_t* b, int nc, i
     add3(torque + 3 * j, tor, armj);
     add3(torque + 3 * i, troll, 1.0);
     add3(torque + 3 * j, troll, -1.0);
-    /* Pair::ev_tally_xyz as restated at hooke_history.py:219-229 */
+    /* Pair::ev_tally_xyz as restated at hooke_history.py:181-191 */
     double vir[6] = {0.5 * (dpos[0] * ftot[0]), 0.5 * (dpos[1] * ftot[1]), 0.5 * (dpos[2] * ftot[2]),
                      0.5 * (dpos[0] * ftot[1]), 0.5 * (dpos[0] * ftot[2]), 0.5 * (dpos[1] * ftot[2])};
     add_raw(virial + 6 * i, vir, 6);
@@ -649,7 +649,7 @@ void or_clear_forces(int n, double* f, double* torque, double* virial) {
     memset(virial, 0, sizeof(double) * 6 * (size_t)n);
 }
 
-/* FixNVESphere.initial_integrate_kernel (nve_sphere.py:100-133) */
+/* FixNVESphere.initial_integrate_kernel (nve_sphere.py:44-77) */
 void or_nve_initial(int n, double dt, double* x, double* v, double* om, const double* f,
                     const double* torque, const double* rad, const double* rmass) {
 #pragma omp parallel for if (g_nthreads > 1)
@@ -663,7 +663,7 @@ void or_nve_initial(int n, double dt, double* x, double* v, double* om, const do
     }
 }
 
-/* FixNVESphere.final_integrate_kernel (nve_sphere.py:135-153) */
+/* FixNVESphere.final_integrate_kernel (nve_sphere.py:79-96) */
 void or_nve_final(int n, double dt, double* v, double* om, const double* f, const double* torque,
                   const double* rad, const double* rmass) {
 #pragma omp parallel for if (g_nthreads > 1)
@@ -676,7 +676,7 @@ void or_nve_final(int n, double dt, double* v, double* om, const double* f, cons
     }
 }
 
-/* FixDampingCundall.post_force_kernel (damping_cundall.py:206-224) */
+/* FixDampingCundall.post_force_kernel (damping_cundall.py:36-53) */
 void or_cundall(int n, double gl, double ga, double* f, double* torque, const double* v, const double* om) {
 #pragma omp parallel for if (g_nthreads > 1)
     for (int i = 0; i < n; ++i)

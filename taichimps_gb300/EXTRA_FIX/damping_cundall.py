@@ -1,7 +1,7 @@
 """
 fix damping/cundall: sign-based local damping of forces and torques.
 
-Mirrors taichimps ``FixDampingCundall`` (src/taichimps/EXTRA_FIX/damping_cundall.py:187-234).
+Mirrors taichimps ``FixDampingCundall`` (src/taichimps/EXTRA_FIX/damping_cundall.py:17-63).
 """
 
 from __future__ import annotations

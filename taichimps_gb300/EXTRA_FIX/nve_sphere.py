@@ -1,7 +1,7 @@
 """
 fix nve/sphere: velocity-Verlet translation and rotation, I = 0.4 m r^2.
 
-Mirrors taichimps ``FixNVESphere`` (src/taichimps/EXTRA_FIX/nve_sphere.py:90-171);
+Mirrors taichimps ``FixNVESphere`` (src/taichimps/EXTRA_FIX/nve_sphere.py:34-114);
 no wrap per step -- positions are wrapped at reneighboring only.
 """
 

@@ -1,4 +1,4 @@
-"""pair_style gran/hooke/history (src/taichimps/GRANULAR/hooke_history.py:71-255)."""
+"""pair_style gran/hooke/history (src/taichimps/GRANULAR/hooke_history.py:71-217)."""
 
 from __future__ import annotations
 

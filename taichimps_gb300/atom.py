@@ -153,7 +153,7 @@ class AtomSystem:
     def _assign_internal(self, name: str, t: torch.Tensor) -> None:
         self._internal_view(name).copy_(t)
         if name in ("radius", "rmass"):
-            # keep the packed inertia in step (atom.py:110-111, nve_sphere.py:120)
+            # keep the packed inertia in step (atom.py:110-111, nve_sphere.py:63)
             b = self._buf
             m, r = b.vm[:, 3], b.xr[:, 3]
             b.om[:, 3] = ((0.4 * m) * r) * r

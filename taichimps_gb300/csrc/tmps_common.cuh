@@ -53,6 +53,9 @@ TMPS_DEV float l1f(float a, float b, float c) { return (fabsf(a) + fabsf(b)) + f
 // outside the plain case (results below the FP32 normal range, infinities,
 // NaNs) go to the hardware conversion.
 
+// isfinite(x) from the exponent bits
+TMPS_DEV bool finite_bits(double x) { return ((__double2hiint(x) >> 20) & 0x7ff) != 0x7ff; }
+
 // (float)x, round to nearest even
 TMPS_DEV float f32_rn(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);

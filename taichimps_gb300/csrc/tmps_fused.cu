@@ -4,11 +4,11 @@
 // header).
 //
 //   A  final half-kick of the previous step, pending remap x, first
-//      half-kick, drift, skin check          (nve_sphere.py:114-153,
+//      half-kick, drift, skin check          (nve_sphere.py:44-96,
 //                                             deform_pressure.py:512-530,
 //                                             neighbor.py:242-245)
 //   C  contact law + Cundall damping + pair and kinetic virial
-//                                            (GRANULAR/*, damping_cundall.py:214-224,
+//                                            (GRANULAR/*, damping_cundall.py:36-53,
 //                                             thermo.py:89-102)
 //   S  rebuild decision, virial total, servo (neighbor.py:371-403,
 //                                             deform_pressure.py:598-702)
@@ -1990,7 +1990,7 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
     const double xx[3] = {x.x, x.y, x.z};
     float oh[3], ol[3];
     for (int k = 0; k < 3; ++k) {
-        const double origin = b->lo[k] + (double)cc[k] * b->hcell[k];
+        const double origin = b->lo[k] + f64_of(__int2float_rn(cc[k])) * b->hcell[k];
         split(xx[k] - origin, oh[k], ol[k]);
         // the skin check's reference: the position at the last build, as an
         // offset from the same origin (x0 is kept by the build in FP64)
@@ -2004,8 +2004,11 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
     float vh[3], vlo[3], wh[3], wlo[3];
     split(v.x, vh[0], vlo[0]); split(v.y, vh[1], vlo[1]); split(v.z, vh[2], vlo[2]);
     split(w.x, wh[0], wlo[0]); split(w.y, wh[1], wlo[1]); split(w.z, wh[2], wlo[2]);
-    reinterpret_cast<float2*>(a.inv32)[i] = make_float2(f32_rn(1.0 / v.w), f32_rn(1.0 / w.w));
-    store_vw<false>(a, i, make_float4(vh[0], vh[1], vh[2], f32_rn(v.w)), make_float4(vlo[0], vlo[1], vlo[2], 0.0f),
+    // 1/m and 1/I of the mixed form's update: FP32 reciprocals of the FP32 values (within an ulp of
+    // the rounded FP64 ones; no FP64 division)
+    const float m32 = f32_rn(v.w), I32 = f32_rn(w.w);
+    reinterpret_cast<float2*>(a.inv32)[i] = make_float2(__frcp_rn(m32), __frcp_rn(I32));
+    store_vw<false>(a, i, make_float4(vh[0], vh[1], vh[2], m32), make_float4(vlo[0], vlo[1], vlo[2], 0.0f),
                     make_float4(wh[0], wh[1], wh[2], 0.0f), make_float4(wlo[0], wlo[1], wlo[2], 0.0f));
 }
 

@@ -18,7 +18,7 @@ constexpr int kBlock = 256;
 
 // ---------------------------------------------------------------- Verlet
 
-// FixNVESphere.initial_integrate_kernel (nve_sphere.py:114-133):
+// FixNVESphere.initial_integrate_kernel (nve_sphere.py:44-77):
 //   v += dtf * (f / m);  x = x + dtv * v;  omega += dtf * (torque / I)
 __global__ void __launch_bounds__(kBlock) k_verlet_initial(tmps_atoms a, double dt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(kBlock) k_verlet_initial(tmps_atoms a, double 
     st4(a.om, i, w);
 }
 
-// FixNVESphere.final_integrate_kernel (nve_sphere.py:143-153)
+// FixNVESphere.final_integrate_kernel (nve_sphere.py:79-96)
 __global__ void __launch_bounds__(kBlock) k_verlet_final(tmps_atoms a, double dt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -59,21 +59,34 @@ __global__ void __launch_bounds__(kBlock) k_verlet_final(tmps_atoms a, double dt
     st4(a.om, i, w);
 }
 
-// FixDampingCundall.post_force_kernel (damping_cundall.py:214-224)
+// a * b >= 0.0, as the FP64 product compares: from the sign bits where the
+// exponents keep the product clear of underflow (and neither is a NaN), the
+// product itself otherwise.
+__device__ __forceinline__ bool prod_nonneg(double a, double b) {
+    const int ha = __double2hiint(a), hb = __double2hiint(b);
+    const int ea = (ha >> 20) & 0x7ff, eb = (hb >> 20) & 0x7ff;
+    if (ea > 0x200 && ea < 0x600 && eb > 0x200 && eb < 0x600) return (ha ^ hb) >= 0;
+    return a * b >= 0.0;
+}
+
+// FixDampingCundall.post_force (damping_cundall.py:36-53):
+//   f_d *= 1 - gamma_lin sign(f_d v_d),  torque_d *= 1 - gamma_ang sign(torque_d omega_d)
+// The factors 1 -+ gamma are the same two roundings for every atom (gamma *
+// sign is exact), so they are formed once; each component then costs one
+// FP64 multiply.
 __global__ void __launch_bounds__(kBlock) k_cundall(tmps_atoms a, double gl, double ga) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const int n = a.n;
+    const double lp = 1.0 - gl, lm = 1.0 + gl, ap = 1.0 - ga, am = 1.0 + ga;
     const double4 v = ld4(a.vm, i), w = ld4(a.om, i);
     const double vv[3] = {v.x, v.y, v.z}, ww[3] = {w.x, w.y, w.z};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        double fd = a.f[d * n + i];
-        double sf = fd * vv[d] >= 0.0 ? 1.0 : -1.0;
-        a.f[d * n + i] = fd * (1.0 - gl * sf);
-        double td = a.torque[d * n + i];
-        double st = td * ww[d] >= 0.0 ? 1.0 : -1.0;
-        a.torque[d * n + i] = td * (1.0 - ga * st);
+        const double fd = a.f[d * n + i];
+        a.f[d * n + i] = __dmul_rn(fd, prod_nonneg(fd, vv[d]) ? lp : lm);
+        const double td = a.torque[d * n + i];
+        a.torque[d * n + i] = __dmul_rn(td, prod_nonneg(td, ww[d]) ? ap : am);
     }
 }
 

@@ -22,42 +22,58 @@ constexpr int kScanBlock = 1024;
 // reference's lamda for an orthogonal box adds products with zero tilt terms,
 // which leave the quotient unchanged.
 //
-// The two divisions are correctly rounded, and only the floor of the second
-// quotient matters: t = (x - lo) * (1/prd) * (1/csize) with the reciprocals
-// rounded once differs from the exact chain's quotient by a few ulps of t
-// (relative ~1e-15), so wherever t lies further than 1e-12 (1 + |t|) from an
-// integer both floors agree and no division is needed; within that margin
-// (or for a NaN) the exact chain decides.  `rcp` holds 1/prd and 1/csize.
-__device__ __forceinline__ int cell_axis(double x, double lo, double prd, double csize, double rprd,
-                                         double rcs, int g) {
-    const double d = __dsub_rn(x, lo);
-    const double t = __dmul_rn(__dmul_rn(d, rprd), rcs);
-    double q = floor(t);
-    const double r = __dsub_rn(t, q);
-    const double m = 1e-12 * (1.0 + fabs(t));
-    if (!(r > m && r < 1.0 - m)) q = floor(__ddiv_rn(__ddiv_rn(d, prd), csize));
+// Only the floor of the quotient t matters.  An FP32 estimate of t from the
+// truncated position (approx_f32: integer operations) is within 4e-6 of
+// ((|x| + |lo|) / h + |t| + 1) of the exact chain's quotient (h = prd csize,
+// the cell edge; the bound is four times the truncation and FP32 rounding
+// errors), so wherever the estimate lies further than that from an integer
+// both floors agree; within it (a few atoms in 10^4, or a NaN) the exact
+// chain of two correctly rounded FP64 divisions decides.  No FP64 arithmetic
+// otherwise: this part's FP64 pipe is narrow.
+struct AxisBin {
+    double lo, prd, csize;
+    float lo32, rprd32, rcs32, rh32;  // FP32 lo, 1/prd, 1/csize, 1/(prd csize)
+    int g;
+};
+
+__device__ __forceinline__ int cell_axis(double x, const AxisBin& ax) {
+    const float xf = approx_f32(x);
+    const float t = ((xf - ax.lo32) * ax.rprd32) * ax.rcs32;
+    const float qf = floorf(t);
+    const float r = t - qf;
+    const float m = 4e-6f * (((fabsf(xf) + fabsf(ax.lo32)) * ax.rh32 + fabsf(t)) + 1.0f);
+    if (r > m && r < 1.0f - m)
+        return qf >= (float)(ax.g - 1) ? ax.g - 1 : (qf > 0.0f ? (int)qf : 0);
+    const double q = floor(__ddiv_rn(__ddiv_rn(__dsub_rn(x, ax.lo), ax.prd), ax.csize));
     // clamp in floating point first so a stray NaN/Inf cannot overflow the
     // int conversion; NaN falls to cell 0
-    return q >= (double)(g - 1) ? g - 1 : (q > 0.0 ? (int)q : 0);
+    return q >= (double)(ax.g - 1) ? ax.g - 1 : (q > 0.0 ? (int)q : 0);
 }
 
 __global__ void __launch_bounds__(kBlock) k_bin(tmps_atoms a, const tmps_box* __restrict__ b,
                                                 const int32_t* __restrict__ rank, int32_t* old_cell,
                                                 int32_t* count, int32_t* status) {
-    __shared__ double rprd[3], rcs[3];
+    __shared__ AxisBin sax[3];
     if (threadIdx.x < 3) {
-        rprd[threadIdx.x] = 1.0 / b->prd[threadIdx.x];
-        rcs[threadIdx.x] = 1.0 / b->csize[threadIdx.x];
+        const int k = threadIdx.x;
+        AxisBin ax;
+        ax.lo = b->lo[k];
+        ax.prd = b->prd[k];
+        ax.csize = b->csize[k];
+        ax.g = b->g[k];
+        ax.lo32 = approx_f32(ax.lo);
+        ax.rprd32 = (float)(1.0 / ax.prd);
+        ax.rcs32 = (float)(1.0 / ax.csize);
+        ax.rh32 = (float)(1.0 / (ax.prd * ax.csize));
+        sax[k] = ax;
     }
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double4 x = ld4(a.xr, i);
-    if (!isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z)) atomicOr(status, TMPS_STATUS_NONFINITE);
-    const int cx = cell_axis(x.x, b->lo[0], b->prd[0], b->csize[0], rprd[0], rcs[0], b->g[0]);
-    const int cy = cell_axis(x.y, b->lo[1], b->prd[1], b->csize[1], rprd[1], rcs[1], b->g[1]);
-    const int cz = cell_axis(x.z, b->lo[2], b->prd[2], b->csize[2], rprd[2], rcs[2], b->g[2]);
-    int lin = cx + cy * b->g[0] + cz * b->g[0] * b->g[1];
+    if (!finite_bits(x.x) || !finite_bits(x.y) || !finite_bits(x.z)) atomicOr(status, TMPS_STATUS_NONFINITE);
+    const int cx = cell_axis(x.x, sax[0]), cy = cell_axis(x.y, sax[1]), cz = cell_axis(x.z, sax[2]);
+    int lin = cx + cy * sax[0].g + cz * sax[0].g * sax[1].g;
     old_cell[i] = lin;
     atomicAdd(&count[rank[lin]], 1);
 }

@@ -53,7 +53,7 @@ def test_dense_steps_with_rebuilds(gpu, oracle, pair):
 
 
 def test_shear_history_survives_rebuild(gpu):
-    """tests/test_lammps_parity.py:180-212 on the GPU: rebuild every step == never, rtol 1e-8."""
+    """tests/test_lammps_parity.py:124-157 on the GPU: rebuild every step == never, rtol 1e-8."""
     import taichimps_gb300 as G
     rng = np.random.default_rng(11)
     box = 6.0
@@ -199,7 +199,7 @@ def test_pbc_and_stale_box(gpu):
 
 
 def test_friction_damps_spin(gpu):
-    """tests/test_lammps_parity.py:215-246 on the GPU path."""
+    """tests/test_lammps_parity.py:159-190 on the GPU path."""
     import taichimps_gb300 as G
     radius, overlap, spin = 0.5, 0.01, 3.0
     d = 2.0 * radius - overlap

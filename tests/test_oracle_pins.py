@@ -87,7 +87,7 @@ def test_pressure_translation_invariant(oracle):
 
 
 def test_shear_history_survives_rebuild(oracle):
-    """tests/test_lammps_parity.py:180-212: rebuild every step == never rebuild, rtol 1e-8."""
+    """tests/test_lammps_parity.py:124-157: rebuild every step == never rebuild, rtol 1e-8."""
     O = oracle
     rng = np.random.default_rng(11)
     box = 6.0
@@ -112,7 +112,7 @@ def test_shear_history_survives_rebuild(oracle):
 
 
 def test_friction_damps_spin(oracle):
-    """tests/test_lammps_parity.py:215-246: friction opposes spin; Newton's third law."""
+    """tests/test_lammps_parity.py:159-190: friction opposes spin; Newton's third law."""
     O = oracle
     radius, overlap, spin = 0.5, 0.01, 3.0
     d = 2.0 * radius - overlap
