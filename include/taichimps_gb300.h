@@ -225,6 +225,8 @@ typedef struct tmps_engine {
                               * tmps_fused_bounds left in the scratch (set by S
                               * after the first step that follows the bounds) */
     int64_t stop_step;       /* fused launches do nothing once step >= stop_step (batched runs) */
+    int32_t touching;        /* atoms whose gap bound at the last tmps_fused_bounds is <= 0 */
+    int32_t pad4_;
 } tmps_engine;
 
 /* One instance of a batched run (tmps_batch_*): the device state of one
@@ -415,8 +417,9 @@ int tmps_servo_step(tmps_box* d_box, tmps_servo* d_servo, const double* d_virial
 
 /* After a neighbor build: 1/m and 1/I for the fused step and, with
  * d_eng->mixed, the split positions (offset from each atom's cell origin in
- * xr, cell32, FP32 copies, o0_32).  `cell_of` is the linear cell id from
- * tmps_nlist_build; records lo0 / h0 in d_eng. */
+ * xr, cell32, FP32 copies, o0_32) and FP32 copies of f and torque into f32,
+ * torque32.  `cell_of` is the linear cell id from tmps_nlist_build; records
+ * lo0 / h0 in d_eng and clears d_eng->touching for tmps_fused_bounds. */
 int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* d_eng,
                        const int32_t* cell_of, void* stream);
 

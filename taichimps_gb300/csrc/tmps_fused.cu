@@ -468,6 +468,10 @@ __global__ void __launch_bounds__(kBlockA) k_bounds(tmps_atoms A, tmps_nlist L, 
             if ((hist && L.touch[i] != 0ull) || single) gmin = -3e38f;
             agap[i] = gmin;
         }
+        {
+            const int t = __popc(__ballot_sync(0xffffffffu, i < n && !(gmin > 0.0f)));
+            if (lane == 0 && t) atomicAdd(&E->touching, t);
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gmin = fminf(gmin, __shfl_down_sync(0xffffffffu, gmin, o));
         if (lane == 0) {
@@ -1997,6 +2001,11 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
         a.o0_32[k * n + i] = f32_rn(a.x0[k * n + i] - origin);
     }
     a.cell32[i] = cx | (cy << 10) | (cz << 20);
+    // the forces in hand (the setup forces at a run's start; at a rebuild C rewrites them first)
+    for (int k = 0; k < 3; ++k) {
+        a.f32[k * n + i] = f32_rn(a.f[k * n + i]);
+        a.torque32[k * n + i] = f32_rn(a.torque[k * n + i]);
+    }
     float rh, rl;
     split(x.w, rh, rl);
     st4f(a.pos32, i, make_float4(oh[0], oh[1], oh[2], rh));
@@ -2016,6 +2025,7 @@ __global__ void k_prepare_engine(const tmps_box* __restrict__ b, tmps_engine* e,
     if (threadIdx.x || blockIdx.x) return;
     e->part_off = part_off;
     e->cull = 0;  // until tmps_fused_bounds sets the bounds
+    e->touching = 0;
     e->maxd2_bits = 0u;
     e->shift_bound = 0.0f;
     for (int d = 0; d < 3; ++d) {

@@ -121,8 +121,8 @@ class FusedEngine:
     def _alloc(self, n: int) -> None:
         if n == self._n:
             return
-        # every per-atom array here is written in full by tmps_fused_prepare (and f32, t32 by begin)
-        # before any kernel reads it: left unset, in one allocation for the mixed form's eleven
+        # every per-atom array here is written in full by tmps_fused_prepare before any kernel reads
+        # it: left unset, in one allocation for the mixed form's eleven
         self.rinv = None if self.mixed else torch.empty((2, n), dtype=torch.float64, device=self.dev)
         style, mixed = int(self.sim.pair_style.params.style), 1 if self.mixed else 0
         self._shape(n)
@@ -219,11 +219,8 @@ class FusedEngine:
         rc = _device.lib().tmps_fused_pressure_log(self._eng.data_ptr(), None if log is None else log.data_ptr(),
                                                    0 if log is None else len(log), _device.stream())
         _lib.check(rc, "tmps_fused_pressure_log")
-        if self.mixed:
-            # the setup forces (FP64) seed the first half-kick
-            b = atom.buffers
-            self.f32.copy_(b.f)
-            self.t32.copy_(b.torque)
+        # (the mixed form's first half-kick takes the setup forces, which tmps_fused_prepare copied
+        # into f32, t32)
         self.status.zero_()
         # the record as pushed above, in the fields run() reads (step, aborted), and a clear status:
         # the first run() starts without a synchronisation
@@ -245,12 +242,10 @@ class FusedEngine:
         if self.contact_path == "auto" and not self.mixed:
             self.rows = False
         elif self.contact_path == "auto":
-            n = self._n
-            ng = (n + 31) // 32
-            r256 = lambda b: (b + 255) // 256 * 256
-            off = r256((ng + 1) * 4) + r256(ng * 4)  # scratch: flag words, group gaps, then the atom gaps
-            agap = self.part[off:off + 4 * n].view(torch.float32)
-            self.rows = n > 0 and int((agap <= 0).sum()) * 2 > n
+            # the bounds kernel counted the atoms whose gap bound is <= 0 into the engine record
+            off = _lib.Engine.touching.offset
+            touching = int(_device.pull_many([(self._eng[off:off + 4], None)])[0].view(np.int32)[0])
+            self.rows = self._n > 0 and touching * 2 > self._n
         self._history_form(True)
 
     def _history_form(self, dw: bool) -> None:

@@ -171,12 +171,14 @@ class NeighborList:
             return
         S = self.slots
         i32 = dict(dtype=torch.int32, device=self.dev)
-        self.nbr = torch.zeros((S, n), **i32)
+        # a row's entries past its length are never read (every reader stops at nnb), so the lists
+        # are left unset; the lengths start at zero (an empty previous list for the first carry-over)
+        self.nbr = torch.empty((S, n), **i32)
         self.nnb = torch.zeros(n, **i32)
-        self.prev_nbr = torch.zeros((S, n), **i32)
+        self.prev_nbr = torch.empty((S, n), **i32)
         self.prev_nnb = torch.zeros(n, **i32)
-        self.order = torch.zeros(n, **i32)
-        self.cell_of = torch.zeros(n, **i32)
+        self.order = torch.empty(n, **i32)
+        self.cell_of = torch.empty(n, **i32)
         self._n = n
 
     def cstruct(self, touch: torch.Tensor | None, shear: torch.Tensor | None, prev: bool = False,
@@ -209,14 +211,14 @@ class NeighborList:
         ncell = int(np.prod(self.grid_dim))
         wsb = int(L.tmps_nlist_workspace_bytes(n, ncell))
         if self._ws.numel() < wsb:
-            self._ws = torch.zeros(wsb, dtype=torch.uint8, device=self.dev)
+            self._ws = torch.empty(wsb, dtype=torch.uint8, device=self.dev)  # the build clears what it counts in
         # the list built last time becomes `prev`, for the history carry-over
         self.nbr, self.prev_nbr = self.prev_nbr, self.nbr
         self.nnb, self.prev_nnb = self.prev_nnb, self.nnb
         self.prev_slots = self.slots
         while True:
             if self.nbr.shape[0] < self.slots:
-                self.nbr = torch.zeros((self.slots, n), dtype=torch.int32, device=self.dev)
+                self.nbr = torch.empty((self.slots, n), dtype=torch.int32, device=self.dev)
             self.status.zero_()
             nl = self.cstruct(None, None)
             src, dst = atom.cstruct(atom.buffers), atom.cstruct(atom.alt_buffers)
@@ -284,8 +286,11 @@ class NeighborList:
     # ------------------------------------------------- reference views
 
     def full_rows(self):
-        """(nbr[S, n] partner internal index, nnb[n]) on the host."""
-        return (self.nbr.cpu().numpy() & NBR_INDEX_MASK), self.nnb.cpu().numpy()
+        """(nbr[S, n] partner internal index, nnb[n]) on the host; entries past a row's length
+        read as 0."""
+        nbr, nnb = self.nbr.cpu().numpy() & NBR_INDEX_MASK, self.nnb.cpu().numpy()
+        nbr[np.arange(nbr.shape[0])[:, None] >= nnb[None, :]] = 0
+        return nbr, nnb
 
     def _half(self):
         atom = self._atom

@@ -125,6 +125,7 @@ def test_rebuild_is_deterministic(gpu):
         atom.add_particles(x=p["x"], radius=p["radius"], density=2.5)
         nl = G.NeighborList(domain=dom, skin=0.1, max_atoms=len(p["x"]), max_neighbors_per_atom=32)
         nl.build(atom)
-        outs.append((nl.nbr.cpu().numpy().copy(), nl.nnb.cpu().numpy().copy(), atom.buffers.uid.cpu().numpy().copy()))
+        nbr, nnb = nl.full_rows()  # entries past a row's length are unspecified
+        outs.append((nbr, nnb, atom.buffers.uid.cpu().numpy().copy()))
     for a, b in zip(*outs):
         np.testing.assert_array_equal(a, b)
