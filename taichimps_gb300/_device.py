@@ -58,13 +58,26 @@ class timed:
         return False
 
 
+_AVAILABLE: bool | None = None  # whether a CUDA device exists does not change within a process
+
+
 def device() -> torch.device:
-    if not torch.cuda.is_available():
+    global _AVAILABLE
+    if _AVAILABLE is None:
+        _AVAILABLE = torch.cuda.is_available()
+    if not _AVAILABLE:
         raise RuntimeError("taichimps_gb300 runs on a CUDA device (GB300, sm_103a); none is available")
     return torch.device("cuda", torch.cuda.current_device())
 
 
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+
+
 def stream() -> int:
+    """The current stream of the current device as a cudaStream_t (a stream set by
+    torch.cuda.stream() or a graph capture included)."""
+    if _raw_stream is not None:
+        return _raw_stream(torch.cuda.current_device())
     return torch.cuda.current_stream().cuda_stream
 
 

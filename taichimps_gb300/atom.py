@@ -47,6 +47,16 @@ class _Buffers:
         self.x0 = new((3, n), **f64)
 
 
+_EMPTY: dict = {}
+
+
+def _empty_buffers(dev: torch.device) -> _Buffers:
+    """The arrays of an empty system (shared: nothing writes to zero-length arrays)."""
+    if dev not in _EMPTY:
+        _EMPTY[dev] = _Buffers(0, dev)
+    return _EMPTY[dev]
+
+
 class FieldView:
     """
     Reference-style access to one per-atom quantity in insertion order:
@@ -120,10 +130,11 @@ class AtomSystem:
         self.nlocal = 0
         self.float_type = float_type
         self.device = _device.device()
-        self._buf = _Buffers(0, self.device)
-        self._alt = _Buffers(0, self.device)
-        self.atom_type_host = np.zeros(0, dtype=np.int32)
-        self.mask_host = np.zeros(0, dtype=np.int32)
+        self._buf = self._alt = _empty_buffers(self.device)
+        # per-atom type and mask on the host; a uniform value stays a scalar until read as an array
+        self._type_arr: np.ndarray | None = np.zeros(0, dtype=np.int32)
+        self._mask_arr: np.ndarray | None = np.zeros(0, dtype=np.int32)
+        self._type_fill = 1
         self._uid_cache: np.ndarray | None = None
         self.x = FieldView(self, "x", 3, np.float64)
         self.v = FieldView(self, "v", 3, np.float64)
@@ -344,8 +355,7 @@ class AtomSystem:
             tt = torch.from_numpy(np.ascontiguousarray(np.asarray(tag, dtype=np.int32))).to(dev)
             keep.append(tt)
             tag_ptr = tt.data_ptr()
-        types = (np.full(n, int(atom_type), dtype=np.int32) if np.isscalar(atom_type)
-                 else np.asarray(atom_type, dtype=np.int32))
+        types = None if np.isscalar(atom_type) else np.asarray(atom_type, dtype=np.int32)
         nb = _Buffers(n, dev, fill=False)  # the kernel writes every array
         self._buf = nb
         self._alt = _Buffers(n, dev, fill=False)
@@ -356,8 +366,11 @@ class AtomSystem:
         _lib.check(rc, "tmps_atoms_assemble")
         # page-locked inputs are read in place: held until a synchronisation shows the kernel has run
         self._pending_inputs = keep
-        self.atom_type_host = types
-        self.mask_host = np.ones(n, dtype=np.int32)
+        if np.isscalar(atom_type):
+            self._type_arr, self._type_fill = None, int(atom_type)
+        else:
+            self.atom_type_host = types
+        self._mask_arr = None
         self._uid_cache = None
         self._max_radius, self._max_radius_dev = 0.0, rmax
         for cb in self._listeners:
@@ -396,6 +409,26 @@ class AtomSystem:
     def on_reorder(self, cb) -> None:
         """Register a callback run whenever internal order or size changes."""
         self._listeners.append(cb)
+
+    @property
+    def atom_type_host(self) -> np.ndarray:
+        if self._type_arr is None:
+            self._type_arr = np.full(self.nlocal, self._type_fill, dtype=np.int32)
+        return self._type_arr
+
+    @atom_type_host.setter
+    def atom_type_host(self, v) -> None:
+        self._type_arr = np.asarray(v, dtype=np.int32)
+
+    @property
+    def mask_host(self) -> np.ndarray:
+        if self._mask_arr is None:
+            self._mask_arr = np.ones(self.nlocal, dtype=np.int32)
+        return self._mask_arr
+
+    @mask_host.setter
+    def mask_host(self, v) -> None:
+        self._mask_arr = np.asarray(v, dtype=np.int32)
 
     @property
     def atom_type(self) -> np.ndarray:

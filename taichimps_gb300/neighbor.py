@@ -82,13 +82,12 @@ def setup_grid_dims(prd, periodicity, max_cutoff: float, skin: float, max_cells:
     if cut <= 0:
         cut = 1.0
     xprd, yprd, zprd = (float(v) for v in prd)
-    a = np.array([xprd, 0.0, 0.0])
-    b = np.array([0.0, yprd, 0.0])
-    c = np.array([0.0, 0.0, zprd])
     vol = xprd * yprd * zprd
-    widths = [vol / np.linalg.norm(np.cross(b, c)), vol / np.linalg.norm(np.cross(c, a)),
-              vol / np.linalg.norm(np.cross(a, b))]
-    g = [max(1, int(np.floor(w / cut))) for w in widths]
+    # |b x c| of the orthogonal edge vectors as numpy forms it: the cross product's one nonzero
+    # component (y z - 0 0 = y z) and norm sqrt(dot) -- the same IEEE operations in plain floats
+    widths = [vol / math.sqrt((yprd * zprd) * (yprd * zprd)), vol / math.sqrt((zprd * xprd) * (zprd * xprd)),
+              vol / math.sqrt((xprd * yprd) * (xprd * yprd))]
+    g = [max(1, int(math.floor(w / cut))) for w in widths]
     for k in range(3):
         if periodicity[k] == 1 and g[k] == 2:
             g[k] = 1
