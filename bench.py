@@ -68,8 +68,10 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="config2", choices=["config2", "dense", "ensemble", "adjoint", "triaxial"],
-                    help="config2: the 1M-sphere servo run (default); ensemble: the batched-instances run")
+    ap.add_argument("--workload", default="config2",
+                    choices=["config2", "dense", "ensemble", "adjoint", "triaxial", "e2e"],
+                    help="config2: the 1M-sphere servo run (default); ensemble: the batched-instances run; "
+                         "e2e: the config-2 end-to-end job alone (for launch lists)")
     ap.add_argument("--instances", type=int, default=512, help="ensemble: number of instances")
     ap.add_argument("--no-dense", action="store_true", help="skip the contact-dense 1M-sphere line")
     ap.add_argument("--dense-reps", type=int, nargs=3, default=[4, 4, 4],
@@ -349,12 +351,37 @@ def run_e2e(args, p, precision):
         times.append(time.perf_counter() - t0)
     dt = statistics.median(times)
     assert np.isfinite(x).all() and np.isfinite(v).all() and np.isfinite(pressures).all()
+
+    # where a job's time goes: one more job, synchronised after each public call (so the phases add up
+    # to a little more than an unsynchronised job)
+    phases = {}
+
+    def lap(name, t0):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        phases[name] = round((t1 - t0) * 1e3, 4)
+        return t1
+
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    sim = make_sim(G, p, n, precision, host=host)
+    t = lap("system from pinned arrays (Domain, AtomSystem.add_particles, list, pair, fixes)", t)
+    fix = sim.fixes[-1]
+    fix.record_pressure(K + 1)
+    sim.run(K)
+    t = lap("Simulation.run: neighbor build, setup forces, K fused steps, hand-back", t)
+    fix.pressure_history(range(1, K + 1))
+    t = lap("pressure_history", t)
+    sim.atom.x.to_numpy()
+    sim.atom.v.to_numpy()
+    lap("x, v to_numpy", t)
     up = n * (3 * 8 + 8 + 3 * 8)                # positions, radius, velocities (mass and inertia are formed on the device)
     down = n * 2 * 3 * 8 + K * 48               # final x, v; per step the pressure tensor
     return {"value": n * K / dt, "unit": UNIT, "h2d_bytes_per_step": up / K, "d2h_bytes_per_step": down / K,
             "seconds": dt, "precision": precision,
             "includes": "upload, neighbor build + setup forces, K steps, per-step pressure to host, download "
-                        "(median of three timed jobs after an untimed one)", "job_seconds": times}
+                        "(median of three timed jobs after an untimed one)", "job_seconds": times,
+            "phases_ms": phases}
 
 
 # ----------------------------------------------------------------- CPU (oracle)
@@ -786,6 +813,19 @@ def main():
             print(json.dumps(out), flush=True)
         if world > 1:
             torch.distributed.destroy_process_group()
+        return
+    if args.workload == "e2e":
+        if args.impl != "ours" or rank != 0:
+            if rank == 0:
+                print(json.dumps({"impl": args.impl, "unavailable": "the e2e job is part of the default run"}))
+            return
+        import torch
+        from taichimps_gb300.packing import config2
+        torch.cuda.set_device(local)
+        prec = "mixed" if args.precision == "both" else args.precision
+        out = run_e2e(args, config2(seed=args.seed, n=args.n), prec)
+        print(json.dumps({"workload": "e2e: " + WORKLOAD, "n_atoms": args.n, "steps": args.steps, "e2e": out}),
+              flush=True)
         return
     if args.impl == "reference":
         out = reference_arm(args, rank, world)

