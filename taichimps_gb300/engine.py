@@ -239,12 +239,23 @@ class FusedEngine:
         rc = L.tmps_fused_bounds(atoms, sim.history.cstruct(nl), sim.domain.dbox, self._eng.data_ptr(),
                                  sim.pair_style.params, 1 if self.cull else 0, self.part.data_ptr(), st)
         _lib.check(rc, "tmps_fused_bounds")
+        # one synchronisation for what the host needs before the steps: the count of touching atoms
+        # (the contact path) and the status of a neighbor build that did not wait for the device
+        auto_rows = self.contact_path == "auto" and self.mixed
+        items = []
+        if auto_rows:
+            off = _lib.Engine.touching.offset
+            items.append((self._eng[off:off + 4], None))
+        if nl.status_pending:
+            items.append((nl.status, None))
+        got = _device.pull_many(items) if items else []
+        if nl.status_pending:
+            nl.check_status(int(got[-1].view(np.int32)[0]))
         if self.contact_path == "auto" and not self.mixed:
             self.rows = False
-        elif self.contact_path == "auto":
+        elif auto_rows:
             # the bounds kernel counted the atoms whose gap bound is <= 0 into the engine record
-            off = _lib.Engine.touching.offset
-            touching = int(_device.pull_many([(self._eng[off:off + 4], None)])[0].view(np.int32)[0])
+            touching = int(got[0].view(np.int32)[0])
             self.rows = self._n > 0 and touching * 2 > self._n
         self._history_form(True)
 
@@ -415,7 +426,7 @@ class FusedEngine:
         sim.domain.pull()
         sim.history.save_state(atom, nl)
         sim.domain.pbc(atom)
-        nl.build(atom)
+        nl.build(atom, defer_check=True)  # its status is read with the engine's next pull
         sim.history.restore_state(atom, nl)
         e = self._engine_state()
         e.aborted = 0

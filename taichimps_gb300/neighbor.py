@@ -134,6 +134,7 @@ class NeighborList:
         self._n = -1
         self._atom = None
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self._status_pending = False
         self.flag = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self._ws = torch.zeros(0, dtype=torch.uint8, device=self.dev)
         self.nbr = self.nnb = self.prev_nbr = self.prev_nnb = None
@@ -194,10 +195,15 @@ class NeighborList:
 
     # ------------------------------------------------------------ build
 
-    def build(self, atom) -> None:
-        """NeighborList.build (neighbor.py:414-435): bin, re-sort, list; raise on overflow."""
+    def build(self, atom, defer_check: bool = False) -> None:
+        """NeighborList.build (neighbor.py:414-435): bin, re-sort, list; raise on overflow.
+        `defer_check` (a fixed slot count only): return without waiting for the device; the build's
+        status (a row past the slot count, a non-finite position) is read and raised by
+        check_status() at the caller's next synchronisation.  A row that overflows keeps its first
+        `slots` entries, so nothing in between reads past the list."""
         if atom.nlocal == 0:
             return
+        self.check_status()  # an earlier deferred build's status first (this one clears the word)
         L = _device.lib()
         self.domain.pull()
         self.setup_grid(2.0 * atom.max_radius)
@@ -225,6 +231,10 @@ class NeighborList:
                                     self.order.data_ptr(), self.cell_of.data_ptr(), nl, self._ws.data_ptr(),
                                     wsb, self.status.data_ptr(), _device.stream())
             _lib.check(rc, "tmps_nlist_build")
+            if defer_check and not self.auto_slots:
+                self._status_pending = True
+                status = 0
+                break
             status = int(self.status.item())
             if not (status & _lib.STATUS_NLIST_OVERFLOW and self.auto_slots and self.slots < MAX_SLOTS):
                 break
@@ -232,21 +242,40 @@ class NeighborList:
             self.slots = MAX_SLOTS
         atom.swap_buffers()
         self._atom = atom
+        if not self._status_pending:
+            if status & _lib.STATUS_NONFINITE:
+                raise RuntimeError("Neighbor build found a non-finite particle position")
+            if self.auto_slots and not status & _lib.STATUS_NLIST_OVERFLOW:
+                fit = self.fit_slots(int(self.nnb.max().item()))
+                if fit < self.slots:
+                    self.nbr = self.nbr[:fit].clone()
+                    self.slots = fit
+            self._raise_for(status)
+        self.has_built = True
+        self.build_count += 1
+        self.last_build_step = self.current_step
+
+    def _raise_for(self, status: int) -> None:
         if status & _lib.STATUS_NONFINITE:
             raise RuntimeError("Neighbor build found a non-finite particle position")
-        if self.auto_slots and not status & _lib.STATUS_NLIST_OVERFLOW:
-            fit = self.fit_slots(int(self.nnb.max().item()))
-            if fit < self.slots:
-                self.nbr = self.nbr[:fit].clone()
-                self.slots = fit
         if status & _lib.STATUS_NLIST_OVERFLOW:
             raise RuntimeError(
                 "Neighbor list overflow: more than "
                 f"{self.max_neighbors_per_atom} neighbors for at least one particle. "
                 "Increase max_neighbors_per_atom, or reduce the neighbor skin.")
-        self.has_built = True
-        self.build_count += 1
-        self.last_build_step = self.current_step
+
+    @property
+    def status_pending(self) -> bool:
+        """Whether a deferred build's status is still to be read."""
+        return self._status_pending
+
+    def check_status(self, status: int | None = None) -> None:
+        """Raise for a deferred build's overflow or non-finite position: reads the status word
+        (synchronises), or takes `status`, the word as the caller read it with other values."""
+        if not self._status_pending:
+            return
+        self._status_pending = False
+        self._raise_for(int(self.status.item()) if status is None else int(status))
 
     def check_displacement(self, atom, trigger_sq: float, stamp: int) -> None:
         L = _device.lib()
@@ -259,6 +288,7 @@ class NeighborList:
         """NeighborList.decide (neighbor.py:371-403), same rules and order."""
         if not self.has_built:
             return True
+        self.check_status()
         if timestep is not None:
             self.current_step = timestep
         else:

@@ -110,6 +110,8 @@ class Simulation:
             self.integrator = None
 
     def check_device_status(self) -> None:
+        if self.neighbor is not None:
+            self.neighbor.check_status()
         for fix in self.fixes:
             fix.check_status()
 
@@ -129,7 +131,9 @@ class Simulation:
             self.history.save_state(self.atom, self.neighbor)
         self.domain.pbc(self.atom)
         self.domain.pull()
-        self.neighbor.build(self.atom)
+        # the build's status is read at the next synchronisation (NeighborList.check_status), so the
+        # host goes on queueing the steps after it while the device builds
+        self.neighbor.build(self.atom, defer_check=True)
         if self.history is not None:
             self.history.restore_state(self.atom, self.neighbor)
         return True
