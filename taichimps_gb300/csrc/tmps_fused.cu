@@ -186,6 +186,8 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
         if (i >= n) continue;
         double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
         const double im = __ldcs(a.rinv + i), iI = __ldcs(a.rinv + n + i);
+        // the skin check's reference with the state (not after the stores, which might alias it)
+        const double x0x = __ldcs(a.x0 + i), x0y = __ldcs(a.x0 + n + i), x0z = __ldcs(a.x0 + 2 * n + i);
         double f[3] = {0.0, 0.0, 0.0}, t[3] = {0.0, 0.0, 0.0};
         if (force_live(flags, i)) {
             f[0] = __ldcs(a.f + i); f[1] = __ldcs(a.f + n + i); f[2] = __ldcs(a.f + 2 * n + i);
@@ -206,8 +208,7 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
         st4(a.xr, i, x);
         st4(a.vm, i, v);
         st4(a.om, i, w);
-        const double d0 = __dsub_rn(x.x, __ldcs(a.x0 + i)), d1 = __dsub_rn(x.y, __ldcs(a.x0 + n + i)),
-                     d2 = __dsub_rn(x.z, __ldcs(a.x0 + 2 * n + i));
+        const double d0 = __dsub_rn(x.x, x0x), d1 = __dsub_rn(x.y, x0y), d2 = __dsub_rn(x.z, x0z);
         const double q = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
         // a non-finite displacement forces the rebuild, whose binning reports the position
         hit = hit || !(q <= e->trigger_sq);
@@ -315,6 +316,10 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
         float4 p = ld4f(a.pos32, i), pl = ld4f_cs(a.pos32lo, i);
         float4 v, vl, w, wl;
         load_vw<true, false>(a, i, v, vl, w, wl);
+        // the skin check's words with the state's, in the same round trip (the stores below could
+        // alias them as far as the compiler knows, so it would not hoist these loads above them)
+        const int32_t c = __ldcs(a.cell32 + i);
+        const float o0x = __ldcs(a.o0_32 + i), o0y = __ldcs(a.o0_32 + n + i), o0z = __ldcs(a.o0_32 + 2 * n + i);
         if (force_live(flags, i)) {  // an unflagged atom's force is an exact zero: nothing to add
             const float2 inv = __ldcs(reinterpret_cast<const float2*>(a.inv32) + i);  // 1/m, 1/I
             const float km = kick * inv.x, kI = kick * inv.y;
@@ -339,10 +344,9 @@ __device__ __forceinline__ void a32_body(const tmps_atoms& a, const tmps_box* __
         st4f_cs(a.pos32lo, i, pl);
         store_vw<true>(a, i, v, vl, w, wl);
         // displacement since the build: offset change + cell origin change
-        const int32_t c = __ldcs(a.cell32 + i);
-        const float d0 = ((p.x - __ldcs(a.o0_32 + i)) + pl.x) + (float)cell_x(c) * e->dh32[0] + e->dlo32[0];
-        const float d1 = ((p.y - __ldcs(a.o0_32 + n + i)) + pl.y) + (float)cell_y(c) * e->dh32[1] + e->dlo32[1];
-        const float d2 = ((p.z - __ldcs(a.o0_32 + 2 * n + i)) + pl.z) + (float)cell_z(c) * e->dh32[2] + e->dlo32[2];
+        const float d0 = ((p.x - o0x) + pl.x) + (float)cell_x(c) * e->dh32[0] + e->dlo32[0];
+        const float d1 = ((p.y - o0y) + pl.y) + (float)cell_y(c) * e->dh32[1] + e->dlo32[1];
+        const float d2 = ((p.z - o0z) + pl.z) + (float)cell_z(c) * e->dh32[2] + e->dlo32[2];
         const float q = (d0 * d0 + d1 * d1) + d2 * d2;
         hit = hit || !(q <= e->trigger32);  // NaN included (see a64_body)
         dd = q == q ? fmaxf(dd, q) : __int_as_float(0x7fffffff);
