@@ -1988,13 +1988,26 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
     const int n = a.n;
     if (i >= n) return;
     const double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
+    const bool mixed = e->mixed != 0;
+    // every load before the first store (a store could alias them as far as
+    // the compiler knows, and would hold each later load back a round trip)
+    double x0[3] = {0, 0, 0}, f[3] = {0, 0, 0}, t[3] = {0, 0, 0};
+    int lin = 0;
+    if (mixed) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            x0[k] = a.x0[k * n + i];
+            f[k] = a.f[k * n + i];
+            t[k] = a.torque[k * n + i];
+        }
+        lin = cell_of[i];
+    }
     if (a.rinv) {
         a.rinv[i] = 1.0 / v.w;
         a.rinv[n + i] = 1.0 / w.w;
     }
-    if (!e->mixed) return;
+    if (!mixed) return;
     const int gx = b->g[0], gxy = b->g[0] * b->g[1];
-    const int lin = cell_of[i];
     const int cz = lin / gxy, cy = (lin - cz * gxy) / gx, cx = lin - cz * gxy - cy * gx;
     const int cc[3] = {cx, cy, cz};
     const double xx[3] = {x.x, x.y, x.z};
@@ -2004,13 +2017,13 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
         split(xx[k] - origin, oh[k], ol[k]);
         // the skin check's reference: the position at the last build, as an
         // offset from the same origin (x0 is kept by the build in FP64)
-        a.o0_32[k * n + i] = f32_rn(a.x0[k * n + i] - origin);
+        a.o0_32[k * n + i] = f32_rn(x0[k] - origin);
     }
     a.cell32[i] = cx | (cy << 10) | (cz << 20);
     // the forces in hand (the setup forces at a run's start; at a rebuild C rewrites them first)
     for (int k = 0; k < 3; ++k) {
-        a.f32[k * n + i] = f32_rn(a.f[k * n + i]);
-        a.torque32[k * n + i] = f32_rn(a.torque[k * n + i]);
+        a.f32[k * n + i] = f32_rn(f[k]);
+        a.torque32[k * n + i] = f32_rn(t[k]);
     }
     float rh, rl;
     split(x.w, rh, rl);
@@ -2061,6 +2074,13 @@ __global__ void __launch_bounds__(kBlockA) k_unpack(tmps_atoms a, const tmps_box
     float4 vv, vl, ww, wl;
     load_vw<false>(a, i, vv, vl, ww, wl);
     const int32_t c = a.cell32[i];
+    // the FP32 forces with the rest, before any store (see k_prepare)
+    float f32[3], t32[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        f32[k] = a.f32[k * n + i];
+        t32[k] = a.torque32[k * n + i];
+    }
     const int cc[3] = {cell_x(c), cell_y(c), cell_z(c)};
     const float oh[3] = {p.x, p.y, p.z}, ol[3] = {pl.x, pl.y, pl.z};
     double xx[3];
@@ -2073,8 +2093,8 @@ __global__ void __launch_bounds__(kBlockA) k_unpack(tmps_atoms a, const tmps_box
     st4(a.vm, i, v);
     st4(a.om, i, w);
     for (int k = 0; k < 3; ++k) {
-        a.f[k * n + i] = f64_of(a.f32[k * n + i]);
-        a.torque[k * n + i] = f64_of(a.torque32[k * n + i]);
+        a.f[k * n + i] = f64_of(f32[k]);
+        a.torque[k * n + i] = f64_of(t32[k]);
     }
 }
 
