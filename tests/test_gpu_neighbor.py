@@ -113,6 +113,28 @@ def test_overflow_raises(gpu):
         nl.build(atom)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_overflow_raises_through_a_run(gpu, precision):
+    """Inside a run the build does not wait for the device: the overflow is read at the run's next
+    synchronisation and raised there, before any step's result is handed back; a deferred status is
+    read once (a later build or check does not raise it again)."""
+    import taichimps_gb300 as G
+    rng = np.random.default_rng(2)
+    x, r = dense_packing(rng, 216, 4.0, 0.5, 0.6)
+    dom = G.Domain(boxlo=[0.0] * 3, boxhi=[4.0] * 3)
+    atom = G.AtomSystem(max_atoms=216)
+    atom.add_particles(x=x, radius=r, density=2.5)
+    nl = G.NeighborList(domain=dom, skin=0.1, max_atoms=216, max_neighbors_per_atom=2)
+    hist = G.ContactHistory(max_atoms=216, max_neighbors=2)
+    pair = G.GranHertzHistory(domain=dom, kn=2e5, kt=2e5 * 2 / 7, gamman=50.0, gammat=25.0, xmu=0.5)
+    sim = G.Simulation(domain=dom, atom=atom, neighbor=nl, history=hist, pair=pair, dt=5e-5, precision=precision)
+    sim.add_fix(G.FixNVESphere(domain=dom))
+    with pytest.raises(RuntimeError, match="Neighbor list overflow"):
+        sim.run(5)
+    assert not nl.status_pending
+    nl.check_status()  # nothing left to raise
+
+
 def test_rebuild_is_deterministic(gpu):
     """The re-sorted layout depends only on positions: two builds agree bit for bit."""
     import taichimps_gb300 as G

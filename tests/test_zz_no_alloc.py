@@ -99,6 +99,48 @@ def test_noalloc_build_matches_workspace_build_twice(gpu):
         _same(_snapshot(out, n), want)
 
 
+def test_noalloc_build_replays_as_a_graph(gpu):
+    """After a first direct call (which looks the built-in scratch up), the build can be captured into
+    a CUDA graph -- no allocation happens inside it -- and the replay gives the workspace build's output."""
+    from taichimps_gb300 import _device, _lib
+    from taichimps_gb300.neighbor import morton_rank
+    L = _lib.load()
+    dom, atom, nl = _system(seed=5)
+    n, slots = atom.nlocal, nl.slots
+    ncell = int(np.prod(nl.grid_dim))
+    rank = torch.from_numpy(morton_rank(*[int(g) for g in nl.grid_dim])).to(atom.device)
+    src = atom.cstruct(atom.buffers)
+    ref = _outputs(atom, n, slots)
+    wsb = int(L.tmps_nlist_workspace_bytes(n, ncell))
+    ws = torch.zeros(wsb, dtype=torch.uint8, device=atom.device)
+    rc = L.tmps_nlist_build(src, atom.cstruct(ref["dst"]), dom.dbox, ncell, 0.1, rank.data_ptr(),
+                            ref["order"].data_ptr(), ref["cell_of"].data_ptr(), _nl_struct(ref, n, slots),
+                            ws.data_ptr(), wsb, ref["status"].data_ptr(), _device.stream())
+    assert rc == _lib.TMPS_OK
+    torch.cuda.synchronize()
+    want = _snapshot(ref, n)
+
+    def call(o):
+        return L.tmps_nlist_build_noalloc(src, atom.cstruct(o["dst"]), dom.dbox, ncell, 0.1, rank.data_ptr(),
+                                          o["order"].data_ptr(), o["cell_of"].data_ptr(), _nl_struct(o, n, slots),
+                                          o["status"].data_ptr(), _device.stream())
+
+    first = _outputs(atom, n, slots)
+    assert call(first) == _lib.TMPS_OK
+    torch.cuda.synchronize()
+    out = _outputs(atom, n, slots)
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.graph(g, stream=side):
+        rc = call(out)
+    torch.cuda.current_stream().wait_stream(side)
+    assert rc == _lib.TMPS_OK
+    g.replay()
+    torch.cuda.synchronize()
+    _same(_snapshot(out, n), want)
+
+
 def test_noalloc_build_refuses_sizes_beyond_its_scratch(gpu):
     """Checked on the host before anything is launched."""
     from taichimps_gb300 import _device, _lib
