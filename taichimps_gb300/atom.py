@@ -363,6 +363,10 @@ class AtomSystem:
         rmax = torch.empty(1, dtype=torch.float64, device=dev)
         rc = L.tmps_atoms_assemble(self.cstruct(nb), xt.data_ptr(), v_ptr, w_ptr, r_ptr, r_val, d_ptr, d_val,
                                    tag_ptr, rmax.data_ptr(), _device.stream())
+        if rc != _lib.TMPS_OK:
+            # nothing was added: back to the empty system before reporting
+            self._buf = self._alt = _empty_buffers(dev)
+            self.nlocal = 0
         _lib.check(rc, "tmps_atoms_assemble")
         # page-locked inputs are read in place: held until a synchronisation shows the kernel has run
         self._pending_inputs = keep
