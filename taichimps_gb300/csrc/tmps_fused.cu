@@ -177,6 +177,7 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
     const int32_t s = (int32_t)(e->step + 1);
     const double dt = e->dt, dtf = 0.5 * dt;
     const bool fin = e->final_pending != 0, remap = b->remap_pending != 0;
+    const float trig32 = approx_f32(e->trigger_sq);
     bool hit = false;
     float dd = 0.0f;
     double K[6] = {0, 0, 0, 0, 0, 0};
@@ -209,10 +210,24 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
         st4(a.vm, i, v);
         st4(a.om, i, w);
         const double d0 = __dsub_rn(x.x, x0x), d1 = __dsub_rn(x.y, x0y), d2 = __dsub_rn(x.z, x0z);
-        const double q = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
-        // a non-finite displacement forces the rebuild, whose binning reports the position
-        hit = hit || !(q <= e->trigger_sq);
-        dd = q == q ? fmaxf(dd, __double2float_ru(q)) : __int_as_float(0x7fffffff);
+        // |d|^2 first in FP32 from the truncated differences (integer operations;
+        // relative error under 1e-5): the exact FP64 test decides only within
+        // that margin of the trigger, or for a non-finite displacement
+        const float f0 = approx_f32(d0), f1 = approx_f32(d1), f2 = approx_f32(d2);
+        const float q32 = (f0 * f0 + f1 * f1) + f2 * f2;
+        bool far;
+        if (q32 < trig32 * 0.99998f) {
+            far = false;
+        } else if (q32 > trig32 * 1.00002f && q32 <= 3e38f) {
+            far = true;
+        } else {
+            const double q = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+            // a non-finite displacement forces the rebuild, whose binning reports the position
+            far = !(q <= e->trigger_sq);
+        }
+        hit = hit || far;
+        // the running maximum only has to bound |d|^2 from above (C's cull threshold)
+        dd = q32 == q32 ? fmaxf(dd, q32 * 1.00002f + 1e-30f) : __int_as_float(0x7fffffff);
         const double kin[6] = {(v.w * v.x) * v.x, (v.w * v.y) * v.y, (v.w * v.z) * v.z,
                                (v.w * v.x) * v.y, (v.w * v.x) * v.z, (v.w * v.y) * v.z};
 #pragma unroll
