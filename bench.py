@@ -161,16 +161,16 @@ def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float, flag
              72 + 72), reads m (kinetic term, 4), the offset at the last build (12) and the packed cell
              (4)                                                                                  = 164
              plus per flagged atom (`flagged` = fraction) the force and torque and 1/m, 1/I: 32
-      FP64:  reads x, v, omega (72), 1/m and 1/I (16), x at the last build (24); writes x, v, omega (72)
-             = 184, plus per flagged atom the force and torque: 48
+      FP64:  reads x, v, omega (72), x at the last build (24); writes x, v, omega (72)      = 168
+             plus per flagged atom the force and torque and 1/m, 1/I: 64
       A's records also carry per-build constants in their fourth lanes for C's gathers (radius hi and
-      lo, m), which it reads and writes with them (layout_bytes: 184 mixed / 232 FP64 per atom); those
+      lo, m), which it reads and writes with them (layout_bytes: 184 mixed / 216 FP64 per atom); those
       are not counted here.
     fused_c (C): the contact kernel's per-atom bytes, S + 4 n_nb + 52 n_c (own state read once and
       force written once, S = 84 mixed / 140 FP64; 4 per neighbor index; 4 partner + 48 shear per
       touching slot)."""
     if kernel == "fused_a":
-        return (164.0 + 32.0 * flagged) if precision == "mixed" else (184.0 + 48.0 * flagged)
+        return (164.0 + 32.0 * flagged) if precision == "mixed" else (168.0 + 64.0 * flagged)
     if kernel == "fused_c":
         return (84.0 if precision == "mixed" else 140.0) + 4.0 * n_nb + 52.0 * n_c
     return 0.0
@@ -179,7 +179,7 @@ def algorithmic_bytes(kernel: str, precision: str, n_nb: float, n_c: float, flag
 def layout_bytes(kernel: str, precision: str, flagged: float) -> float:
     """Bytes per atom A's record layout makes it read and write (see algorithmic_bytes)."""
     if kernel == "fused_a":
-        return (184.0 + 32.0 * flagged) if precision == "mixed" else (232.0 + 48.0 * flagged)
+        return (184.0 + 32.0 * flagged) if precision == "mixed" else (216.0 + 64.0 * flagged)
     return 0.0
 
 

@@ -226,7 +226,10 @@ typedef struct tmps_engine {
                               * after the first step that follows the bounds) */
     int64_t stop_step;       /* fused launches do nothing once step >= stop_step (batched runs) */
     int32_t touching;        /* atoms whose gap bound at the last tmps_fused_bounds is <= 0 */
-    int32_t pad4_;
+    int32_t kick_all;        /* set by tmps_fused_prepare when some 1/m or 1/I is not a positive
+                              * finite number (or dt <= 0): the FP64 update then kicks every atom;
+                              * else it skips the kick of an atom whose force and torque are exact
+                              * zeros (its C flag clear), which would leave it unchanged */
 } tmps_engine;
 
 /* One instance of a batched run (tmps_batch_*): the device state of one
@@ -419,7 +422,8 @@ int tmps_servo_step(tmps_box* d_box, tmps_servo* d_servo, const double* d_virial
  * d_eng->mixed, the split positions (offset from each atom's cell origin in
  * xr, cell32, FP32 copies, o0_32) and FP32 copies of f and torque into f32,
  * torque32.  `cell_of` is the linear cell id from tmps_nlist_build; records
- * lo0 / h0 in d_eng and clears d_eng->touching for tmps_fused_bounds. */
+ * lo0 / h0 in d_eng, clears d_eng->touching for tmps_fused_bounds and sets
+ * d_eng->kick_all. */
 int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* d_eng,
                        const int32_t* cell_of, void* stream);
 

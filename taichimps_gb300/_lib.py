@@ -106,7 +106,7 @@ class Engine(ctypes.Structure):
         ("shift_bound", ctypes.c_float), ("maxd2_bits", ctypes.c_uint32), ("cull", c_i32),
         ("cull_tol", ctypes.c_float),
         ("plog", ctypes.c_void_p), ("plog_len", c_i32), ("order_ready", c_i32),
-        ("stop_step", ctypes.c_int64), ("touching", c_i32), ("pad4_", c_i32),
+        ("stop_step", ctypes.c_int64), ("touching", c_i32), ("kick_all", c_i32),
     ]
 
 

@@ -160,11 +160,66 @@ __device__ __forceinline__ bool force_live(const uint32_t* __restrict__ flags, i
     return flags == nullptr || ((flags[i >> 5] >> (i & 31)) & 1u);
 }
 
+// A negative zero becomes a positive zero, every other value (NaN included)
+// is kept: the result of adding +0 to it, by integer operations.
+__device__ __forceinline__ double plus_zero(double x) {
+    const long long b = __double_as_longlong(x);
+    return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+}
+
+// Block sum of the FP64 update's six kinetic components by halving
+// exchanges: the FP64 pipe charges an instruction per warp however few lanes
+// use it, so a shuffle tree per component (30 additions per warp) costs as
+// much as several atoms' updates.  Padded to eight components, each exchange
+// keeps half of what a lane holds (4 + 2 + 1 + 1 + 1 = 9 additions per
+// warp), after which lane l holds component 4 b4 + 2 b3 + b2 (its lane bits
+// 4, 3, 2) of the warp's total.  Lanes 0..5 of warp 0 then add the warp
+// totals of their component in warp order and return the block's total; the
+// other threads return 0.  Fixed order: deterministic for a block size.
+__device__ __forceinline__ double block_sum6_halving(const double (&v)[6], double* smem /* [6][kBlockA / 32] */) {
+    constexpr int kW = kBlockA / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double a[8] = {v[0], v[1], v[2], v[3], v[4], v[5], 0.0, 0.0};
+    const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0, b2 = (lane & 4) != 0;
+    double r4[4], r2[2];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double send = b4 ? a[k] : a[4 + k], keep = b4 ? a[4 + k] : a[k];
+        r4[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const double send = b3 ? r4[k] : r4[2 + k], keep = b3 ? r4[2 + k] : r4[k];
+        r2[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    double r = (b2 ? r2[1] : r2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? r2[0] : r2[1], 4);
+    r += __shfl_xor_sync(0xffffffffu, r, 2);  // both lanes of a pair add the same two values
+    r += __shfl_xor_sync(0xffffffffu, r, 1);
+    const int c = (b4 ? 4 : 0) + (b3 ? 2 : 0) + (b2 ? 1 : 0);
+    if ((lane & 3) == 0 && c < 6) smem[c * kW + warp] = r;
+    __syncthreads();
+    double t = 0.0;
+    if (warp == 0 && lane < 6) {
+        t = smem[lane * kW];
+#pragma unroll
+        for (int w = 1; w < kW; ++w) t += smem[lane * kW + w];
+    }
+    return t;
+}
+
 // A runs as one resident wave striding over the atoms; besides the update
 // it sums the kinetic part of the virial, sum m v(t+dt/2) v(t+dt/2), over
 // every atom into per-block partials: an atom C finds contact-free ends the
 // step with that velocity, and C adds m (v(t+dt) v(t+dt) - v(t+dt/2)
 // v(t+dt/2)) for the rest (thermo.py:94-101).
+//
+// An atom whose flag bit is clear holds a force and torque of exact zeros:
+// with 1/m and 1/I positive and finite and dt > 0 (tmps_fused_prepare
+// records any exception in kick_all) its half-kicks v += (dt/2) (f/m) add +0
+// to each component, which changes a negative zero alone, so such an atom
+// takes plus_zero instead of the FP64 kick arithmetic (half of this kernel's
+// FP64 instructions) and its 1/m, 1/I are not read.  The results are the
+// kick's, bit for bit.
 __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __restrict__ b,
                                          tmps_engine* __restrict__ e, const uint32_t* __restrict__ flags,
                                          double* __restrict__ part, const int bid, const int nblk) {
@@ -177,6 +232,7 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
     const int32_t s = (int32_t)(e->step + 1);
     const double dt = e->dt, dtf = 0.5 * dt;
     const bool fin = e->final_pending != 0, remap = b->remap_pending != 0;
+    const bool kick_all = e->kick_all != 0 || !(dtf > 0.0);
     const float trig32 = approx_f32(e->trigger_sq);
     bool hit = false;
     float dd = 0.0f;
@@ -186,26 +242,32 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
         const int i = b0 + lane;
         if (i >= n) continue;
         double4 x = ld4(a.xr, i), v = ld4(a.vm, i), w = ld4(a.om, i);
-        const double im = __ldcs(a.rinv + i), iI = __ldcs(a.rinv + n + i);
         // the skin check's reference with the state (not after the stores, which might alias it)
         const double x0x = __ldcs(a.x0 + i), x0y = __ldcs(a.x0 + n + i), x0z = __ldcs(a.x0 + 2 * n + i);
-        double f[3] = {0.0, 0.0, 0.0}, t[3] = {0.0, 0.0, 0.0};
-        if (force_live(flags, i)) {
-            f[0] = __ldcs(a.f + i); f[1] = __ldcs(a.f + n + i); f[2] = __ldcs(a.f + 2 * n + i);
-            t[0] = __ldcs(a.torque + i); t[1] = __ldcs(a.torque + n + i); t[2] = __ldcs(a.torque + 2 * n + i);
-        }
-        if (fin) {  // second half-kick of the previous step
+        const bool live = force_live(flags, i);
+        if (live || kick_all) {
+            const double im = __ldcs(a.rinv + i), iI = __ldcs(a.rinv + n + i);
+            double f[3] = {0.0, 0.0, 0.0}, t[3] = {0.0, 0.0, 0.0};
+            if (live) {
+                f[0] = __ldcs(a.f + i); f[1] = __ldcs(a.f + n + i); f[2] = __ldcs(a.f + 2 * n + i);
+                t[0] = __ldcs(a.torque + i); t[1] = __ldcs(a.torque + n + i); t[2] = __ldcs(a.torque + 2 * n + i);
+            }
+            if (fin) {  // second half-kick of the previous step
+                v.x += dtf * (f[0] * im); v.y += dtf * (f[1] * im); v.z += dtf * (f[2] * im);
+                w.x += dtf * (t[0] * iI); w.y += dtf * (t[1] * iI); w.z += dtf * (t[2] * iI);
+            }
             v.x += dtf * (f[0] * im); v.y += dtf * (f[1] * im); v.z += dtf * (f[2] * im);
             w.x += dtf * (t[0] * iI); w.y += dtf * (t[1] * iI); w.z += dtf * (t[2] * iI);
+        } else {
+            v.x = plus_zero(v.x); v.y = plus_zero(v.y); v.z = plus_zero(v.z);
+            w.x = plus_zero(w.x); w.y = plus_zero(w.y); w.z = plus_zero(w.z);
         }
         if (remap) {  // remap x of the previous step's servo update
             x.x = b->lo[0] + (x.x - b->old_lo[0]) * e->remap_scale[0];
             x.y = b->lo[1] + (x.y - b->old_lo[1]) * e->remap_scale[1];
             x.z = b->lo[2] + (x.z - b->old_lo[2]) * e->remap_scale[2];
         }
-        v.x += dtf * (f[0] * im); v.y += dtf * (f[1] * im); v.z += dtf * (f[2] * im);
         x.x = x.x + dt * v.x; x.y = x.y + dt * v.y; x.z = x.z + dt * v.z;
-        w.x += dtf * (t[0] * iI); w.y += dtf * (t[1] * iI); w.z += dtf * (t[2] * iI);
         st4(a.xr, i, x);
         st4(a.vm, i, v);
         st4(a.om, i, w);
@@ -235,11 +297,8 @@ __device__ __forceinline__ void a64_body(const tmps_atoms& a, const tmps_box* __
     }
     if (__any_sync(0xffffffffu, hit) && lane == 0) e->disp_stamp = s;
     note_displacement(e, dd);
-    block_sum<6, kBlockA>(K, smem);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int c = 0; c < 6; ++c) part[(size_t)c * nb + bid] = K[c];
-    }
+    const double tot = block_sum6_halving(K, smem);
+    if (threadIdx.x < 6) part[(size_t)threadIdx.x * nb + bid] = tot;
 }
 
 __global__ void __launch_bounds__(kBlockA) k_a64(tmps_atoms a, const tmps_box* __restrict__ b,
@@ -1998,7 +2057,7 @@ __global__ void kb_state(const tmps_instance* __restrict__ inst, int ninst, int6
 // -------------------------------------------------------- prepare / unpack
 
 __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_box* __restrict__ b,
-                                                      const tmps_engine* __restrict__ e, const int32_t* cell_of) {
+                                                      tmps_engine* __restrict__ e, const int32_t* cell_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = a.n;
     if (i >= n) return;
@@ -2018,8 +2077,12 @@ __global__ void __launch_bounds__(kBlockA) k_prepare(tmps_atoms a, const tmps_bo
         lin = cell_of[i];
     }
     if (a.rinv) {
-        a.rinv[i] = 1.0 / v.w;
-        a.rinv[n + i] = 1.0 / w.w;
+        const double rm = 1.0 / v.w, rI = 1.0 / w.w;
+        a.rinv[i] = rm;
+        a.rinv[n + i] = rI;
+        // the FP64 update leaves out a zero force's kick only where 1/m and 1/I are positive and
+        // finite (0 * inf is a NaN; a negative factor would keep a negative zero velocity)
+        if (!(rm > 0.0 && isfinite(rm) && rI > 0.0 && isfinite(rI))) e->kick_all = 1;
     }
     if (!mixed) return;
     const int gx = b->g[0], gxy = b->g[0] * b->g[1];
@@ -2060,6 +2123,7 @@ __global__ void k_prepare_engine(const tmps_box* __restrict__ b, tmps_engine* e,
     e->part_off = part_off;
     e->cull = 0;  // until tmps_fused_bounds sets the bounds
     e->touching = 0;
+    e->kick_all = 0;  // k_prepare, launched next, sets it for an atom of odd mass or inertia
     e->maxd2_bits = 0u;
     e->shift_bound = 0.0f;
     for (int d = 0; d < 3; ++d) {
@@ -2333,12 +2397,12 @@ int tmps_fused_prepare(const tmps_atoms* a, const tmps_box* d_box, tmps_engine* 
                        void* stream) {
     if (!a || !d_box || !d_eng || !cell_of || a->n < 0) return TMPS_ERR_BAD_ARG;
     cudaStream_t s = (cudaStream_t)stream;
+    k_prepare_engine<<<1, 32, 0, s>>>(d_box, d_eng, (int64_t)part_offset(a->n));
+    note_launches(1);
     if (a->n > 0) {
         k_prepare<<<grid_for(a->n, kBlockA), kBlockA, 0, s>>>(*a, d_box, d_eng, cell_of);
         note_launches(1);
     }
-    k_prepare_engine<<<1, 32, 0, s>>>(d_box, d_eng, (int64_t)part_offset(a->n));
-    note_launches(1);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
 

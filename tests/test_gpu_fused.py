@@ -222,6 +222,48 @@ def test_contact_bound_culling_is_exact(gpu, oracle, precision):
         np.testing.assert_array_equal(states[0][k], states[1][k])
 
 
+def test_zero_force_kicks_left_out_exactly(gpu, oracle):
+    """The FP64 update leaves out the half-kicks of atoms whose force and torque
+    are exact zeros (C flag clear) and only turns a negative zero velocity
+    component into +0, as adding the zero kick would: the run is bit for bit
+    the one that kicks every atom (kick_all set on the device).  Negative zero
+    components are written into contact-free atoms mid-run, after the first
+    contact pass has cleared their flags."""
+    from taichimps_gb300 import _device, _lib
+    from taichimps_gb300.engine import FusedEngine
+    from taichimps_gb300.packing import make_packing
+    p = make_packing(2000, 0.9, 1.1, 0.40, seed=5, jitter=0.05, vel_sigma=0.1)
+    L = p["L"]
+    states = []
+    for kick_all in (False, True):
+        sim, _ = make_twin(oracle, p["x"], p["radius"], 2.5, [0.0] * 3, [L] * 3, v=p["v"], pair="hertz/history",
+                           dt=5e-5, cundall=(0.7, 0.7), skin=0.3)
+        sim.setup_run(80)
+        sim.init_simulation()
+        eng = FusedEngine(sim, "fp64", chunk=16, contact_path="screened")
+        eng.begin()
+        assert _device.pull_struct(eng._eng, _lib.Engine).kick_all == 0  # every 1/m, 1/I positive and finite
+        if kick_all:
+            e = _lib.Engine()
+            e.kick_all = 1
+            _device.push_fields(eng._eng, e, "kick_all", "kick_all")
+        eng.run(40)
+        vm, om = sim.atom._buf.vm, sim.atom._buf.om
+        vm[::7, 0] = -0.0
+        vm[3::11, 2] = -0.0
+        om[5::13, 1] = -0.0
+        eng.run(40)
+        eng.finish()
+        assert eng.rebuilds == 0  # a rebuild's prepare would reset kick_all
+        states.append(gpu_state(sim))
+    for k in ("x", "v", "omega", "f", "torque"):
+        a, b = (np.ascontiguousarray(s[k]).view(np.int64) for s in states)
+        np.testing.assert_array_equal(a, b, err_msg=k)
+    for k in ("v", "omega"):
+        z = states[0][k] == 0.0
+        assert z.any() and not np.signbit(states[0][k][z]).any(), k
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_pressure_record_each_step(gpu, oracle, precision):
     """record_pressure: every fused step writes the servo's pressure tensor to pinned host memory; the
