@@ -348,14 +348,14 @@ int tmps_nlist_build(const tmps_atoms* src, const tmps_atoms* dst, const tmps_bo
  * allocator (an allocation can synchronise the device and stall the loop),
  * or a foreign-language host that can only pass the arrays it registered.
  * Same arguments and results as tmps_nlist_build minus the workspace: the
- * scratch is one static device array built into the library (about 6.6 MB,
+ * scratch is one static device array built into the library (about 23 MB,
  * held by every GPU that loads the library until the process exits), so it
  * takes at most TMPS_NOALLOC_MAX_ATOMS atoms and TMPS_NOALLOC_MAX_CELLS grid
  * cells (the reference's own cell cap) and returns TMPS_ERR_TOO_LARGE beyond
- * that.  It calls no allocator.  It has no room for the FP32 copy of the
- * positions that lets tmps_nlist_build settle most candidate pairs in FP32,
- * so every candidate goes to the exact FP64 test: the same pair set, more
- * slowly.  The first call on a device looks up the scratch's device address
+ * that.  It calls no allocator.  It runs the kernels of tmps_nlist_build,
+ * the FP32 pre-test of the candidate pairs included (its cell-local offsets
+ * take 16 MB of the array): the same pair set at the same speed.  The first
+ * call on a device looks up the scratch's device address
  * (cudaGetSymbolAddress) and keeps it for the life of the process, so make
  * that first call before any stream capture, and do not use the library
  * across a cudaDeviceReset (the kept address belongs to the old context).

@@ -507,7 +507,8 @@ constexpr size_t kCountWords = kWords((size_t)TMPS_NOALLOC_MAX_CELLS * 4);
 constexpr size_t kStartWords = kWords(((size_t)TMPS_NOALLOC_MAX_CELLS + 1) * 4);
 constexpr size_t kFillWords = kWords((size_t)TMPS_NOALLOC_MAX_CELLS * 4);
 constexpr size_t kCellWords = kWords((size_t)TMPS_NOALLOC_MAX_ATOMS * 4);
-constexpr size_t kScratchWords = kCountWords + kStartWords + kFillWords + kCellWords;
+constexpr size_t kOffWords = kWords((size_t)TMPS_NOALLOC_MAX_ATOMS * 16);  // float4 cell-local offsets
+constexpr size_t kScratchWords = kCountWords + kStartWords + kFillWords + kCellWords + kOffWords;
 
 static __device__ __align__(256) int32_t g_build_scratch[kScratchWords];
 
@@ -547,6 +548,7 @@ extern "C" int tmps_nlist_build_noalloc(const tmps_atoms* src, const tmps_atoms*
     int32_t* start = count + kCountWords;
     int32_t* fill = start + kStartWords;
     int32_t* old_cell = fill + kFillWords;
+    float4* off32 = reinterpret_cast<float4*>(old_cell + kCellWords);  // 256-byte aligned
     cudaStream_t s = (cudaStream_t)stream;
     const int m = ncell;
     // the previous call left its counts behind: both counters must start at zero
@@ -558,8 +560,8 @@ extern "C" int tmps_nlist_build_noalloc(const tmps_atoms* src, const tmps_atoms*
     if (cudaMemsetAsync(fill, 0, (size_t)m * 4, s) != cudaSuccess) return TMPS_ERR_CUDA;
     k_scatter<<<gb, kBlock, 0, s>>>(n, cell_rank, old_cell, start, fill, order);
     k_cell_sort<<<grid_for(m, kBlock), kBlock, 0, s>>>(m, start, src->uid, order);
-    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, d_box, order, old_cell, cell_of, nullptr);
-    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, nullptr, d_status);
+    k_permute<<<gb, kBlock, 0, s>>>(*src, *dst, d_box, order, old_cell, cell_of, off32);
+    k_build<<<gb, kBlock, 0, s>>>(*dst, d_box, skin, cell_of, cell_rank, start, *nl, off32, d_status);
     note_launches(7);
     return launch_ok() ? TMPS_OK : TMPS_ERR_CUDA;
 }
